@@ -1,0 +1,27 @@
+#!/usr/bin/env bash
+# Builds the parity checker from the UNMODIFIED dCNS reference sources where they lie (read-only checkout),
+# plus oracle/ref_harness.cpp, into oracle/_ref/libdcns_ref.so.  Test infrastructure only.
+#
+#   -include cstdint : model/Matrix.cpp uses int32_t without including <cstdint> (GCC 13 rejects it otherwise)
+#   -mavx2           : selects the reference's AVX2 SmithWaterman (impl/sequenceAlignment3.cpp:223), the path its
+#                      shipped x86 binary runs; on a non-x86 host the scalar SmithWaterman_non_avx is selected by the
+#                      reference's own #ifdef, which needs an x86 <immintrin.h>, so the build is skipped there.
+set -euo pipefail
+REF="${DCNS_REFERENCE:-/root/reference}"
+HERE="$(cd "$(dirname "$0")" && pwd)"
+OUT="$HERE/_ref"
+if [ ! -d "$REF/impl" ]; then echo "build_ref: reference checkout not found at $REF; skipped"; exit 0; fi
+case "$(uname -m)" in x86_64) ;; *) echo "build_ref: non-x86 host; skipped"; exit 0;; esac
+mkdir -p "$OUT"
+SRCS="impl/sequenceAlignment3.cpp impl/findSimilarFragmentsForPairedSequence4.cpp impl/slidingWindowAlignment.cpp
+      impl/SequenceCharToUInt8.cpp model/Seed.cpp model/Matrix.cpp model/Score.cpp model/PairedSimilarFragment.cpp"
+OBJS=""
+for s in $SRCS; do
+  o="$OUT/$(echo "$s" | tr '/' '_').o"
+  g++ -O3 -funroll-all-loops -mavx2 -std=gnu++14 -include cstdint -fPIC -w -I"$REF" -c "$REF/$s" -o "$o" &
+  OBJS="$OBJS $o"
+done
+g++ -O2 -mavx2 -std=gnu++14 -include cstdint -fPIC -w -I"$REF" -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness.o" &
+wait
+g++ -shared -o "$OUT/libdcns_ref.so" $OBJS "$OUT/ref_harness.o"
+echo "build_ref: $OUT/libdcns_ref.so"

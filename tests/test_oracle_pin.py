@@ -1,0 +1,125 @@
+"""Pins the oracle restatement (oracle/dcns_oracle.cpp) to the reference: against the golden fixtures the reference
+generated (always), and against the live reference build where its checkout exists (skipped elsewhere)."""
+import numpy as np
+import pytest
+
+from conftest import ragged
+from dcns_gb300 import workloads as W
+
+
+def test_known_answer_inline_sequences(oracle, golden):
+    z = golden
+    for i in range(len(z["ka_sw"])):
+        a, b = ragged(z, "ka_a", i), ragged(z, "ka_b", i)
+        got = oracle.sw(a, b)
+        exp = tuple(int(v) for v in z["ka_sw"][i])
+        assert got[0] == exp[0]
+        if exp[1] != -7:  # the reference's scalar fallback reports no position unless asked twice
+            assert got == exp
+        x = oracle.xextend(a, b, cigar=True)
+        assert (x["score"], x["end1"], x["end2"], x["iii"], x["jjj"]) == tuple(int(v) for v in z["ka_xe"][i])
+        assert x["cigar"] == [int(c) for c in ragged(z, "ka_cigar", 2 * i)]
+        g = oracle.semiglobal(a, b, cigar=True, open2=-80, ext2=-1, zdrop=100, bandwidth=100)
+        assert (g["score"], g["end1"], g["end2"]) == tuple(int(v) for v in z["ka_sg"][i])
+        assert g["cigar"] == [int(c) for c in ragged(z, "ka_cigar", 2 * i + 1)]
+
+
+def test_sw_golden(oracle, golden):
+    z = golden
+    for i in range(len(z["sw_exp"])):
+        a, b = ragged(z, "sw_a", i), ragged(z, "sw_b", i)
+        o, e, m, x = (int(v) for v in z["sw_prm"][i])
+        got = oracle.sw(a, b, o, e, m, x)
+        exp = tuple(int(v) for v in z["sw_exp"][i])
+        assert got[0] == exp[0], i
+        if exp[0] > 0 and exp[1] != -7:
+            assert got == exp, i
+
+
+def test_xextend_golden(oracle, golden):
+    z = golden
+    for i in range(len(z["xe_exp"])):
+        a, b = ragged(z, "xe_a", i), ragged(z, "xe_b", i)
+        w, xd, cig = (int(v) for v in z["xe_prm"][i])
+        r = oracle.xextend(a, b, xdrop=xd, w=w, cigar=bool(cig))
+        assert (r["score"], r["end1"], r["end2"], r["iii"], r["jjj"]) == tuple(int(v) for v in z["xe_exp"][i]), i
+        assert r["cigar"] == [int(c) for c in ragged(z, "xe_cigar", i)], i
+
+
+def test_semiglobal_golden(oracle, golden):
+    z = golden
+    for i in range(len(z["sg_exp"])):
+        a, b = ragged(z, "sg_a", i), ragged(z, "sg_b", i)
+        bw, zd, o2, e2, cig = (int(v) for v in z["sg_prm"][i])
+        r = oracle.semiglobal(a, b, cigar=bool(cig), bandwidth=bw, zdrop=zd, open2=o2, ext2=e2)
+        assert (r["score"], r["end1"], r["end2"]) == tuple(int(v) for v in z["sg_exp"][i]), i
+        assert r["cigar"] == [int(c) for c in ragged(z, "sg_cigar", i)], i
+
+
+def _golden_fragments(z, name):
+    out, k = [], 0
+    for n in z[name + "_nfrag"]:
+        fr = []
+        for _ in range(int(n)):
+            f = tuple(int(v) for v in z[name + "_frag"][k])
+            cg = tuple(int(c) for c in ragged(z, name + "_cigar", k))
+            fr.append((f + (cg,), tuple(float(v) for v in z[name + "_pe"][k])))
+            k += 1
+        out.append(fr)
+    return out
+
+
+@pytest.mark.parametrize("name,two_gap", [("p1", False), ("p2", True)])
+def test_pipeline_golden(oracle, golden, name, two_gap):
+    z = golden
+    exp_all = _golden_fragments(z, name)
+    for i, exp in enumerate(exp_all):
+        a, b = ragged(z, "pp_a", i), ragged(z, "pp_b", i)
+        got, _ = oracle.find(a, b, two_gap=two_gap)
+        assert [f.key() for f in got] == [e[0] for e in exp], (name, i)
+        # p/e-values are FP64 from identical integer scores; exp() may differ by an ulp across libm builds
+        for f, e in zip(got, exp):
+            assert f.pvalue == pytest.approx(e[1][0], rel=1e-12, abs=0)
+            assert f.evalue == pytest.approx(e[1][1], rel=1e-12, abs=0)
+
+
+def test_seed_sets_golden(oracle, golden):
+    z = golden
+    kr = kl = 0
+    for i in range(len(z["seeds_nraw"])):
+        a, b = ragged(z, "pp_a", i), ragged(z, "pp_b", i)
+        raw, lk = oracle.seeds(a, b)
+        nr, nl = int(z["seeds_nraw"][i]), int(z["seeds_nlinked"][i])
+        assert raw == [tuple(int(v) for v in r) for r in z["seeds_raw"][kr:kr + nr]], i
+        assert lk == [tuple(int(v) for v in r) for r in z["seeds_linked"][kl:kl + nl]], i
+        kr += nr
+        kl += nl
+
+
+def test_sliding_golden(oracle, golden):
+    z = golden
+    seqs = [ragged(z, "sl_seq", i) for i in range(len(z["sl_seq_off"]) - 1)]
+    rows = {(int(j), int(i)): str(t) for (j, i), t in zip(z["sl_rows"], z["sl_text"])}
+    for i in range(1, len(seqs)):
+        sc, _ = oracle.sliding(seqs[0], seqs[i])
+        for k, v in enumerate(sc):
+            assert "%g" % v == rows[(k * 8, i)], (i, k)
+
+
+def test_live_reference_random(oracle, reference):
+    """Fresh random cases against the live reference build (skipped where the reference is absent)."""
+    rng = np.random.default_rng(99)
+    for _ in range(300):
+        a, b = W.random_pair(rng, int(rng.integers(0, 150)), int(rng.integers(0, 50)), alphabet=5)
+        x, y = oracle.sw(a, b), reference.sw(a, b)
+        assert x[0] == y[0] and (x[0] == 0 or x == y)
+    for _ in range(6):
+        x, y = W.planted_pair(rng, int(rng.integers(100, 1500)), int(rng.integers(50, 1500)), 5, 30, 200, 0.7, 0.98,
+                              0.01, 0.1)
+        a, b = W.prepare(x), W.prepare(y)
+        for tg in (False, True):
+            if tg and len(b) < 8:
+                continue  # the reference's 2-gap window loop aborts on queries shorter than one step (bad_alloc)
+            got, _ = oracle.find(a, b, two_gap=tg)
+            exp = reference.find(a, b, two_gap=tg)
+            assert [f.key() for f in got] == [f.key() for f in exp]
