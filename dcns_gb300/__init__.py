@@ -1,0 +1,351 @@
+"""dcns_gb300 — GB300-native pairwise CNS alignment (dCNS's seed scan, x-drop extension and 2-piece semi-global DP).
+
+The engine is a C-ABI shared library (``include/dcns_gb300.h``, built from ``dcns_gb300/csrc`` for sm_103a) driven
+through ctypes.  This module builds it in-tree, loads it, and mirrors the reference's entry points:
+
+* :meth:`Engine.findSimilarFragmentsForPairedSequence` — the 1-gap / 2-gap overloads
+  (impl/findSimilarFragmentsForPairedSequence.h:26-42 of the reference) for one pair,
+* :meth:`Engine.align_pairs` — the batched form (many independent pairs in one call),
+* :meth:`Engine.SmithWaterman`, :meth:`Engine.SemiGlobal_xextend`, :meth:`Engine.SemiGlobal` and
+  :meth:`Engine.slidingWindowAlignment` — the kernel-level functions (impl/sequenceAlignment.h:18-88,
+  impl/slidingWindowAlignment.h:21-24).
+
+There is no CPU fallback: :func:`load` raises when the library is missing or no CUDA device is usable.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+LIBDIR = os.path.join(HERE, "_lib")
+LIB = os.path.join(LIBDIR, "libdcnsgpu.so")
+INCLUDE = os.path.join(ROOT, "include")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+MODE_ONE_GAP = 1
+MODE_TWO_GAP = 2
+
+ERRORS = {-1: "invalid argument", -2: "out of memory", -3: "device error", -4: "timeout", -5: "not found",
+          -6: "busy"}
+
+
+class DcnsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _sources():
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+
+
+def _headers():
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    return hs + [os.path.join(INCLUDE, "dcns_gb300.h")]
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile every CUDA/C++ source for sm_103a into dcns_gb300/_lib/libdcnsgpu.so (in-tree, parallel)."""
+    os.makedirs(LIBDIR, exist_ok=True)
+    srcs = _sources()
+    newest = max(os.path.getmtime(p) for p in srcs + _headers())
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    nvcc = os.environ.get("NVCC", "nvcc")
+    common = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC] + ARCH
+
+    def compile_one(src):
+        obj = os.path.join(LIBDIR, os.path.basename(src) + ".o")
+        cmd = [nvcc] + common + ["-c", src, "-o", obj]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
+        if verbose and r.stderr:
+            print(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    tmp = LIB + ".tmp"
+    r = subprocess.run([nvcc, "-shared"] + ARCH + objs + ["-o", tmp, "-lpthread"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+# ------------------------------------------------------------------ ctypes mirror of include/dcns_gb300.h
+class Params(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("match", "mismatch", "open1", "ext1", "open2", "ext2", "window",
+                                         "min_score", "step", "w", "xdrop", "zdrop", "bandwidth",
+                                         "max_align_len")] + [("pvalue", C.c_double), ("lambda_", C.c_double),
+                                                              ("kvalue", C.c_double)]
+
+
+class Pair(C.Structure):
+    _fields_ = [("seq1", C.POINTER(C.c_int8)), ("len1", C.c_int32), ("seq2", C.POINTER(C.c_int8)),
+                ("len2", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("cells_scan", "cells_scan_reverse", "cells_xdrop", "cells_semiglobal",
+                                         "tasks_scan", "tasks_scan_speculative", "seeds", "xdrop_passes",
+                                         "semiglobal_dps")] + \
+               [(n, C.c_double) for n in ("ms_upload", "ms_scan", "ms_replay", "ms_xdrop", "ms_semiglobal",
+                                          "ms_download", "ms_total", "ms_scan_kernel")] + \
+               [("scan_launches", C.c_int32), ("kernel_launches", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Results(C.Structure):
+    _fields_ = [("n_pairs", C.c_int64), ("n_fragments", C.c_int64), ("n_cigar", C.c_int64),
+                ("pair_offset", C.POINTER(C.c_int64)), ("frag", C.POINTER(C.c_int64)),
+                ("pvalue", C.POINTER(C.c_double)), ("evalue", C.POINTER(C.c_double)),
+                ("cigar", C.POINTER(C.c_uint32)), ("stats", Stats)]
+
+
+@dataclass
+class Fragment:
+    """PairedSimilarFragment (model/PairedSimilarFragment.h:14 of the reference): 1-based coordinates, uint32 score,
+    CIGAR words (length << 4 | op; op 0=M, 1=I, 2=D), FP64 p- and e-value."""
+    start1: int
+    end1: int
+    start2: int
+    end2: int
+    score: int
+    cigar: list = field(default_factory=list)
+    pvalue: float = 0.0
+    evalue: float = 0.0
+
+    def key(self):
+        return (self.start1, self.end1, self.start2, self.end2, self.score, tuple(self.cigar))
+
+
+_I8P = C.POINTER(C.c_int8)
+_I32P = C.POINTER(C.c_int32)
+_I64P = C.POINTER(C.c_int64)
+_U32P = C.POINTER(C.c_uint32)
+_F64P = C.POINTER(C.c_double)
+
+
+def _bind(lib):
+    P = C.POINTER
+    lib.dcns_params_default.argtypes = [P(Params)]
+    lib.dcns_ctx_create.argtypes = [C.c_int, C.c_size_t, P(C.c_void_p)]
+    lib.dcns_ctx_destroy.argtypes = [C.c_void_p]
+    lib.dcns_last_error.argtypes = [C.c_void_p]
+    lib.dcns_last_error.restype = C.c_char_p
+    lib.dcns_ctx_stream.argtypes = [C.c_void_p]
+    lib.dcns_ctx_stream.restype = C.c_void_p
+    lib.dcns_align_pairs.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(Params), C.c_int, P(P(Results))]
+    lib.dcns_results_free.argtypes = [P(Results)]
+    lib.dcns_last_stats.argtypes = [C.c_void_p, P(Stats)]
+    lib.dcns_smith_waterman_batch.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(Params), _I32P]
+    lib.dcns_xextend_batch.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(Params), C.c_int, _I32P, _U32P, C.c_int64,
+                                       _I64P]
+    lib.dcns_semiglobal_batch.argtypes = lib.dcns_xextend_batch.argtypes
+    lib.dcns_sliding_window.argtypes = [C.c_void_p, P(_I8P), _I32P, C.c_int32, P(Params), _F64P, _I32P]
+    lib.dcns_serve_start.argtypes = [C.c_void_p, P(Params), C.c_int, C.c_int]
+    lib.dcns_submit.argtypes = [C.c_void_p, P(Pair), P(C.c_uint64)]
+    lib.dcns_poll.argtypes = [C.c_void_p, C.c_uint64, P(P(Results))]
+    lib.dcns_serve_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_int64, P(P(Results))]
+    lib.dcns_serve_stop.argtypes = [C.c_void_p]
+    return lib
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def library():
+    """The loaded C-ABI library (raises if it was not built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB):
+                raise RuntimeError(f"{LIB} is missing: call dcns_gb300.build() (no CPU fallback exists)")
+            _lib = _bind(C.CDLL(LIB))
+    return _lib
+
+
+def params(**kw) -> Params:
+    p = Params()
+    library().dcns_params_default(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, "lambda_" if k == "lambda" else k, v)
+    return p
+
+
+def _codes(a):
+    a = np.ascontiguousarray(a, dtype=np.int8)
+    return a
+
+
+def _pairs(pairs):
+    keep = [(_codes(a), _codes(b)) for a, b in pairs]
+    arr = (Pair * max(1, len(keep)))()
+    for k, (a, b) in enumerate(keep):
+        arr[k].seq1 = a.ctypes.data_as(_I8P)
+        arr[k].len1 = len(a)
+        arr[k].seq2 = b.ctypes.data_as(_I8P)
+        arr[k].len2 = len(b)
+    return arr, keep
+
+
+def _unpack(res, nonempty=True):
+    R = res.contents
+    n = int(R.n_pairs)
+    out = []
+    if n == 0:
+        return out
+    off = np.ctypeslib.as_array(R.pair_offset, shape=(n + 1,)).copy()
+    nf = int(R.n_fragments)
+    frag = np.ctypeslib.as_array(R.frag, shape=(max(nf, 1) * 7,))[:nf * 7].reshape(nf, 7).copy() if nf else \
+        np.zeros((0, 7), np.int64)
+    pv = np.ctypeslib.as_array(R.pvalue, shape=(max(nf, 1),))[:nf].copy() if nf else np.zeros(0)
+    ev = np.ctypeslib.as_array(R.evalue, shape=(max(nf, 1),))[:nf].copy() if nf else np.zeros(0)
+    nc = int(R.n_cigar)
+    cg = np.ctypeslib.as_array(R.cigar, shape=(max(nc, 1),))[:nc].copy() if nc else np.zeros(0, np.uint32)
+    for k in range(n):
+        fr = []
+        for i in range(int(off[k]), int(off[k + 1])):
+            r = frag[i]
+            fr.append(Fragment(int(r[0]), int(r[1]), int(r[2]), int(r[3]), int(r[4]),
+                               [int(c) for c in cg[int(r[5]):int(r[5]) + int(r[6])]], float(pv[i]), float(ev[i])))
+        out.append(fr)
+    return out
+
+
+class Engine:
+    """One device context (stream + device buffers) of the engine."""
+
+    def __init__(self, device: int = 0, mem_budget: int = 0):
+        self.lib = library()
+        h = C.c_void_p()
+        rc = self.lib.dcns_ctx_create(device, mem_budget, C.byref(h))
+        if rc != 0:
+            raise DcnsError(rc, "could not create a context on cuda:%d (the engine needs an sm_103a GPU)" % device)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dcns_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise DcnsError(rc, self.lib.dcns_last_error(self.h).decode(errors="replace"))
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.dcns_ctx_stream(self.h) or 0)
+
+    def last_stats(self) -> dict:
+        s = Stats()
+        self._check(self.lib.dcns_last_stats(self.h, C.byref(s)))
+        return s.as_dict()
+
+    # -------------------------------------------------------------- whole path
+    def align_pairs(self, pairs, mode=MODE_ONE_GAP, **kw):
+        """Align many independent (seq1 codes, seq2 codes) pairs; returns one fragment list per pair."""
+        arr, keep = _pairs(pairs)
+        p = params(**kw)
+        res = C.POINTER(Results)()
+        self._check(self.lib.dcns_align_pairs(self.h, arr, len(keep), C.byref(p), mode, C.byref(res)))
+        try:
+            return _unpack(res)
+        finally:
+            self.lib.dcns_results_free(res)
+
+    def findSimilarFragmentsForPairedSequence(self, seq1, seq2, two_gap=False, **kw):
+        """One pair, the reference's 1-gap (default) or 2-gap overload."""
+        return self.align_pairs([(seq1, seq2)], MODE_TWO_GAP if two_gap else MODE_ONE_GAP, **kw)[0]
+
+    # -------------------------------------------------------------- kernel-level
+    def SmithWaterman(self, tasks, **kw):
+        """SmithWaterman(ref, read, ...) per (ref, read) task -> int32 array [n, 3] (max, end1, end2)."""
+        arr, keep = _pairs(tasks)
+        out = np.zeros((max(1, len(keep)), 3), np.int32)
+        self._check(self.lib.dcns_smith_waterman_batch(self.h, arr, len(keep), C.byref(params(**kw)),
+                                                       out.ctypes.data_as(_I32P)))
+        return out[:len(keep)]
+
+    def _banded(self, fn, tasks, width, want_cigar, kw):
+        arr, keep = _pairs(tasks)
+        n = len(keep)
+        out = np.zeros((max(1, n), width), np.int32)
+        cap = sum(len(a) + len(b) + 4 for a, b in keep) + 4
+        cig = np.zeros(cap, np.uint32)
+        off = np.zeros(n + 1, np.int64)
+        self._check(fn(self.h, arr, n, C.byref(params(**kw)), int(want_cigar), out.ctypes.data_as(_I32P),
+                       cig.ctypes.data_as(_U32P), cap, off.ctypes.data_as(_I64P)))
+        cigars = [[int(c) for c in cig[off[k]:off[k + 1]]] for k in range(n)]
+        return out[:n], cigars
+
+    def SemiGlobal_xextend(self, tasks, cigar=False, **kw):
+        """x-drop extension per (seq1, seq2) task -> ([n, 6] = max, end1, end2, iii, jjj, ncigar; cigars)."""
+        return self._banded(self.lib.dcns_xextend_batch, tasks, 6, cigar, kw)
+
+    def SemiGlobal(self, tasks, cigar=False, **kw):
+        """2-piece affine semi-global per task -> ([n, 4] = max, end1, end2, ncigar; cigars)."""
+        return self._banded(self.lib.dcns_semiglobal_batch, tasks, 4, cigar, kw)
+
+    def slidingWindowAlignment(self, seqs, **kw):
+        """Per-window scores of seqs[0] against each other sequence: (score [n-1, n_windows], max [n-1, n_windows])."""
+        keep = [_codes(s) for s in seqs]
+        ptrs = (_I8P * len(keep))(*[s.ctypes.data_as(_I8P) for s in keep])
+        lens = np.array([len(s) for s in keep], np.int32)
+        p = params(**kw)
+        nw = (len(keep[0]) + p.step - 1) // p.step
+        sc = np.zeros((max(1, len(keep) - 1), max(nw, 1)), np.float64)
+        mx = np.zeros_like(sc, dtype=np.int32)
+        self._check(self.lib.dcns_sliding_window(self.h, ptrs, lens.ctypes.data_as(_I32P), len(keep), C.byref(p),
+                                                 sc.ctypes.data_as(_F64P), mx.ctypes.data_as(_I32P)))
+        return sc[:len(keep) - 1, :nw], mx[:len(keep) - 1, :nw]
+
+    # -------------------------------------------------------------- serving loop
+    def serve_start(self, mode=MODE_ONE_GAP, max_inflight=256, **kw):
+        self._serve_params = params(**kw)
+        self._check(self.lib.dcns_serve_start(self.h, C.byref(self._serve_params), mode, max_inflight))
+
+    def submit(self, seq1, seq2) -> int:
+        arr, keep = _pairs([(seq1, seq2)])
+        t = C.c_uint64()
+        self._check(self.lib.dcns_submit(self.h, arr, C.byref(t)))
+        return int(t.value)
+
+    def wait(self, ticket: int, timeout_ms: int = 600000):
+        res = C.POINTER(Results)()
+        self._check(self.lib.dcns_serve_wait(self.h, ticket, timeout_ms, C.byref(res)))
+        try:
+            return _unpack(res)[0]
+        finally:
+            self.lib.dcns_results_free(res)
+
+    def serve_stop(self):
+        self._check(self.lib.dcns_serve_stop(self.h))
+
+
+def load(device: int = 0, mem_budget: int = 0) -> Engine:
+    """Build (if needed) and open an engine on cuda:<device>."""
+    build()
+    return Engine(device, mem_budget)

@@ -1,0 +1,403 @@
+// C ABI of the engine (include/dcns_gb300.h).  Every entry point converts C++ exceptions into status codes and keeps
+// the message in the context.
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+
+#include "engine.h"
+
+using namespace dcns;
+
+struct ResultsImpl {
+  dcns_results pub{};
+  std::vector<int64_t> off, frag;
+  std::vector<double> pv, ev;
+  std::vector<uint32_t> cig;
+  void finish(const std::vector<std::vector<FragOut>> &fr, const dcns_stats &st) {
+    off.assign(fr.size() + 1, 0);
+    int64_t nf = 0, nc = 0;
+    for (size_t k = 0; k < fr.size(); ++k) {
+      nf += (int64_t)fr[k].size();
+      for (auto &f : fr[k]) nc += (int64_t)f.cigar.size();
+      off[k + 1] = nf;
+    }
+    frag.resize(nf * 7);
+    pv.resize(nf);
+    ev.resize(nf);
+    cig.resize(nc);
+    int64_t i = 0, c = 0;
+    for (auto &v : fr)
+      for (auto &f : v) {
+        int64_t *r = frag.data() + i * 7;
+        r[0] = f.s1, r[1] = f.e1, r[2] = f.s2, r[3] = f.e2, r[4] = f.score, r[5] = c, r[6] = (int64_t)f.cigar.size();
+        pv[i] = f.p;
+        ev[i] = f.e;
+        std::memcpy(cig.data() + c, f.cigar.data(), f.cigar.size() * sizeof(uint32_t));
+        c += (int64_t)f.cigar.size();
+        ++i;
+      }
+    pub.n_pairs = (int64_t)fr.size();
+    pub.n_fragments = nf;
+    pub.n_cigar = nc;
+    pub.pair_offset = off.data();
+    pub.frag = frag.data();
+    pub.pvalue = pv.data();
+    pub.evalue = ev.data();
+    pub.cigar = cig.data();
+    pub.stats = st;
+  }
+};
+
+static_assert(offsetof(ResultsImpl, pub) == 0, "dcns_results must be the first member");
+
+// ---------------------------------------------------------------- serving state
+struct Server {
+  Params P{};
+  int mode = DCNS_MODE_ONE_GAP;
+  int max_inflight = 256;
+  bool running = false;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  struct Req {
+    uint64_t ticket;
+    std::vector<int8_t> s1, s2;
+  };
+  std::deque<Req> queue;
+  std::unordered_map<uint64_t, ResultsImpl *> done;
+  std::unordered_map<uint64_t, std::string> failed;
+  uint64_t next = 1;
+  std::vector<std::unique_ptr<Context>> lanes;  // one pipeline (stream + buffers) per worker
+  std::vector<std::thread> workers;
+};
+
+struct dcns_ctx {
+  Context C;
+  std::unique_ptr<Server> srv;
+};
+
+namespace {
+
+int fail(dcns_ctx *ctx, const Error &e) {
+  if (ctx) ctx->C.err = e.what();
+  return e.code;
+}
+
+template <class F>
+int guarded(dcns_ctx *ctx, F f) {
+  try {
+    f();
+    return DCNS_OK;
+  } catch (const Error &e) {
+    return fail(ctx, e);
+  } catch (const std::bad_alloc &) {
+    if (ctx) ctx->C.err = "host allocation failed";
+    return DCNS_ERR_NOMEM;
+  } catch (const std::exception &e) {
+    if (ctx) ctx->C.err = e.what();
+    return DCNS_ERR_DEVICE;
+  }
+}
+
+void init_context(Context &C, int device, size_t budget) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    (void)cudaGetLastError();
+    throw Error(DCNS_ERR_DEVICE, "no CUDA device available (this library has no CPU fallback)");
+  }
+  if (device < 0 || device >= ndev) throw Error(DCNS_ERR_INVALID, "device ordinal out of range");
+  DCNS_CK(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  DCNS_CK(cudaGetDeviceProperties(&prop, device));
+  if (prop.major < 10) throw Error(DCNS_ERR_DEVICE, "this build targets sm_103a (GB300); found sm_" +
+                                                        std::to_string(prop.major * 10 + prop.minor));
+  C.device = device;
+  C.nsm = prop.multiProcessorCount;
+  C.scan_blocks_per_sm = scan_occupancy();
+  DCNS_CK(cudaStreamCreateWithFlags(&C.st, cudaStreamNonBlocking));
+  DCNS_CK(cudaEventCreate(&C.ev0));
+  DCNS_CK(cudaEventCreate(&C.ev1));
+  if (budget == 0) {
+    size_t fr = 0, tot = 0;
+    DCNS_CK(cudaMemGetInfo(&fr, &tot));
+    budget = fr / 10 * 8;
+  }
+  C.budget = budget;
+}
+
+std::vector<PairIn> to_pairs(const dcns_pair *pairs, int64_t n) {
+  if (n < 0 || (n > 0 && !pairs)) throw Error(DCNS_ERR_INVALID, "bad pair array");
+  std::vector<PairIn> v((size_t)n);
+  for (int64_t k = 0; k < n; ++k) v[k] = PairIn{pairs[k].seq1, pairs[k].len1, pairs[k].seq2, pairs[k].len2};
+  return v;
+}
+
+void worker_loop(Server *S, Context *C) {
+  DCNS_CK(cudaSetDevice(C->device));
+  for (;;) {
+    std::vector<Server::Req> batch;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_work.wait(lk, [&] { return !S->running || !S->queue.empty(); });
+      if (!S->running && S->queue.empty()) return;
+      // admit whatever arrived, up to the in-flight limit
+      while (!S->queue.empty() && (int)batch.size() < S->max_inflight) {
+        batch.push_back(std::move(S->queue.front()));
+        S->queue.pop_front();
+      }
+    }
+    std::vector<PairIn> pairs;
+    for (auto &r : batch) pairs.push_back(PairIn{r.s1.data(), (int32_t)r.s1.size(), r.s2.data(), (int32_t)r.s2.size()});
+    // admission by device memory: a batch that does not fit is split until it does
+    std::vector<std::pair<size_t, size_t>> parts{{0, pairs.size()}};
+    while (!parts.empty()) {
+      auto [a, b] = parts.back();
+      parts.pop_back();
+      std::vector<PairIn> sub(pairs.begin() + a, pairs.begin() + b);
+      std::vector<std::vector<FragOut>> out;
+      std::string err;
+      try {
+        align_pairs(*C, sub, S->P, S->mode, out);
+      } catch (const Error &e) {
+        if (e.code == DCNS_ERR_NOMEM && b - a > 1) {
+          parts.push_back({a, a + (b - a) / 2});
+          parts.push_back({a + (b - a) / 2, b});
+          continue;
+        }
+        err = e.what();
+      } catch (const std::exception &e) {
+        err = e.what();
+      }
+      std::lock_guard<std::mutex> lk(S->mu);
+      for (size_t k = a; k < b; ++k) {
+        if (!err.empty()) {
+          S->failed[batch[k].ticket] = err;
+        } else {
+          auto *R = new ResultsImpl;
+          std::vector<std::vector<FragOut>> one{std::move(out[k - a])};
+          R->finish(one, C->stats);
+          S->done[batch[k].ticket] = R;
+        }
+      }
+      S->cv_done.notify_all();
+    }
+  }
+}
+
+}  // namespace
+
+namespace dcns {
+int scan_occupancy_impl();
+int scan_occupancy() { return scan_occupancy_impl(); }
+}  // namespace dcns
+
+extern "C" {
+
+void dcns_params_default(dcns_params *p) {
+  if (!p) return;
+  p->match = 2;
+  p->mismatch = -3;
+  p->open1 = -4;
+  p->ext1 = -2;
+  p->open2 = -45;
+  p->ext2 = 0;
+  p->window = 38;
+  p->min_score = 40;
+  p->step = 8;
+  p->w = 10;
+  p->xdrop = 20;
+  p->zdrop = 50;
+  p->bandwidth = 20000;
+  p->max_align_len = 0;
+  p->pvalue = 0.1;
+  p->lambda = 0.382291;
+  p->kvalue = 0.006662;
+}
+
+int dcns_ctx_create(int device, size_t mem_budget, dcns_ctx **out) {
+  if (!out) return DCNS_ERR_INVALID;
+  *out = nullptr;
+  auto *ctx = new dcns_ctx;
+  try {
+    init_context(ctx->C, device, mem_budget);
+  } catch (const Error &e) {
+    delete ctx;
+    return e.code;
+  }
+  *out = ctx;
+  return DCNS_OK;
+}
+
+void dcns_ctx_destroy(dcns_ctx *ctx) {
+  if (!ctx) return;
+  dcns_serve_stop(ctx);
+  delete ctx;
+}
+
+const char *dcns_last_error(const dcns_ctx *ctx) { return ctx ? ctx->C.err.c_str() : "null context"; }
+
+void *dcns_ctx_stream(dcns_ctx *ctx) { return ctx ? (void *)ctx->C.st : nullptr; }
+
+int dcns_align_pairs(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, const dcns_params *params, int mode,
+                     dcns_results **out) {
+  if (!ctx || !params || !out) return DCNS_ERR_INVALID;
+  *out = nullptr;
+  return guarded(ctx, [&] {
+    std::vector<PairIn> v = to_pairs(pairs, n_pairs);
+    std::vector<std::vector<FragOut>> fr;
+    align_pairs(ctx->C, v, to_params(params), mode, fr);
+    auto *R = new ResultsImpl;
+    R->finish(fr, ctx->C.stats);
+    *out = &R->pub;
+  });
+}
+
+void dcns_results_free(dcns_results *res) { delete reinterpret_cast<ResultsImpl *>(res); }
+
+int dcns_last_stats(const dcns_ctx *ctx, dcns_stats *out) {
+  if (!ctx || !out) return DCNS_ERR_INVALID;
+  *out = ctx->C.stats;
+  return DCNS_OK;
+}
+
+int dcns_smith_waterman_batch(dcns_ctx *ctx, const dcns_pair *tasks, int64_t n, const dcns_params *params,
+                              int32_t *out) {
+  if (!ctx || !params || (n > 0 && !out)) return DCNS_ERR_INVALID;
+  return guarded(ctx, [&] { smith_waterman_batch(ctx->C, to_pairs(tasks, n), to_params(params), out); });
+}
+
+static int copy_cigars(const std::vector<std::vector<uint32_t>> &cg, uint32_t *cigar, int64_t cap, int64_t *off) {
+  int64_t tot = 0;
+  for (auto &c : cg) tot += (int64_t)c.size();
+  if (off) {
+    off[0] = 0;
+    for (size_t k = 0; k < cg.size(); ++k) off[k + 1] = off[k] + (int64_t)cg[k].size();
+  }
+  if (!cigar) return DCNS_OK;
+  if (tot > cap) return DCNS_ERR_NOMEM;
+  int64_t c = 0;
+  for (auto &v : cg) {
+    std::memcpy(cigar + c, v.data(), v.size() * sizeof(uint32_t));
+    c += (int64_t)v.size();
+  }
+  return DCNS_OK;
+}
+
+int dcns_xextend_batch(dcns_ctx *ctx, const dcns_pair *tasks, int64_t n, const dcns_params *params, int want_cigar,
+                       int32_t *out, uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_offset) {
+  if (!ctx || !params || (n > 0 && !out)) return DCNS_ERR_INVALID;
+  std::vector<std::vector<uint32_t>> cg;
+  int rc = guarded(ctx, [&] { xextend_batch(ctx->C, to_pairs(tasks, n), to_params(params), want_cigar != 0, out, cg); });
+  if (rc != DCNS_OK) return rc;
+  return copy_cigars(cg, cigar, cigar_cap, cigar_offset);
+}
+
+int dcns_semiglobal_batch(dcns_ctx *ctx, const dcns_pair *tasks, int64_t n, const dcns_params *params,
+                          int want_cigar, int32_t *out, uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_offset) {
+  if (!ctx || !params || (n > 0 && !out)) return DCNS_ERR_INVALID;
+  std::vector<std::vector<uint32_t>> cg;
+  int rc =
+      guarded(ctx, [&] { semiglobal_batch(ctx->C, to_pairs(tasks, n), to_params(params), want_cigar != 0, out, cg); });
+  if (rc != DCNS_OK) return rc;
+  return copy_cigars(cg, cigar, cigar_cap, cigar_offset);
+}
+
+int dcns_sliding_window(dcns_ctx *ctx, const int8_t *const *seqs, const int32_t *lens, int32_t n_seqs,
+                        const dcns_params *params, double *score, int32_t *max_out) {
+  if (!ctx || !params || !seqs || !lens || n_seqs < 1 || !score || !max_out) return DCNS_ERR_INVALID;
+  return guarded(ctx, [&] { sliding_window(ctx->C, seqs, lens, n_seqs, to_params(params), score, max_out); });
+}
+
+int dcns_serve_start(dcns_ctx *ctx, const dcns_params *params, int mode, int max_inflight_pairs) {
+  if (!ctx || !params) return DCNS_ERR_INVALID;
+  if (ctx->srv) return DCNS_ERR_BUSY;
+  return guarded(ctx, [&] {
+    Params P = to_params(params);
+    validate(P);
+    if (mode != DCNS_MODE_ONE_GAP && mode != DCNS_MODE_TWO_GAP) throw Error(DCNS_ERR_INVALID, "bad mode");
+    auto S = std::make_unique<Server>();
+    S->P = P;
+    S->mode = mode;
+    S->max_inflight = max_inflight_pairs > 0 ? max_inflight_pairs : 256;
+    S->running = true;
+    const int nlanes = 2;
+    for (int k = 0; k < nlanes; ++k) {
+      auto L = std::make_unique<Context>();
+      init_context(*L, ctx->C.device, ctx->C.budget / nlanes);
+      S->lanes.push_back(std::move(L));
+    }
+    for (auto &L : S->lanes) S->workers.emplace_back(worker_loop, S.get(), L.get());
+    ctx->srv = std::move(S);
+  });
+}
+
+int dcns_submit(dcns_ctx *ctx, const dcns_pair *pair, uint64_t *ticket) {
+  if (!ctx || !pair || !ticket || !ctx->srv) return DCNS_ERR_INVALID;
+  if (pair->len1 < 0 || pair->len2 < 0 || (pair->len1 && !pair->seq1) || (pair->len2 && !pair->seq2))
+    return DCNS_ERR_INVALID;
+  Server &S = *ctx->srv;
+  Server::Req r;
+  r.s1.assign(pair->seq1, pair->seq1 + pair->len1);
+  r.s2.assign(pair->seq2, pair->seq2 + pair->len2);
+  {
+    std::lock_guard<std::mutex> lk(S.mu);
+    r.ticket = S.next++;
+    *ticket = r.ticket;
+    S.queue.push_back(std::move(r));
+  }
+  S.cv_work.notify_one();
+  return DCNS_OK;
+}
+
+int dcns_poll(dcns_ctx *ctx, uint64_t ticket, dcns_results **out) {
+  if (!ctx || !out || !ctx->srv) return DCNS_ERR_INVALID;
+  *out = nullptr;
+  Server &S = *ctx->srv;
+  std::lock_guard<std::mutex> lk(S.mu);
+  auto it = S.done.find(ticket);
+  if (it != S.done.end()) {
+    *out = &it->second->pub;
+    S.done.erase(it);
+    return DCNS_OK;
+  }
+  auto f = S.failed.find(ticket);
+  if (f != S.failed.end()) {
+    ctx->C.err = f->second;
+    S.failed.erase(f);
+    return DCNS_ERR_DEVICE;
+  }
+  if (ticket == 0 || ticket >= S.next) return DCNS_ERR_NOTFOUND;
+  return DCNS_ERR_BUSY;
+}
+
+int dcns_serve_wait(dcns_ctx *ctx, uint64_t ticket, int64_t timeout_ms, dcns_results **out) {
+  if (!ctx || !out || !ctx->srv) return DCNS_ERR_INVALID;
+  Server &S = *ctx->srv;
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
+  {
+    std::unique_lock<std::mutex> lk(S.mu);
+    if (!S.cv_done.wait_until(lk, deadline, [&] { return S.done.count(ticket) || S.failed.count(ticket); }))
+      return DCNS_ERR_TIMEOUT;
+  }
+  return dcns_poll(ctx, ticket, out);
+}
+
+int dcns_serve_stop(dcns_ctx *ctx) {
+  if (!ctx || !ctx->srv) return DCNS_OK;
+  Server &S = *ctx->srv;
+  {
+    std::lock_guard<std::mutex> lk(S.mu);
+    S.running = false;
+  }
+  S.cv_work.notify_all();
+  for (auto &t : S.workers) t.join();
+  for (auto &kv : S.done) delete kv.second;
+  ctx->srv.reset();
+  return DCNS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,113 @@
+// Shared host/device definitions of the GB300 CNS pair-alignment engine.
+//
+// Sequences live on the device in one packed arena: 2-bit A/C/G/T codes (16 bases per uint32 word) plus a 1-bit N
+// mask (32 bases per word).  Every sequence starts on a 64-base boundary, so one 128-bit load fetches 64 bases of a
+// single sequence.  Kernels decode to dCNS integer codes (A=0 C=1 N=2 G=3 T=4, impl/SequenceCharToUInt8.cpp:6-33)
+// and read reverse complements by mirrored indexing (4 - code, impl/SequenceCharToUInt8.cpp:61-66), so no
+// reverse-complement copy is stored.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dcns {
+
+constexpr int32_t kOut = -536870912;  // score of cells outside a band (impl/sequenceAlignment3.cpp:34)
+constexpr int kScanW = 38;            // window width the fast seed-scan kernel is specialised for
+constexpr int kKillCode = 5;          // read-code slot whose score is kKillScore (pads short windows)
+constexpr int kKillScore = -128;
+
+struct Params {
+  int32_t match, mismatch, open1, ext1, open2, ext2;
+  int32_t window, min_score, step, w, xdrop, zdrop, bandwidth, max_align_len;
+  double pvalue, lambda, kvalue;
+};
+
+struct Arena {
+  const uint32_t *pk;  // 2-bit codes
+  const uint32_t *nm;  // N mask
+};
+
+// One thread of the seed-scan kernel: up to two Smith-Waterman tasks (int16x2 halves) of the same pair that scan
+// the same absolute reference rows.  Half h scores window [s2[h], s2[h]+tw[h]) of seq2 against reference rows
+// [lo[h], hi[h]); the tile computes rows [row_begin, row_end) and reports maxima only for rows >= cnt_begin.
+struct ScanTile {
+  int64_t ref_base, qry_base;
+  int32_t s2[2], tw[2];
+  int32_t lo[2], hi[2];
+  int32_t row_begin, cnt_begin, row_end;
+  int32_t task[2];  // result slot of each half, -1 when the half is unused
+};
+
+// Per Smith-Waterman task (window x reference range): the reduced maximum and, after the reverse scan, the seed.
+struct ScanTask {
+  int32_t pair, s2, tw, lo, hi;
+  int32_t score, end1, end2;      // absolute 0-based first argmax (valid when score > 0)
+  int32_t start1, start2;         // seed start from the reverse scan (valid when score >= min_score)
+  int32_t striped;                // 1: the reference runs its striped (AVX2) kernel for this task, 0: scalar
+  int32_t pad;
+};
+
+// Packed reduction key of a task maximum: larger score wins, then the earlier row, then the earlier column.
+__host__ __device__ inline unsigned long long scan_key(int32_t score, int32_t row, int32_t col) {
+  return ((unsigned long long)(uint32_t)score << 40) | ((unsigned long long)(0xFFFFFFu - (uint32_t)row) << 16) |
+         (unsigned long long)(0xFFFFu - (uint32_t)col);
+}
+__host__ __device__ inline void scan_unkey(unsigned long long k, int32_t &score, int32_t &row, int32_t &col) {
+  score = (int32_t)(k >> 40);
+  row = (int32_t)(0xFFFFFFu - (uint32_t)((k >> 16) & 0xFFFFFF));
+  col = (int32_t)(0xFFFFu - (uint32_t)(k & 0xFFFF));
+}
+
+// One banded x-drop pass (SemiGlobal_xextend, impl/sequenceAlignment3.cpp:1234/1318) of one seed.
+//   dir 0: forward from (a1, a2) over seq1[a1..), seq2[a2..)
+//   dir 1: backward over the reverse complements ending at (a1, a2): row i reads seq1[a1-i+1] complemented
+struct XTask {
+  int64_t base1, base2;
+  int32_t a1, a2, n1, n2;
+  int32_t dir, w, want_codes, tb_cap;  // tb_cap: traceback slot capacity in 32-bit words
+  int64_t tb_off;
+  // outputs
+  int32_t score, end1, end2;           // 1-based best cell (0 when none)
+  int32_t rows;                        // rows evaluated in this pass
+  int32_t status;                      // 0 done, 1 band-edge restart needed (w doubled), 2 traceback slot too small
+  int32_t iii, jjj, ncig;              // traceback results
+  int64_t cig_off;                     // CIGAR slot (uint32 entries) and its capacity
+  int32_t cig_cap, pad;
+};
+
+// One 2-piece affine semi-global DP (SemiGlobal_no_avx, impl/sequenceAlignment3.cpp:681-928).
+//   dir 0: seq1[a1 .. a1+n1), seq2[a2 .. a2+n2)        dir 1: reverse complements ending at (a1, a2)
+struct SgTask {
+  int64_t base1, base2;
+  int32_t a1, a2, n1, n2;
+  int32_t dir, want_codes;
+  int64_t tb_off;                      // byte offset of the direction-code store (want_codes)
+  int64_t tb_bytes;
+  int64_t bnd_off;                     // scratch for the band boundary rows (int32 x 3 x (n2+1))
+  // outputs
+  int32_t score, end1, end2, rows;     // end1/end2 1-based (-1 when none) ; rows evaluated
+  int32_t status, ncig;
+  int64_t cig_off;
+  int32_t cig_cap, pad;
+};
+
+// ---- kernel launchers (defined in the .cu files)
+void launch_pack(const int8_t *codes, const int64_t *src_off, const int64_t *dst_base, const int32_t *len, int nseq,
+                 uint32_t *pk, uint32_t *nm, cudaStream_t st);
+void launch_scan(const ScanTile *tiles, int ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
+                 int grid, cudaStream_t st);
+void launch_scan_generic(const ScanTask *tasks, const int *idx, int n, const int64_t *seq_base, Arena ar, Params p,
+                         unsigned long long *keys, int32_t *scratch, int64_t scratch_per_thread, cudaStream_t st);
+void launch_reverse(ScanTask *tasks, int first, int n, const unsigned long long *keys, const int64_t *pair_base,
+                    const int32_t *pair_len, Arena ar, Params p, cudaStream_t st);
+void launch_xdrop(XTask *tasks, const int *idx, int n, Arena ar, Params p, uint32_t *tb, int wcap, int32_t *scratch,
+                  int64_t scratch_per_thread, cudaStream_t st);
+void launch_xdrop_traceback(XTask *tasks, const int *idx, int n, const uint32_t *tb, uint32_t *cig, cudaStream_t st);
+void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p, uint8_t *tb, int32_t *bnd,
+                       int64_t bnd_stride, int *work_counter, int grid_warps, cudaStream_t st);
+void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, uint32_t *cig,
+                         cudaStream_t st);
+int64_t sg_tb_bytes(int n1, int n2, int w);
+
+}  // namespace dcns

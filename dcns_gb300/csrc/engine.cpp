@@ -1,0 +1,1175 @@
+// Host orchestration of the GB300 CNS pair-alignment path.
+//
+// align_pairs() runs, for a batch of independent (reference, query) pairs, what the reference runs per pair in
+// findSimilarFragmentsForPairedSequence (impl/findSimilarFragmentsForPairedSequence4.cpp:433 for 1-gap, :752 for
+// 2-gap):
+//   1. upload + pack            all sequences into one 2-bit arena (one H2D, one pack kernel)
+//   2. seed scan                every window x full reference as ScanTasks -> int16x2 tiles (seedscan.cu), then the
+//                               reverse scan that fixes each seed's start
+//   3. recursion + replay       the reference recurses into the reference on both sides of every new seed and
+//                               gates the top-level recursion on set membership with a non-strict-weak comparator.
+//                               Recursion tasks are computed level-synchronously on the device; the host replays the
+//                               exact std::set insertion sequence per pair, requesting the children it needs, until
+//                               no pair needs more (optimistic replay: windows later gated out may have had their
+//                               children computed; such work is counted as speculative, not algorithmic).
+//   4. link_seeds               per pair, host (:288-344)
+//   5. x-drop                   forward pass, reverse pass with 4-bit direction codes, traceback (xdrop.cu); band
+//                               restarts and traceback-slot growth are relaunches
+//   6. fragments                p/e-values in FP64 on the host, dedupe in the reference's order (:497-520)
+//   2-gap mode replaces 5-6 by the x-drop filter (:395-427) and the 2-piece semi-global stage (:532-616).
+#include "engine.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <thread>
+
+namespace dcns {
+
+// ------------------------------------------------------------------ buffers
+void DevBuf::ensure(Context &C, size_t bytes) {
+  if (bytes <= cap) return;
+  size_t want = std::max(bytes, cap + cap / 2);
+  want = (want + 255) & ~size_t(255);
+  if (C.used - cap + want > C.budget) {
+    want = bytes;
+    if (C.used - cap + want > C.budget)
+      throw Error(DCNS_ERR_NOMEM, "device memory budget exhausted (" + std::to_string(C.used - cap + want) +
+                                      " > " + std::to_string(C.budget) + " bytes)");
+  }
+  if (p) {
+    DCNS_CK(cudaFree(p));
+    C.used -= cap;
+    p = nullptr;
+    cap = 0;
+  }
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    (void)cudaGetLastError();
+    throw Error(DCNS_ERR_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  }
+  cap = want;
+  C.used += want;
+}
+
+void DevBuf::release(Context &C) {
+  if (p) {
+    cudaFree(p);
+    C.used -= cap;
+  }
+  p = nullptr;
+  cap = 0;
+}
+
+void HostBuf::ensure(size_t bytes) {
+  if (bytes <= cap) return;
+  size_t want = std::max(bytes, cap + cap / 2);
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+  DCNS_CK(cudaMallocHost(&p, want));
+  cap = want;
+}
+
+void HostBuf::release() {
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+}
+
+Context::~Context() {
+  DevBuf *bufs[] = {&d_codes, &d_srcoff, &d_dstbase, &d_len, &d_pk, &d_nm, &d_seqbase, &d_flag, &d_tasks, &d_keys,
+                    &d_tiles, &d_counter, &d_idx, &d_scratch, &d_x, &d_tb, &d_cig, &d_sg, &d_sgtb, &d_bnd};
+  for (DevBuf *b : bufs) b->release(*this);
+  h_codes.release();
+  h_misc.release();
+  h_out.release();
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+  if (st) cudaStreamDestroy(st);
+}
+
+Params to_params(const dcns_params *p) {
+  Params P;
+  P.match = p->match;
+  P.mismatch = p->mismatch;
+  P.open1 = p->open1;
+  P.ext1 = p->ext1;
+  P.open2 = p->open2;
+  P.ext2 = p->ext2;
+  P.window = p->window;
+  P.min_score = p->min_score;
+  P.step = p->step;
+  P.w = p->w;
+  P.xdrop = p->xdrop;
+  P.zdrop = p->zdrop;
+  P.bandwidth = p->bandwidth;
+  P.max_align_len = p->max_align_len;
+  P.pvalue = p->pvalue;
+  P.lambda = p->lambda;
+  P.kvalue = p->kvalue;
+  return P;
+}
+
+void validate(const Params &P) {
+  auto bad = [](const char *m) { throw Error(DCNS_ERR_INVALID, m); };
+  // Scorei stores scores as int8 (model/Score.cpp:105); the reference's striped kernels cast gap penalties to int8.
+  if (P.match < 1 || P.match > 127 || P.mismatch < -127 || P.mismatch > 127) bad("match must be 1..127, mismatch -127..127");
+  if (P.open1 > 0 || P.ext1 > 0 || P.open1 < -127 || P.ext1 < -127) bad("open1/ext1 must be in -127..0");
+  if (P.open2 > 0 || P.ext2 > 0 || P.open2 < -100000 || P.ext2 < -100000) bad("open2/ext2 must be <= 0");
+  if (P.window < 1 || P.window > 128) bad("window must be 1..128");
+  if (P.step < 1) bad("step must be >= 1");
+  if (P.min_score < 1) bad("min_score must be >= 1");
+  if (P.w < 1 || P.w > (1 << 20)) bad("w must be 1..2^20");
+  if (P.xdrop < 0 || P.zdrop < 0) bad("xdrop/zdrop must be >= 0");
+  if (P.bandwidth < 1) bad("bandwidth must be >= 1");
+}
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+double ms_since(Clock::time_point t) { return std::chrono::duration<double, std::milli>(Clock::now() - t).count(); }
+
+void parallel_for(int64_t n, const std::function<void(int64_t)> &f) {
+  int nt = (int)std::min<int64_t>(std::max(1u, std::thread::hardware_concurrency()), 32);
+  if (n < 64 || nt <= 1) {
+    for (int64_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<int64_t> next(0);
+  auto work = [&]() {
+    for (int64_t i; (i = next.fetch_add(1)) < n;) f(i);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+  work();
+  for (auto &th : pool) th.join();
+}
+
+template <class T>
+void h2d(Context &C, DevBuf &d, const T *src, size_t n, size_t off_elems = 0) {
+  if (!n) return;
+  DCNS_CK(cudaMemcpyAsync(d.as<T>() + off_elems, src, n * sizeof(T), cudaMemcpyHostToDevice, C.st));
+}
+template <class T>
+void d2h(Context &C, T *dst, const DevBuf &d, size_t n, size_t off_elems = 0) {
+  if (!n) return;
+  DCNS_CK(cudaMemcpyAsync(dst, d.as<T>() + off_elems, n * sizeof(T), cudaMemcpyDeviceToHost, C.st));
+}
+void sync(Context &C) {
+  DCNS_CK(cudaStreamSynchronize(C.st));
+  DCNS_CK(cudaGetLastError());
+}
+
+bool striped_for_host(int nref, int nread, int open, int ext, int match) {
+  auto ok = [&](int64_t lim) {
+    return ((-(int64_t)nref * ext - open) < lim || (-(int64_t)nread * ext - open) < lim) &&
+           ((int64_t)nref * match < lim || (int64_t)nread * match < lim);
+  };
+  return ok(125) || ok(32767);
+}
+
+// ------------------------------------------------------------------ 1. upload + pack
+void upload(Context &C, const std::vector<PairIn> &pairs) {
+  const int64_t np = (int64_t)pairs.size(), ns = 2 * np;
+  C.seq_base.assign(ns, 0);
+  std::vector<int64_t> src_off(ns);
+  std::vector<int32_t> len(ns);
+  int64_t total_src = 0, total_dst = 0;
+  for (int64_t k = 0; k < np; ++k) {
+    for (int h = 0; h < 2; ++h) {
+      const int32_t n = h ? pairs[k].n2 : pairs[k].n1;
+      if (n < 0) throw Error(DCNS_ERR_INVALID, "negative sequence length");
+      len[2 * k + h] = n;
+      src_off[2 * k + h] = total_src;
+      C.seq_base[2 * k + h] = total_dst;
+      total_src += n;
+      total_dst += ((int64_t)n + 63) / 64 * 64;
+    }
+  }
+  total_dst += 128;  // lets every kernel read one 64-base block past any sequence end
+  C.h_codes.ensure((size_t)std::max<int64_t>(total_src, 1));
+  int8_t *stage = C.h_codes.as<int8_t>();
+  parallel_for(ns, [&](int64_t s) {
+    const PairIn &p = pairs[s / 2];
+    const int8_t *src = (s & 1) ? p.s2 : p.s1;
+    if (len[s]) std::memcpy(stage + src_off[s], src, (size_t)len[s]);
+  });
+  C.d_codes.ensure(C, (size_t)std::max<int64_t>(total_src, 1));
+  C.d_srcoff.ensure(C, sizeof(int64_t) * ns + 8);
+  C.d_dstbase.ensure(C, sizeof(int64_t) * ns + 8);
+  C.d_len.ensure(C, sizeof(int32_t) * ns + 8);
+  C.d_seqbase.ensure(C, sizeof(int64_t) * ns + 8);
+  C.d_pk.ensure(C, sizeof(uint32_t) * (total_dst / 16));
+  C.d_nm.ensure(C, sizeof(uint32_t) * (total_dst / 32));
+  C.d_flag.ensure(C, 64);
+  h2d(C, C.d_codes, stage, (size_t)total_src);
+  h2d(C, C.d_srcoff, src_off.data(), ns);
+  h2d(C, C.d_dstbase, C.seq_base.data(), ns);
+  h2d(C, C.d_len, len.data(), ns);
+  h2d(C, C.d_seqbase, C.seq_base.data(), ns);
+  DCNS_CK(cudaMemsetAsync(C.d_pk.p, 0, sizeof(uint32_t) * (total_dst / 16), C.st));
+  DCNS_CK(cudaMemsetAsync(C.d_nm.p, 0, sizeof(uint32_t) * (total_dst / 32), C.st));
+  launch_pack(C.d_codes.as<int8_t>(), C.d_srcoff.as<int64_t>(), C.d_dstbase.as<int64_t>(), C.d_len.as<int32_t>(),
+              (int)ns, C.d_pk.as<uint32_t>(), C.d_nm.as<uint32_t>(), C.st);
+  C.stats.kernel_launches += 1;
+  C.arena.pk = C.d_pk.as<uint32_t>();
+  C.arena.nm = C.d_nm.as<uint32_t>();
+  // the reference indexes its 5x5 score table with the codes: anything outside 0..4 is rejected up front
+  std::atomic<bool> badcode(false);
+  parallel_for((total_src + (1 << 20) - 1) >> 20, [&](int64_t b) {
+    const int64_t lo = b << 20, hi = std::min<int64_t>(total_src, lo + (1 << 20));
+    for (int64_t i = lo; i < hi; ++i)
+      if ((uint8_t)stage[i] > 4) {
+        badcode = true;
+        break;
+      }
+  });
+  if (badcode) throw Error(DCNS_ERR_INVALID, "sequence codes must be dCNS codes 0..4 (A C N G T)");
+}
+
+// ------------------------------------------------------------------ 2./3. seed scan with recursion replay
+struct ScanState {
+  std::vector<ScanTask> tasks;
+  std::vector<int32_t> left, right;      // child task id, -1 none/not created
+  std::vector<std::vector<int32_t>> win;  // per pair: level-0 task ids in window order
+  std::vector<int32_t> pair_len1, pair_len2;
+  int64_t first_new = 0;                 // tasks [first_new, size) still to be computed
+  int64_t speculative = 0;
+};
+
+int warmup_rows(const Params &P, int tw) {
+  // A positive-scoring local path over tw read columns spans at most tw diagonal rows plus fewer than
+  // match*tw/g vertical-gap rows (g = cheapest gap row), so a scan restarted K rows early is exact from row K on.
+  const int g = std::min(-P.open1, -P.ext1);
+  if (g <= 0) return INT_MAX;
+  return tw + (P.match * tw + g - 1) / g + 4;
+}
+
+// Computes tasks [S.first_new, size): fast int16x2 tiles where the reference's striped semantics and the int16 bound
+// hold, the generic int32 kernel otherwise; then the reverse scans.  Downloads the finished tasks.
+void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
+  const int64_t first = S.first_new, n = (int64_t)S.tasks.size() - first;
+  if (n <= 0) return;
+  S.first_new = (int64_t)S.tasks.size();
+  auto t0 = Clock::now();
+
+  std::vector<int32_t> fast, generic;
+  for (int64_t k = first; k < first + n; ++k) {
+    ScanTask &T = S.tasks[k];
+    T.striped = striped_for_host(T.hi - T.lo, T.tw, P.open1, P.ext1, P.match) ? 1 : 0;
+    if (T.tw <= 0 || T.hi <= T.lo) continue;  // nothing to scan: key stays 0
+    if (T.striped && T.tw <= kScanW)
+      fast.push_back((int32_t)k);
+    else
+      generic.push_back((int32_t)k);
+  }
+  // Pair consecutive fast tasks of one pair (same rows for level 0; similar ranges for recursion children).
+  std::sort(fast.begin(), fast.end(), [&](int32_t a, int32_t b) {
+    const ScanTask &x = S.tasks[a], &y = S.tasks[b];
+    if (x.pair != y.pair) return x.pair < y.pair;
+    if (x.lo != y.lo) return x.lo < y.lo;
+    if (x.hi != y.hi) return x.hi < y.hi;
+    return x.s2 < y.s2;
+  });
+  struct Half2 {
+    int32_t a, b;
+  };
+  std::vector<Half2> duo;
+  for (size_t i = 0; i < fast.size(); i += 2) {
+    const int32_t a = fast[i];
+    int32_t b = -1;
+    if (i + 1 < fast.size() && S.tasks[fast[i + 1]].pair == S.tasks[a].pair) b = fast[i + 1];
+    if (b < 0 && i + 1 < fast.size()) {
+      duo.push_back({a, -1});
+      i -= 1;  // fast[i+1] starts the next duo
+      continue;
+    }
+    duo.push_back({a, b});
+  }
+  // Row chunking: enough tiles for ~8 resident waves of threads, each tile at least 4 warm-up lengths long.
+  int64_t total_rows = 0;
+  for (const Half2 &d : duo) {
+    const ScanTask &A = S.tasks[d.a];
+    int lo = A.lo, hi = A.hi;
+    if (d.b >= 0) lo = std::min(lo, S.tasks[d.b].lo), hi = std::max(hi, S.tasks[d.b].hi);
+    total_rows += hi - lo;
+  }
+  const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * 128;
+  const int64_t want_tiles = 8 * resident;
+  const int K = warmup_rows(P, kScanW);
+  int64_t chunk = INT64_MAX;
+  if ((int64_t)duo.size() < want_tiles && K != INT_MAX && total_rows > 0)
+    chunk = std::max<int64_t>(4 * (int64_t)K, (total_rows + want_tiles - 1) / want_tiles);
+  std::vector<ScanTile> tiles;
+  tiles.reserve(duo.size() + 16);
+  for (const Half2 &d : duo) {
+    ScanTile tl{};
+    const ScanTask &A = S.tasks[d.a];
+    tl.ref_base = C.seq_base[2 * A.pair];
+    tl.qry_base = C.seq_base[2 * A.pair + 1];
+    int lo = A.lo, hi = A.hi;
+    tl.s2[0] = A.s2, tl.tw[0] = A.tw, tl.lo[0] = A.lo, tl.hi[0] = A.hi, tl.task[0] = d.a;
+    if (d.b >= 0) {
+      const ScanTask &B = S.tasks[d.b];
+      tl.s2[1] = B.s2, tl.tw[1] = B.tw, tl.lo[1] = B.lo, tl.hi[1] = B.hi, tl.task[1] = d.b;
+      lo = std::min(lo, B.lo);
+      hi = std::max(hi, B.hi);
+    } else {
+      tl.s2[1] = 0, tl.tw[1] = 0, tl.lo[1] = A.lo, tl.hi[1] = A.hi, tl.task[1] = -1;
+    }
+    for (int64_t c0 = lo; c0 < hi; c0 += chunk) {
+      const int64_t c1 = std::min<int64_t>(hi, c0 + chunk);
+      ScanTile t = tl;
+      t.cnt_begin = (int32_t)c0;
+      t.row_end = (int32_t)c1;
+      t.row_begin = (int32_t)std::max<int64_t>(lo, c0 - (c0 == lo ? 0 : K));
+      tiles.push_back(t);
+      if (chunk == INT64_MAX) break;
+    }
+  }
+  std::sort(tiles.begin(), tiles.end(), [](const ScanTile &a, const ScanTile &b) {
+    return (a.row_end - a.row_begin) > (b.row_end - b.row_begin);
+  });
+
+  // device: tasks segment, keys, tiles
+  C.d_tasks.ensure(C, sizeof(ScanTask) * S.tasks.size());
+  C.d_keys.ensure(C, sizeof(unsigned long long) * S.tasks.size());
+  h2d(C, C.d_tasks, S.tasks.data() + first, (size_t)n, (size_t)first);
+  DCNS_CK(cudaMemsetAsync(C.d_keys.as<unsigned long long>() + first, 0, sizeof(unsigned long long) * n, C.st));
+  if (!tiles.empty()) {
+    C.d_tiles.ensure(C, sizeof(ScanTile) * tiles.size());
+    C.d_counter.ensure(C, 64);
+    h2d(C, C.d_tiles, tiles.data(), tiles.size());
+    DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int), C.st));
+    const int grid = (int)std::min<int64_t>((int64_t)C.nsm * C.scan_blocks_per_sm, ((int64_t)tiles.size() + 127) / 128);
+    DCNS_CK(cudaEventRecord(C.ev0, C.st));
+    launch_scan(C.d_tiles.as<ScanTile>(), (int)tiles.size(), C.arena, P, C.d_keys.as<unsigned long long>(),
+                C.d_counter.as<int>(), grid, C.st);
+    DCNS_CK(cudaEventRecord(C.ev1, C.st));
+    C.stats.scan_launches += 1;
+    C.stats.kernel_launches += 1;
+  }
+  if (!generic.empty()) {
+    int maxtw = 0;
+    for (int32_t k : generic) maxtw = std::max(maxtw, S.tasks[k].tw);
+    const int64_t per = 3 * ((int64_t)maxtw + 2);
+    C.d_idx.ensure(C, sizeof(int32_t) * generic.size());
+    C.d_scratch.ensure(C, sizeof(int32_t) * per * generic.size());
+    h2d(C, C.d_idx, generic.data(), generic.size());
+    launch_scan_generic(C.d_tasks.as<ScanTask>(), C.d_idx.as<int>(), (int)generic.size(), C.d_seqbase.as<int64_t>(),
+                        C.arena, P, C.d_keys.as<unsigned long long>(), C.d_scratch.as<int32_t>(), per, C.st);
+    C.stats.kernel_launches += 1;
+  }
+  launch_reverse(C.d_tasks.as<ScanTask>(), (int)first, (int)n, C.d_keys.as<unsigned long long>(),
+                 C.d_seqbase.as<int64_t>(), nullptr, C.arena, P, C.st);
+  C.stats.kernel_launches += 1;
+  d2h(C, S.tasks.data() + first, C.d_tasks, (size_t)n, (size_t)first);
+  sync(C);
+  if (!tiles.empty()) {
+    float ms = 0;
+    DCNS_CK(cudaEventElapsedTime(&ms, C.ev0, C.ev1));
+    C.stats.ms_scan_kernel += ms;
+  }
+  C.stats.ms_scan += ms_since(t0);
+  S.left.resize(S.tasks.size(), -1);
+  S.right.resize(S.tasks.size(), -1);
+}
+
+inline Seed4 seed_of(const ScanTask &T) { return Seed4{T.start1, T.end1, T.start2, T.end2}; }
+
+struct ReplayCtx {
+  const ScanState &S;
+  const Params &P;
+  int mini;
+  std::vector<std::pair<int32_t, int32_t>> req;  // (task, side) whose child must be created
+  int64_t cells = 0, cells_rev = 0, visited = 0;
+};
+
+// getSeeds' recursive variant (:61-128): the local set gets the seed, then the left subtree's seeds in their set
+// order, then the right subtree's.  Returns false when some child is not computed yet (requests it and continues).
+bool subtree(ReplayCtx &R, int32_t t, SeedSet &out) {
+  const ScanTask &T = R.S.tasks[t];
+  R.visited++;
+  R.cells += (int64_t)(T.hi - T.lo) * std::max(T.tw, 0);
+  if (T.score < R.P.min_score) return true;
+  const int lim = T.tw + R.P.window;
+  R.cells_rev += (int64_t)std::min(T.end1 - T.lo + 1, lim) * std::min(T.end2 - T.s2 + 1, lim);
+  out.insert(seed_of(T));
+  bool ok = true;
+  if (T.start1 - T.lo >= R.mini) {
+    const int32_t c = R.S.left[t];
+    if (c < 0) {
+      R.req.push_back({t, 0});
+      ok = false;
+    } else {
+      SeedSet sub;
+      ok &= subtree(R, c, sub);
+      for (const Seed4 &s : sub) out.insert(s);
+    }
+  }
+  if (T.hi - T.end1 - 1 >= R.mini) {
+    const int32_t c = R.S.right[t];
+    if (c < 0) {
+      R.req.push_back({t, 1});
+      ok = false;
+    } else {
+      SeedSet sub;
+      ok &= subtree(R, c, sub);
+      for (const Seed4 &s : sub) out.insert(s);
+    }
+  }
+  return ok;
+}
+
+// The set-gated window loop (:131-201 per window, :462-480 over windows).
+bool replay_pair(ReplayCtx &R, int64_t p, SeedSet &global) {
+  bool ok = true;
+  for (int32_t t : R.S.win[p]) {
+    const ScanTask &T = R.S.tasks[t];
+    R.visited++;
+    R.cells += (int64_t)(T.hi - T.lo) * std::max(T.tw, 0);
+    if (T.score < R.P.min_score) continue;
+    const int lim = T.tw + R.P.window;
+    R.cells_rev += (int64_t)std::min(T.end1 - T.lo + 1, lim) * std::min(T.end2 - T.s2 + 1, lim);
+    const Seed4 sd = seed_of(T);
+    if (global.find(sd) != global.end()) continue;
+    global.insert(sd);
+    for (int side = 0; side < 2; ++side) {
+      const bool cond = side == 0 ? (T.start1 - T.lo >= R.mini) : (T.hi - T.end1 - 1 >= R.mini);
+      if (!cond) continue;
+      const int32_t c = side == 0 ? R.S.left[t] : R.S.right[t];
+      if (c < 0) {
+        R.req.push_back({t, side});
+        ok = false;
+        continue;
+      }
+      SeedSet sub;
+      ok &= subtree(R, c, sub);
+      for (const Seed4 &s : sub) global.insert(s);
+    }
+  }
+  return ok;
+}
+
+void link_seeds(SeedSet &seeds) {  // :288-344
+  std::vector<Seed4> cur(seeds.begin(), seeds.end());
+  std::sort(cur.begin(), cur.end(), [](Seed4 a, Seed4 b) { return a.s1 < b.s1; });
+  bool changed = true;
+  while (changed) {
+    changed = false;
+    std::vector<Seed4> next;
+    std::set<int> used;
+    const int n = (int)cur.size();
+    for (int i = 0; i < n; ++i) {
+      if (used.count(i)) continue;
+      const Seed4 a = cur[i];
+      bool merged = false;
+      for (int j = i + 1; j < n; ++j) {
+        if (used.count(j)) continue;
+        const Seed4 b = cur[j];
+        if (a.s2 <= b.s2 && a.e1 >= b.e1 && a.e2 >= b.e2) {
+          used.insert(j);
+        } else if (a.s2 <= b.s2 && a.e1 <= b.e1 && a.e2 <= b.e2) {
+          const int32_t d = b.s1 - a.s1;
+          if (d == b.s2 - a.s2 && d == b.e1 - a.e1 && d == b.e2 - a.e2) {
+            next.push_back(Seed4{a.s1, b.e1, a.s2, b.e2});
+            used.insert(i);
+            used.insert(j);
+            merged = true;
+            break;
+          }
+        } else if (b.s1 > a.e1 || b.s2 > a.e2) {
+          break;
+        }
+      }
+      if (merged)
+        changed = true;
+      else
+        next.push_back(a);
+    }
+    cur.swap(next);
+  }
+  seeds.clear();
+  for (const Seed4 &s : cur) seeds.insert(s);
+}
+
+// Window starts of the 1-gap driver (:462-480, stops once past the query end) and of getAllExtendSeed (:376-390).
+void window_starts(int32_t n2, const Params &P, bool stop_past_end, std::vector<int32_t> &st) {
+  st.clear();
+  int32_t s = 0;
+  while (true) {
+    st.push_back(s);
+    s += P.step;
+    if (stop_past_end && s > n2) break;
+    if (s + P.window > n2) {
+      st.push_back(s);
+      break;
+    }
+  }
+}
+
+// Seed scan + replay + linking for every pair; returns the linked seed list of each pair in set order.
+void scan_and_link(Context &C, const std::vector<PairIn> &pairs, const Params &P, bool one_gap,
+                   std::vector<std::vector<Seed4>> &linked) {
+  const int64_t np = (int64_t)pairs.size();
+  ScanState S;
+  S.win.resize(np);
+  std::vector<int32_t> starts;
+  for (int64_t p = 0; p < np; ++p) {
+    window_starts(pairs[p].n2, P, one_gap, starts);
+    for (int32_t s : starts) {
+      ScanTask T{};
+      T.pair = (int32_t)p;
+      T.s2 = s;
+      T.tw = (s + P.window) > pairs[p].n2 ? (pairs[p].n2 - s) : P.window;
+      T.lo = 0;
+      T.hi = pairs[p].n1;
+      T.score = 0;
+      S.win[p].push_back((int32_t)S.tasks.size());
+      S.tasks.push_back(T);
+    }
+  }
+  const int mini = P.min_score / P.match;
+  std::vector<SeedSet> sets(np);
+  std::vector<uint8_t> done(np, 0);
+  int64_t cells = 0, cells_rev = 0, visited_final = 0;
+  for (int round = 0;; ++round) {
+    compute_scan_tasks(C, S, P);
+    auto t0 = Clock::now();
+    std::vector<ReplayCtx> rc;
+    std::vector<std::vector<std::pair<int32_t, int32_t>>> reqs(np);
+    std::vector<int64_t> pc(np, 0), pr(np, 0), pv(np, 0);
+    std::vector<int64_t> todo;
+    for (int64_t p = 0; p < np; ++p)
+      if (!done[p]) todo.push_back(p);
+    parallel_for((int64_t)todo.size(), [&](int64_t q) {
+      const int64_t p = todo[q];
+      ReplayCtx R{S, P, mini, {}, 0, 0, 0};
+      SeedSet g;
+      const bool ok = replay_pair(R, p, g);
+      if (ok) {
+        sets[p].swap(g);
+        done[p] = 1;
+        pc[p] = R.cells;
+        pr[p] = R.cells_rev;
+        pv[p] = R.visited;
+      } else {
+        reqs[p].swap(R.req);
+      }
+    });
+    int64_t nreq = 0;
+    for (int64_t p = 0; p < np; ++p) {
+      cells += pc[p];
+      cells_rev += pr[p];
+      visited_final += pv[p];
+      for (auto &rq : reqs[p]) {
+        const int32_t t = rq.first;
+        int32_t &slot = rq.second == 0 ? S.left[t] : S.right[t];
+        if (slot >= 0) continue;
+        const ScanTask &P0 = S.tasks[t];
+        ScanTask ch{};
+        ch.pair = P0.pair;
+        ch.s2 = P0.s2;
+        ch.tw = P0.tw;
+        if (rq.second == 0) {
+          ch.lo = P0.lo;
+          ch.hi = P0.start1;
+        } else {
+          ch.lo = P0.end1 + 1;
+          ch.hi = P0.hi;
+        }
+        slot = (int32_t)S.tasks.size();
+        S.tasks.push_back(ch);
+        ++nreq;
+      }
+    }
+    S.left.resize(S.tasks.size(), -1);
+    S.right.resize(S.tasks.size(), -1);
+    C.stats.ms_replay += ms_since(t0);
+    if (nreq == 0) break;
+    if (round > 100000) throw Error(DCNS_ERR_DEVICE, "seed recursion did not converge");
+  }
+  C.stats.cells_scan += cells;
+  C.stats.cells_scan_reverse += cells_rev;
+  C.stats.tasks_scan += visited_final;
+  C.stats.tasks_scan_speculative += (int64_t)S.tasks.size() - visited_final;
+  auto t0 = Clock::now();
+  linked.assign(np, {});
+  parallel_for(np, [&](int64_t p) {
+    link_seeds(sets[p]);
+    linked[p].assign(sets[p].begin(), sets[p].end());
+  });
+  C.stats.ms_replay += ms_since(t0);
+}
+
+// ------------------------------------------------------------------ 5. x-drop passes
+int64_t band_cells(int rows, int w, int n2) {
+  int64_t c = 0;
+  for (int i = 1; i <= rows; ++i) c += std::max(0, std::min(i + w, n2) - std::max(i - w, 1) + 1);
+  return c;
+}
+
+int wpr_of(int w) { return (2 * w + 1 + 7) / 8; }
+
+// Runs the given x-drop passes to completion (band restarts, traceback-slot growth), then their tracebacks when
+// want_codes.  X lives on the host between launches.
+void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_codes,
+               std::vector<std::vector<uint32_t>> *cigars) {
+  if (X.empty()) return;
+  auto t0 = Clock::now();
+  const int64_t n = (int64_t)X.size();
+  std::vector<int64_t> rows_cap(n, 0);
+  for (int64_t k = 0; k < n; ++k) {
+    X[k].want_codes = want_codes ? 1 : 0;
+    X[k].status = 0;
+    X[k].score = X[k].end1 = X[k].end2 = X[k].rows = 0;
+    X[k].iii = X[k].jjj = X[k].ncig = 0;
+    rows_cap[k] = std::min<int64_t>(X[k].n1, 1024);
+  }
+  if (cigars) cigars->assign(n, {});
+  std::vector<int32_t> pend(n);
+  for (int64_t k = 0; k < n; ++k) pend[k] = (int32_t)k;
+  C.d_x.ensure(C, sizeof(XTask) * n);
+  while (!pend.empty()) {
+    // traceback slots for this round, laid out from offset 0
+    int64_t words = 0;
+    if (want_codes)
+      for (int32_t k : pend) {
+        X[k].tb_off = words;
+        X[k].tb_cap = (int32_t)std::min<int64_t>(INT32_MAX, rows_cap[k] * wpr_of(X[k].w));
+        words += X[k].tb_cap;
+      }
+    if (want_codes) C.d_tb.ensure(C, sizeof(uint32_t) * std::max<int64_t>(words, 1));
+    h2d(C, C.d_x, X.data(), (size_t)n);
+    std::vector<int32_t> g10, g20, gw;
+    int maxw = 0;
+    for (int32_t k : pend) {
+      if (X[k].w <= 10)
+        g10.push_back(k);
+      else if (X[k].w <= 20)
+        g20.push_back(k);
+      else
+        gw.push_back(k), maxw = std::max(maxw, X[k].w);
+    }
+    C.d_idx.ensure(C, sizeof(int32_t) * pend.size());
+    size_t off = 0;
+    auto launch_group = [&](std::vector<int32_t> &g, int wcap) {
+      if (g.empty()) return;
+      h2d(C, C.d_idx, g.data(), g.size(), off);
+      int32_t *scratch = nullptr;
+      int64_t per = 0;
+      if (wcap == 0) {
+        per = 2 * (2 * (int64_t)maxw + 2);
+        C.d_scratch.ensure(C, sizeof(int32_t) * per * g.size());
+        scratch = C.d_scratch.as<int32_t>();
+      }
+      launch_xdrop(C.d_x.as<XTask>(), C.d_idx.as<int>() + off, (int)g.size(), C.arena, P, C.d_tb.as<uint32_t>(),
+                   wcap, scratch, per, C.st);
+      C.stats.kernel_launches += 1;
+      C.stats.xdrop_passes += (int64_t)g.size();
+      off += g.size();
+    };
+    launch_group(g10, 10);
+    launch_group(g20, 20);
+    launch_group(gw, 0);
+    d2h(C, X.data(), C.d_x, (size_t)n);
+    sync(C);
+    std::vector<int32_t> next, finished;
+    for (int32_t k : pend) {
+      if (X[k].status == 1) {
+        X[k].w *= 2;  // the reference restarts the whole pass with twice the band (:1272-1276)
+        next.push_back(k);
+      } else if (X[k].status == 2) {
+        rows_cap[k] = X[k].n1;
+        next.push_back(k);
+      } else {
+        finished.push_back(k);
+      }
+    }
+    if (want_codes && !finished.empty()) {
+      int64_t cw = 0;
+      for (int32_t k : finished) {
+        X[k].cig_off = cw;
+        X[k].cig_cap = X[k].end1 + X[k].end2 + 2;
+        cw += X[k].cig_cap;
+      }
+      C.d_cig.ensure(C, sizeof(uint32_t) * std::max<int64_t>(cw, 1));
+      h2d(C, C.d_x, X.data(), (size_t)n);
+      h2d(C, C.d_idx, finished.data(), finished.size());
+      launch_xdrop_traceback(C.d_x.as<XTask>(), C.d_idx.as<int>(), (int)finished.size(), C.d_tb.as<uint32_t>(),
+                             C.d_cig.as<uint32_t>(), C.st);
+      C.stats.kernel_launches += 1;
+      C.h_out.ensure(sizeof(uint32_t) * std::max<int64_t>(cw, 1));
+      d2h(C, X.data(), C.d_x, (size_t)n);
+      d2h(C, C.h_out.as<uint32_t>(), C.d_cig, (size_t)cw);
+      sync(C);
+      const uint32_t *hc = C.h_out.as<uint32_t>();
+      for (int32_t k : finished) {
+        if (X[k].status == 3) throw Error(DCNS_ERR_DEVICE, "x-drop traceback exceeded its CIGAR slot");
+        (*cigars)[k].assign(hc + X[k].cig_off, hc + X[k].cig_off + X[k].ncig);
+      }
+    }
+    pend.swap(next);
+  }
+  for (int64_t k = 0; k < n; ++k) C.stats.cells_xdrop += band_cells(X[k].rows, X[k].w, X[k].n2);
+  C.stats.ms_xdrop += ms_since(t0);
+}
+
+inline void evalue(const Params &P, double L1, double L2, int32_t score, double &e, double &p) {
+  e = P.kvalue * L1 * L2 * exp(-1.0 * P.lambda * double(score));
+  p = 1.0 - exp(-1.0 * e);
+}
+
+struct XSeedOut {
+  bool ok;
+  int32_t start1, end1, start2, end2, score;
+  std::vector<uint32_t> cigar;
+};
+
+// x_extend_seed (:205-285) for every linked seed of every pair: forward pass, reverse pass (with codes when
+// want_cigar), then the coordinate bookkeeping of the reference.
+void extend_seeds(Context &C, const std::vector<PairIn> &pairs, const Params &P,
+                  const std::vector<std::vector<Seed4>> &linked, bool want_cigar,
+                  std::vector<std::vector<XSeedOut>> &res) {
+  const int64_t np = (int64_t)pairs.size();
+  res.assign(np, {});
+  std::vector<XTask> F;
+  std::vector<std::pair<int32_t, int32_t>> owner;
+  for (int64_t p = 0; p < np; ++p) {
+    res[p].resize(linked[p].size());
+    for (size_t s = 0; s < linked[p].size(); ++s) {
+      const Seed4 &sd = linked[p][s];
+      XTask x{};
+      x.base1 = C.seq_base[2 * p];
+      x.base2 = C.seq_base[2 * p + 1];
+      x.a1 = sd.s1 + 1;  // the extension starts one base after the seed start (:492-495)
+      x.a2 = sd.s2 + 1;
+      x.n1 = pairs[p].n1 - x.a1;
+      x.n2 = pairs[p].n2 - x.a2;
+      x.dir = 0;
+      x.w = P.w;
+      F.push_back(x);
+      owner.push_back({(int32_t)p, (int32_t)s});
+    }
+  }
+  C.stats.seeds += (int64_t)F.size();
+  run_xdrop(C, F, P, false, nullptr);
+  std::vector<XTask> R;
+  std::vector<int32_t> rmap;
+  for (size_t k = 0; k < F.size(); ++k) {
+    const XTask &f = F[k];
+    XSeedOut &o = res[owner[k].first][owner[k].second];
+    o.ok = false;
+    o.score = f.score;
+    if (f.end1 - 1 < 0 || f.end2 - 1 < 0) continue;  // p = 100
+    const int32_t b1 = f.a1 + f.end1 - 1, b2 = f.a2 + f.end2 - 1;
+    XTask r{};
+    r.base1 = f.base1;
+    r.base2 = f.base2;
+    r.a1 = b1;
+    r.a2 = b2;
+    r.n1 = b1 + 1;
+    r.n2 = b2 + 1;
+    r.dir = 1;
+    r.w = P.w;
+    R.push_back(r);
+    rmap.push_back((int32_t)k);
+  }
+  std::vector<std::vector<uint32_t>> cg;
+  run_xdrop(C, R, P, want_cigar, want_cigar ? &cg : nullptr);
+  for (size_t q = 0; q < R.size(); ++q) {
+    const XTask &r = R[q];
+    const XTask &f = F[rmap[q]];
+    XSeedOut &o = res[owner[rmap[q]].first][owner[rmap[q]].second];
+    o.score = r.score;
+    if (want_cigar) o.cigar.swap(cg[q]);
+    if (r.end1 - 1 < 0 || r.end2 - 1 < 0) continue;
+    const int32_t b1 = f.a1 + f.end1 - 1, b2 = f.a2 + f.end2 - 1;
+    o.ok = true;
+    o.end1 = b1;
+    o.end2 = b2;
+    o.start1 = b1 - (r.end1 - 1);
+    o.start2 = b2 - (r.end2 - 1);
+    if (want_cigar) {
+      o.end1 -= r.iii;
+      o.end2 -= r.jjj;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ 2-gap stage (:532-616)
+int64_t sg_band_cells(int rows, int w, int n2) {
+  int64_t c = 0;
+  for (int i = 1; i <= rows; ++i) c += std::max(0, std::min(i + w, n2) - std::max(i - w, 1) + 1);
+  return c;
+}
+
+
+// Runs 2-piece semi-global DPs; with codes, bounded by the memory budget per launch (admission by traceback bytes).
+void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool want_codes,
+                    std::vector<std::vector<uint32_t>> *cigars) {
+  if (G.empty()) return;
+  auto t0 = Clock::now();
+  const int64_t n = (int64_t)G.size();
+  if (cigars) cigars->assign(n, {});
+  int maxn2 = 1;
+  for (auto &g : G) maxn2 = std::max(maxn2, g.n2);
+  // device work split into batches whose direction-code stores fit a fraction of the budget
+  const size_t free_budget = C.budget > C.used ? C.budget - C.used : 0;
+  const int64_t cap_bytes = std::max<int64_t>((int64_t)(free_budget / 2), (int64_t)64 << 20);
+  int64_t k0 = 0;
+  C.d_sg.ensure(C, sizeof(SgTask) * n);
+  while (k0 < n) {
+    int64_t bytes = 0, k1 = k0;
+    while (k1 < n) {
+      const int64_t b = want_codes ? sg_tb_bytes(G[k1].n1, G[k1].n2, P.bandwidth) : 0;
+      if (k1 > k0 && bytes + b > cap_bytes) break;
+      G[k1].tb_off = bytes;
+      G[k1].tb_bytes = b;
+      G[k1].want_codes = want_codes ? 1 : 0;
+      bytes += b;
+      ++k1;
+    }
+    const int64_t m = k1 - k0;
+    if (want_codes) C.d_sgtb.ensure(C, (size_t)std::max<int64_t>(bytes, 1));
+    // whole blocks of 4 warps; every warp of the grid owns a boundary-row slot
+    const int grid_warps = (int)((std::min<int64_t>(m, (int64_t)C.nsm * 16) + 3) / 4 * 4);
+    const int64_t bnd_stride = (int64_t)maxn2 + 2;
+    C.d_bnd.ensure(C, sizeof(int32_t) * 3 * bnd_stride * grid_warps);
+    C.d_counter.ensure(C, 64);
+    DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int), C.st));
+    std::vector<int32_t> idx(m);
+    for (int64_t q = 0; q < m; ++q) idx[q] = (int32_t)(k0 + q);
+    C.d_idx.ensure(C, sizeof(int32_t) * m);
+    h2d(C, C.d_idx, idx.data(), (size_t)m);
+    h2d(C, C.d_sg, G.data(), (size_t)n);
+    launch_semiglobal(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, C.d_sgtb.as<uint8_t>(),
+                      C.d_bnd.as<int32_t>(), bnd_stride, C.d_counter.as<int>(), grid_warps, C.st);
+    C.stats.kernel_launches += 1;
+    C.stats.semiglobal_dps += m;
+    if (want_codes) {
+      d2h(C, G.data(), C.d_sg, (size_t)n);
+      sync(C);
+      int64_t cw = 0;
+      for (int64_t q = k0; q < k1; ++q) {
+        G[q].cig_off = cw;
+        G[q].cig_cap = std::max(G[q].end1, 0) + std::max(G[q].end2, 0) + 2;
+        cw += G[q].cig_cap;
+      }
+      C.d_cig.ensure(C, sizeof(uint32_t) * std::max<int64_t>(cw, 1));
+      h2d(C, C.d_sg, G.data(), (size_t)n);
+      launch_sg_traceback(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, P.bandwidth, C.d_sgtb.as<uint8_t>(),
+                          C.d_cig.as<uint32_t>(), C.st);
+      C.stats.kernel_launches += 1;
+      C.h_out.ensure(sizeof(uint32_t) * std::max<int64_t>(cw, 1));
+      d2h(C, G.data(), C.d_sg, (size_t)n);
+      d2h(C, C.h_out.as<uint32_t>(), C.d_cig, (size_t)cw);
+      sync(C);
+      const uint32_t *hc = C.h_out.as<uint32_t>();
+      for (int64_t q = k0; q < k1; ++q) {
+        if (G[q].status != 0) throw Error(DCNS_ERR_DEVICE, "semi-global traceback exceeded its CIGAR slot");
+        (*cigars)[q].assign(hc + G[q].cig_off, hc + G[q].cig_off + G[q].ncig);
+      }
+    } else {
+      d2h(C, G.data(), C.d_sg, (size_t)n);
+      sync(C);
+    }
+    k0 = k1;
+  }
+  for (auto &g : G) C.stats.cells_semiglobal += sg_band_cells(g.rows, P.bandwidth, g.n2);
+  C.stats.ms_semiglobal += ms_since(t0);
+}
+
+void two_gap_stage(Context &C, const std::vector<PairIn> &pairs, const Params &P,
+                   const std::vector<std::vector<Seed4>> &xs, std::vector<std::vector<FragOut>> &out) {
+  const int64_t np = (int64_t)pairs.size();
+  // reverse 2-piece from every x-seed end (no codes)
+  std::vector<SgTask> Rv;
+  std::vector<std::pair<int32_t, int32_t>> own;
+  for (int64_t p = 0; p < np; ++p)
+    for (size_t s = 0; s < xs[p].size(); ++s) {
+      SgTask g{};
+      g.base1 = C.seq_base[2 * p];
+      g.base2 = C.seq_base[2 * p + 1];
+      g.a1 = xs[p][s].e1;
+      g.a2 = xs[p][s].e2;
+      g.n1 = 1 + xs[p][s].e1;
+      g.n2 = 1 + xs[p][s].e2;
+      g.dir = 1;
+      Rv.push_back(g);
+      own.push_back({(int32_t)p, (int32_t)s});
+    }
+  run_semiglobal(C, Rv, P, false, nullptr);
+  // start gate per pair in x-seed order (StartAlignment set), then forward passes with codes
+  std::vector<SgTask> Fw;
+  std::vector<int32_t> fw_pair;
+  std::vector<std::pair<int32_t, int32_t>> fw_start;
+  {
+    size_t k = 0;
+    for (int64_t p = 0; p < np; ++p) {
+      std::set<std::pair<int32_t, int32_t>> starts;
+      for (size_t s = 0; s < xs[p].size(); ++s, ++k) {
+        const SgTask &r = Rv[k];
+        const int32_t s1 = xs[p][s].e1 - (r.end1 - 1), s2 = xs[p][s].e2 - (r.end2 - 1);
+        if (!starts.insert({s1, s2}).second) continue;
+        SgTask g{};
+        g.base1 = C.seq_base[2 * p];
+        g.base2 = C.seq_base[2 * p + 1];
+        g.a1 = s1;
+        g.a2 = s2;
+        g.n1 = pairs[p].n1 - s1;
+        g.n2 = pairs[p].n2 - s2;
+        g.dir = 0;
+        Fw.push_back(g);
+        fw_pair.push_back((int32_t)p);
+        fw_start.push_back({s1, s2});
+      }
+    }
+  }
+  std::vector<std::vector<uint32_t>> cg;
+  run_semiglobal(C, Fw, P, true, &cg);
+  out.assign(np, {});
+  for (size_t q = 0; q < Fw.size(); ++q) {
+    const int32_t p = fw_pair[q];
+    const SgTask &g = Fw[q];
+    const int32_t s1 = fw_start[q].first, s2 = fw_start[q].second;
+    const int32_t e1z = g.end1 - 1, e2z = g.end2 - 1;  // 0-based as returned by SemiGlobal
+    if (!(cg[q].size() > 0 && e1z > 0 && e2z > 0)) continue;
+    const int64_t e1 = (int64_t)e1z + s1, e2 = (int64_t)e2z + s2;
+    std::vector<FragOut> &fr = out[p];
+    int toRemove = -1;
+    bool found = false;
+    for (int i = 0; i < (int)fr.size(); ++i)
+      if (fr[i].e1 == e1 + 1 && fr[i].e2 == e2 + 1) {
+        found = true;
+        if (s1 + 1 < fr[i].s1 && s2 + 1 < fr[i].s2) toRemove = i;
+      }
+    if (found && toRemove < 0) continue;
+    FragOut f;
+    f.s1 = s1 + 1;
+    f.e1 = e1 + 1;
+    f.s2 = s2 + 1;
+    f.e2 = e2 + 1;
+    f.score = (int64_t)(uint32_t)g.score;
+    f.cigar = cg[q];
+    evalue(P, double(pairs[p].n1), double(pairs[p].n2), g.score, f.e, f.p);
+    if (toRemove >= 0)
+      fr[toRemove] = std::move(f);
+    else
+      fr.push_back(std::move(f));
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ entry points
+void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
+                 std::vector<std::vector<FragOut>> &out) {
+  validate(P);
+  if (mode != DCNS_MODE_ONE_GAP && mode != DCNS_MODE_TWO_GAP) throw Error(DCNS_ERR_INVALID, "mode must be 1 or 2");
+  for (const PairIn &p : pairs) {
+    if ((p.n1 > 0 && !p.s1) || (p.n2 > 0 && !p.s2)) throw Error(DCNS_ERR_INVALID, "NULL sequence");
+    if (p.n1 >= (1 << 24) - 2 || p.n2 >= (1 << 24) - 2) throw Error(DCNS_ERR_INVALID, "sequences must be < 16M bases");
+  }
+  auto t0 = Clock::now();
+  C.stats = dcns_stats{};
+  const int64_t np = (int64_t)pairs.size();
+  out.assign(np, {});
+  if (np == 0) return;
+  auto tu = Clock::now();
+  upload(C, pairs);
+  C.stats.ms_upload = ms_since(tu);
+  const bool one_gap = mode == DCNS_MODE_ONE_GAP;
+  std::vector<std::vector<Seed4>> linked;
+  scan_and_link(C, pairs, P, one_gap, linked);
+  std::vector<std::vector<XSeedOut>> xr;
+  extend_seeds(C, pairs, P, linked, one_gap, xr);
+  if (one_gap) {
+    parallel_for(np, [&](int64_t p) {
+      const double L1 = double(pairs[p].n1), L2 = double(pairs[p].n2);
+      std::vector<FragOut> &fr = out[p];
+      for (XSeedOut &x : xr[p]) {
+        if (!x.ok) continue;
+        double ev, pv;
+        evalue(P, L1, L2, x.score, ev, pv);
+        if (!(pv < P.pvalue)) continue;
+        FragOut f{(int64_t)x.start1 + 1, (int64_t)x.end1 + 1, (int64_t)x.start2 + 1, (int64_t)x.end2 + 1,
+                  (int64_t)(uint32_t)x.score, std::move(x.cigar), pv, ev};
+        bool fresh = true;
+        for (FragOut &g : fr) {  // :503-517: compares 0-based new ends with stored 1-based ones
+          if (g.s1 == f.s1 && g.s2 == f.s2) {
+            fresh = false;
+            if ((int64_t)x.end1 >= g.e1 && (int64_t)x.end2 >= g.e2) g = f;
+            break;
+          } else if (g.e1 == f.e1 && g.e2 == f.e2) {
+            fresh = false;
+            if ((int64_t)x.start1 <= g.s1 && (int64_t)x.start2 <= g.s2) g = f;
+            break;
+          }
+        }
+        if (fresh) fr.push_back(std::move(f));
+      }
+    });
+  } else {
+    // getAllExtendSeed's filter and x-seed merge (:395-427), then the 2-piece stage
+    std::vector<std::vector<Seed4>> xs(np);
+    for (int64_t p = 0; p < np; ++p) {
+      const double L1 = double(pairs[p].n1), L2 = double(pairs[p].n2);
+      for (XSeedOut &x : xr[p]) {
+        if (!x.ok) continue;
+        double ev, pv;
+        evalue(P, L1, L2, x.score, ev, pv);
+        if (!(pv < P.pvalue)) continue;
+        bool fresh = true;
+        for (Seed4 &y : xs[p]) {
+          if (y.s1 == x.start1 && y.s2 == x.start2) {
+            fresh = false;
+            if (x.end1 > y.e1 && x.end2 > y.e2) y.e1 = x.end1, y.e2 = x.end2;
+          } else if (y.e1 == x.end1 && y.e2 == x.end2) {
+            if (x.start1 < y.s1 && x.start2 < y.s2) y.s1 = x.start1, y.s2 = x.start2;
+            fresh = false;
+          }
+        }
+        if (fresh) xs[p].push_back(Seed4{x.start1, x.end1, x.start2, x.end2});
+      }
+    }
+    two_gap_stage(C, pairs, P, xs, out);
+  }
+  C.stats.ms_total = ms_since(t0);
+}
+
+void smith_waterman_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, int32_t *out) {
+  validate(P);
+  const int64_t n = (int64_t)tasks.size();
+  C.stats = dcns_stats{};
+  if (n == 0) return;
+  upload(C, tasks);
+  ScanState S;
+  for (int64_t k = 0; k < n; ++k) {
+    ScanTask T{};
+    T.pair = (int32_t)k;
+    T.s2 = 0;
+    T.tw = tasks[k].n2;
+    T.lo = 0;
+    T.hi = tasks[k].n1;
+    S.tasks.push_back(T);
+  }
+  Params Q = P;
+  Q.min_score = INT_MAX;  // maxima and positions only: no reverse scans
+  compute_scan_tasks(C, S, Q);
+  for (int64_t k = 0; k < n; ++k) {
+    const ScanTask &T = S.tasks[k];
+    out[3 * k] = T.score;
+    out[3 * k + 1] = T.score > 0 ? T.end1 : -1;
+    out[3 * k + 2] = T.score > 0 ? T.end2 : -1;
+  }
+}
+
+void xextend_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, bool want_cigar, int32_t *out,
+                   std::vector<std::vector<uint32_t>> &cigars) {
+  validate(P);
+  const int64_t n = (int64_t)tasks.size();
+  C.stats = dcns_stats{};
+  cigars.assign(n, {});
+  if (n == 0) return;
+  upload(C, tasks);
+  std::vector<XTask> X(n);
+  for (int64_t k = 0; k < n; ++k) {
+    XTask x{};
+    x.base1 = C.seq_base[2 * k];
+    x.base2 = C.seq_base[2 * k + 1];
+    x.n1 = tasks[k].n1;
+    x.n2 = tasks[k].n2;
+    x.dir = 0;
+    x.w = P.w;
+    X[k] = x;
+  }
+  run_xdrop(C, X, P, want_cigar, want_cigar ? &cigars : nullptr);
+  for (int64_t k = 0; k < n; ++k) {
+    out[6 * k + 0] = X[k].score;
+    out[6 * k + 1] = X[k].end1 - 1;
+    out[6 * k + 2] = X[k].end2 - 1;
+    out[6 * k + 3] = want_cigar ? X[k].iii : 0;
+    out[6 * k + 4] = want_cigar ? X[k].jjj : 0;
+    out[6 * k + 5] = (int32_t)cigars[k].size();
+  }
+}
+
+void semiglobal_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, bool want_cigar, int32_t *out,
+                      std::vector<std::vector<uint32_t>> &cigars) {
+  validate(P);
+  const int64_t n = (int64_t)tasks.size();
+  C.stats = dcns_stats{};
+  cigars.assign(n, {});
+  if (n == 0) return;
+  upload(C, tasks);
+  std::vector<SgTask> G(n);
+  for (int64_t k = 0; k < n; ++k) {
+    SgTask g{};
+    g.base1 = C.seq_base[2 * k];
+    g.base2 = C.seq_base[2 * k + 1];
+    g.n1 = tasks[k].n1;
+    g.n2 = tasks[k].n2;
+    g.dir = 0;
+    G[k] = g;
+  }
+  run_semiglobal(C, G, P, want_cigar, want_cigar ? &cigars : nullptr);
+  for (int64_t k = 0; k < n; ++k) {
+    out[4 * k + 0] = G[k].score;
+    out[4 * k + 1] = G[k].end1 - 1;
+    out[4 * k + 2] = G[k].end2 - 1;
+    out[4 * k + 3] = (int32_t)cigars[k].size();
+  }
+}
+
+void sliding_window(Context &C, const int8_t *const *seqs, const int32_t *lens, int32_t n, const Params &P,
+                    double *score, int32_t *max_out) {
+  validate(P);
+  C.stats = dcns_stats{};
+  if (n < 2) return;
+  // pair k-1 = (other sequence k as the scanned "reference", sequence 0 as the windowed "read"),
+  // as slidingWindowAlignment calls SmithWaterman(seq_i, refwindow, ...) (impl/slidingWindowAlignment.cpp:36)
+  std::vector<PairIn> pairs;
+  for (int32_t i = 1; i < n; ++i) pairs.push_back(PairIn{seqs[i], lens[i], seqs[0], lens[0]});
+  upload(C, pairs);
+  ScanState S;
+  const int32_t L0 = lens[0];
+  int32_t nw = 0;
+  std::vector<int32_t> tw_of;
+  {
+    int32_t tw = P.window;
+    for (int32_t j = 0; j < L0; j += P.step) {
+      if (tw + j > L0) tw = L0 - j;
+      tw_of.push_back(tw);
+      ++nw;
+    }
+  }
+  for (int32_t i = 1; i < n; ++i)
+    for (int32_t k = 0; k < nw; ++k) {
+      ScanTask T{};
+      T.pair = i - 1;
+      T.s2 = k * P.step;
+      T.tw = tw_of[k];
+      T.lo = 0;
+      T.hi = lens[i];
+      S.tasks.push_back(T);
+    }
+  Params Q = P;
+  Q.min_score = INT_MAX;
+  compute_scan_tasks(C, S, Q);
+  for (int32_t i = 1; i < n; ++i)
+    for (int32_t k = 0; k < nw; ++k) {
+      const ScanTask &T = S.tasks[(int64_t)(i - 1) * nw + k];
+      const int32_t md = std::min(tw_of[k], lens[i]) * P.match;
+      score[(int64_t)(i - 1) * nw + k] = double(T.score) / double(md);
+      max_out[(int64_t)(i - 1) * nw + k] = T.score;
+    }
+}
+
+}  // namespace dcns

@@ -1,0 +1,123 @@
+// Host side of the GB300 CNS pair-alignment engine: context, device buffers and the pipeline entry points that the
+// C ABI (capi.cpp) exposes.
+#pragma once
+
+#include <cstdint>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/dcns_gb300.h"
+#include "common.h"
+
+namespace dcns {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define DCNS_CK(x)                                                                                      \
+  do {                                                                                                  \
+    cudaError_t e_ = (x);                                                                               \
+    if (e_ != cudaSuccess) throw ::dcns::Error(DCNS_ERR_DEVICE, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct Context;
+
+// Grow-only device buffer accounted against the context's memory budget.
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  void ensure(Context &C, size_t bytes);
+  void release(Context &C);
+  template <class T>
+  T *as() const {
+    return (T *)p;
+  }
+};
+
+// Grow-only pinned host buffer (staging for host<->device copies).
+struct HostBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  void ensure(size_t bytes);
+  void release();
+  template <class T>
+  T *as() const {
+    return (T *)p;
+  }
+};
+
+struct PairIn {
+  const int8_t *s1;
+  int32_t n1;
+  const int8_t *s2;
+  int32_t n2;
+};
+
+struct FragOut {
+  int64_t s1, e1, s2, e2, score;  // 1-based, as PairedSimilarFragment
+  std::vector<uint32_t> cigar;
+  double p, e;
+};
+
+struct Seed4 {
+  int32_t s1, e1, s2, e2;  // 0-based inclusive
+};
+
+// The reference's Seed ordering (model/Seed.h:29-42): seeds sharing their start pair or their end pair compare equal,
+// otherwise lexicographic on (start1, start2).  Not a strict weak order: set contents depend on insertion order and
+// tree shape, so the replay below performs exactly the reference's insertion sequence on a libstdc++ std::set.
+struct SeedLess {
+  bool operator()(const Seed4 &a, const Seed4 &b) const {
+    if (a.s1 == b.s1 && a.s2 == b.s2) return false;
+    if (a.e1 == b.e1 && a.e2 == b.e2) return false;
+    if (a.s1 < b.s1) return true;
+    if (a.s1 == b.s1) return a.s2 < b.s2;
+    return false;
+  }
+};
+using SeedSet = std::set<Seed4, SeedLess>;
+
+struct Context {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  size_t budget = 0, used = 0;
+  int nsm = 0, scan_blocks_per_sm = 1;
+  std::string err;
+  dcns_stats stats{};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  // device buffers
+  DevBuf d_codes, d_srcoff, d_dstbase, d_len, d_pk, d_nm, d_seqbase, d_flag;
+  DevBuf d_tasks, d_keys, d_tiles, d_counter, d_idx, d_scratch;
+  DevBuf d_x, d_tb, d_cig, d_sg, d_sgtb, d_bnd;
+  // pinned staging
+  HostBuf h_codes, h_misc, h_out;
+
+  // arena layout of the current batch
+  std::vector<int64_t> seq_base;  // 2 per pair
+  Arena arena{};
+
+  ~Context();
+};
+
+Params to_params(const dcns_params *p);
+void validate(const Params &P);
+
+// Whole-path entry points (engine.cpp)
+void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
+                 std::vector<std::vector<FragOut>> &out);
+void smith_waterman_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, int32_t *out);
+void xextend_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, bool want_cigar, int32_t *out,
+                   std::vector<std::vector<uint32_t>> &cigars);
+void semiglobal_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, bool want_cigar, int32_t *out,
+                      std::vector<std::vector<uint32_t>> &cigars);
+void sliding_window(Context &C, const int8_t *const *seqs, const int32_t *lens, int32_t n, const Params &P,
+                    double *score, int32_t *max_out);
+
+int scan_occupancy();  // resident blocks per SM of the fast scan kernel (seedscan.cu)
+
+}  // namespace dcns

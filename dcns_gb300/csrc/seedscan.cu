@@ -1,0 +1,375 @@
+// Seed scan: windowed local Smith-Waterman of 38-bp query windows against the reference
+// (SmithWaterman(..., bool&), impl/sequenceAlignment3.cpp:220-469, driven by getSeeds,
+// impl/findSimilarFragmentsForPairedSequence4.cpp:61-201).
+//
+// Kernels
+//   pack_kernel         int8 dCNS codes -> 2-bit + N-mask arena (64-base aligned sequences)
+//   scan_kernel<W>      the hot loop: one thread owns two window tasks of one pair as the two int16 halves of every
+//                       register, scanning the same absolute reference rows; per cell 7.5 DPX/ALU ops for 2 cells
+//   scan_generic_kernel int32 lanes, any window width, both reference semantics (striped / scalar); used where the
+//                       fast kernel's static int16 bound or width does not hold
+//   reverse_kernel      the reverse-complement re-scan that fixes each seed's start (getSeeds :156-166)
+//
+// Semantics reproduced exactly (striped kernels of the reference): per reference row i
+//   Hpre[p] = max(H[i-1][p-1] + s(ref_i, read_p), E[p], 0)
+//   E[p]    = max(E[p] + ext, Hpre[p] + open)            (from Hpre, before the horizontal pass)
+//   F_p     = max(H[i][p-1] + open, F_{p-1} + ext)       (left to right)
+//   H[i][p] = max(Hpre[p], F_p)
+// and the reported position is the first (i-major, p-minor) cell holding the maximum.
+#include <climits>
+
+#include "device_common.cuh"
+
+namespace dcns {
+
+// ------------------------------------------------------------------ packing
+__global__ void pack_kernel(const int8_t *__restrict__ codes, const int64_t *__restrict__ src_off,
+                            const int64_t *__restrict__ dst_base, const int32_t *__restrict__ len,
+                            uint32_t *__restrict__ pk, uint32_t *__restrict__ nm) {
+  const int s = blockIdx.x;
+  const int64_t so = src_off[s], db = dst_base[s];
+  const int32_t n = len[s];
+  const int ngroups = ((n + 63) / 64) * 2;  // 32-base groups covering whole 64-base blocks
+  for (int g = threadIdx.x; g < ngroups; g += blockDim.x) {
+    uint32_t w0 = 0, w1 = 0, nb = 0;
+    for (int t = 0; t < 32; ++t) {
+      const int idx = g * 32 + t;
+      if (idx >= n) break;
+      const int c = codes[so + idx];
+      uint32_t two = 0;
+      if (c == 1)
+        two = 1;
+      else if (c == 3)
+        two = 2;
+      else if (c == 4)
+        two = 3;
+      else if (c != 0)
+        nb |= 1u << t;
+      if (t < 16)
+        w0 |= two << (2 * t);
+      else
+        w1 |= two << (2 * (t - 16));
+    }
+    pk[(db >> 4) + 2 * g] = w0;
+    pk[(db >> 4) + 2 * g + 1] = w1;
+    nm[(db >> 5) + g] = nb;
+  }
+}
+
+void launch_pack(const int8_t *codes, const int64_t *src_off, const int64_t *dst_base, const int32_t *len, int nseq,
+                 uint32_t *pk, uint32_t *nm, cudaStream_t st) {
+  if (nseq > 0) pack_kernel<<<nseq, 128, 0, st>>>(codes, src_off, dst_base, len, pk, nm);
+}
+
+// ------------------------------------------------------------------ fast int16x2 scan
+__device__ __forceinline__ uint32_t pack2(int v) { return (uint32_t)(uint16_t)(int16_t)v * 0x00010001u; }
+
+// prmt with sign-replicating selectors: selector nibble (k | 8) yields the sign of byte k, so (k, k|8) sign-extends
+// table byte k into a 16-bit lane.
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t s) {
+  uint32_t d;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(s));
+  return d;
+}
+
+__device__ __forceinline__ int half_s16(uint32_t v, int h) { return (int)(int16_t)(h ? (v >> 16) : (v & 0xFFFF)); }
+
+__device__ __forceinline__ int min_above(int cur, int a, int b, int c, int d, int e, int f) {
+  int m = INT_MAX;
+  if (a > cur && a < m) m = a;
+  if (b > cur && b < m) m = b;
+  if (c > cur && c < m) m = c;
+  if (d > cur && d < m) m = d;
+  if (e > cur && e < m) m = e;
+  if (f > cur && f < m) m = f;
+  return m;
+}
+
+template <int W>
+__global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ tiles, int ntiles, Arena ar, int open,
+                                                   int ext, int match, int mismatch,
+                                                   unsigned long long *__restrict__ keys, int *__restrict__ counter) {
+  // Score table per reference symbol (index = 2-bit code | N << 2): bytes 0..4 = s(ref, read code 0..4),
+  // byte 5 = the kill score used by padding columns, bytes 6..7 = 0.
+  __shared__ uint32_t tab[16];
+  if (threadIdx.x < 8) {
+    const int idx = threadIdx.x;
+    const int c = (idx & 4) ? 2 : ((idx & 3) + ((idx & 3) >> 1));
+    uint32_t lo = 0, hi = 0;
+    for (int r = 0; r < 5; ++r) {
+      const uint32_t b = (uint32_t)(uint8_t)(int8_t)score_of(c, r, match, mismatch);
+      if (r < 4)
+        lo |= b << (8 * r);
+      else
+        hi |= b;
+    }
+    hi |= (uint32_t)(uint8_t)(int8_t)kKillScore << 8;
+    tab[2 * idx] = lo;
+    tab[2 * idx + 1] = hi;
+  }
+  __syncthreads();
+  const uint32_t open2 = pack2(open), ext2 = pack2(ext);
+
+  for (;;) {
+    const int t = atomicAdd(counter, 1);
+    if (t >= ntiles) break;
+    const ScanTile tl = tiles[t];
+
+    uint32_t sel[W], H[W], E[W];
+#pragma unroll
+    for (int p = 0; p < W; ++p) {
+      const int ra = p < tl.tw[0] ? base_code(ar, tl.qry_base + tl.s2[0] + p) : kKillCode;
+      const int rb = p < tl.tw[1] ? base_code(ar, tl.qry_base + tl.s2[1] + p) : kKillCode;
+      sel[p] = (uint32_t)(ra | ((ra | 8) << 4) | (rb << 8) | ((rb | 8) << 12));
+      H[p] = 0;
+      E[p] = 0;
+    }
+
+    // Row events: a half whose task starts after row_begin is zeroed at its first row; each half counts maxima only
+    // on its own rows within [cnt_begin, row_end).
+    int zr0 = tl.lo[0] > tl.row_begin ? tl.lo[0] : INT_MAX;
+    int zr1 = tl.lo[1] > tl.row_begin ? tl.lo[1] : INT_MAX;
+    int cs0 = max(tl.lo[0], tl.cnt_begin), ce0 = min(tl.hi[0], tl.row_end);
+    int cs1 = max(tl.lo[1], tl.cnt_begin), ce1 = min(tl.hi[1], tl.row_end);
+    if (tl.task[0] < 0 || cs0 >= ce0) cs0 = ce0 = INT_MAX;
+    if (tl.task[1] < 0 || cs1 >= ce1) cs1 = ce1 = INT_MAX;
+    uint32_t cmpb = 0x7FFF7FFFu;  // per-half threshold: the running best while counting, unreachable otherwise
+    int best0 = 0, best1 = 0, brow0 = -1, brow1 = -1, bcol0 = -1, bcol1 = -1;
+
+    int r = tl.row_begin;
+    int nev = min_above(r - 1, zr0, zr1, cs0, ce0, cs1, ce1);
+    int64_t rk = tl.ref_base + r;
+    uint32_t wcur = __ldg(ar.pk + (rk >> 4)) >> (2u * (uint32_t)(rk & 15));
+    uint32_t ncur = __ldg(ar.nm + (rk >> 5)) >> (uint32_t)(rk & 31);
+
+    for (; r < tl.row_end; ++r) {
+      if (r == nev) {
+        if (zr0 == r) {
+#pragma unroll
+          for (int p = 0; p < W; ++p) {
+            H[p] &= 0xFFFF0000u;
+            E[p] &= 0xFFFF0000u;
+          }
+        }
+        if (zr1 == r) {
+#pragma unroll
+          for (int p = 0; p < W; ++p) {
+            H[p] &= 0x0000FFFFu;
+            E[p] &= 0x0000FFFFu;
+          }
+        }
+        if (cs0 == r) cmpb = (cmpb & 0xFFFF0000u) | (uint32_t)(uint16_t)best0;
+        if (ce0 == r) cmpb |= 0x7FFFu;
+        if (cs1 == r) cmpb = (cmpb & 0x0000FFFFu) | ((uint32_t)(uint16_t)best1 << 16);
+        if (ce1 == r) cmpb = (cmpb & 0x0000FFFFu) | 0x7FFF0000u;
+        nev = min_above(r, zr0, zr1, cs0, ce0, cs1, ce1);
+      }
+      const int idx = (int)((wcur & 3u) | ((ncur & 1u) << 2));
+      const uint32_t T0 = tab[2 * idx], T1 = tab[2 * idx + 1];
+      ++rk;
+      wcur >>= 2;
+      ncur >>= 1;
+      if ((rk & 15) == 0) wcur = __ldg(ar.pk + (rk >> 4));
+      if ((rk & 31) == 0) ncur = __ldg(ar.nm + (rk >> 5));
+
+      uint32_t diag = 0, F = 0, u = open2, rmax = 0, hprev = 0;
+#pragma unroll
+      for (int p = 0; p < W; ++p) {
+        const uint32_t s = prmt(T0, T1, sel[p]);
+        const uint32_t hp = __viaddmax_s16x2_relu(diag, s, E[p]);
+        diag = H[p];
+        E[p] = __viaddmax_s16x2(E[p], ext2, __vadd2(hp, open2));
+        F = __viaddmax_s16x2(F, ext2, u);
+        const uint32_t h = __vmaxs2(hp, F);
+        H[p] = h;
+        u = __vadd2(h, open2);
+        if (p & 1)
+          rmax = __vimax3_s16x2(rmax, hprev, h);
+        else if (p == W - 1)
+          rmax = __vmaxs2(rmax, h);
+        else
+          hprev = h;
+      }
+      const uint32_t gt = __vcmpgts2(rmax, cmpb);
+      if (gt) {
+        if (gt & 0xFFFFu) {
+          const int v = half_s16(rmax, 0);
+          int col = W - 1;
+#pragma unroll
+          for (int p = W - 1; p >= 0; --p)
+            if (half_s16(H[p], 0) == v) col = p;
+          best0 = v;
+          brow0 = r;
+          bcol0 = col;
+          cmpb = (cmpb & 0xFFFF0000u) | (uint32_t)(uint16_t)v;
+        }
+        if (gt & 0xFFFF0000u) {
+          const int v = half_s16(rmax, 1);
+          int col = W - 1;
+#pragma unroll
+          for (int p = W - 1; p >= 0; --p)
+            if (half_s16(H[p], 1) == v) col = p;
+          best1 = v;
+          brow1 = r;
+          bcol1 = col;
+          cmpb = (cmpb & 0x0000FFFFu) | ((uint32_t)(uint16_t)v << 16);
+        }
+      }
+    }
+    if (tl.task[0] >= 0 && best0 > 0) atomicMax(keys + tl.task[0], scan_key(best0, brow0, bcol0));
+    if (tl.task[1] >= 0 && best1 > 0) atomicMax(keys + tl.task[1], scan_key(best1, brow1, bcol1));
+  }
+}
+
+void launch_scan(const ScanTile *tiles, int ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
+                 int grid, cudaStream_t st) {
+  if (ntiles <= 0) return;
+  scan_kernel<kScanW><<<grid, 128, 0, st>>>(tiles, ntiles, ar, p.open1, p.ext1, p.match, p.mismatch, keys,
+                                            work_counter);
+}
+
+// ------------------------------------------------------------------ generic int32 Smith-Waterman (one thread)
+// Sequences are accessed through callables; H/Hp/E are per-thread arrays of nb entries.  Returns the maximum and its
+// first position (0-based) exactly as the reference kernel selected by `striped` would.
+template <class A, class B>
+__device__ void sw_one(A sa, int na, B sb, int nb, int open, int ext, int match, int mismatch, bool striped,
+                       int32_t *H, int32_t *Hp, int32_t *E, int &best, int &bi, int &bj) {
+  best = 0;
+  bi = -1;
+  bj = -1;
+  if (nb <= 0) return;
+  if (striped) {
+    for (int p = 0; p < nb; ++p) H[p] = 0, E[p] = 0;
+    for (int i = 0; i < na; ++i) {
+      const int ci = sa(i);
+      int diag = 0;
+      for (int p = 0; p < nb; ++p) {
+        int h = max(diag + score_of(ci, sb(p), match, mismatch), 0);
+        h = max(h, E[p]);
+        Hp[p] = h;
+        E[p] = max(max(E[p] + ext, h + open), 0);
+        diag = H[p];
+      }
+      int del = 0, left = 0;
+      for (int p = 0; p < nb; ++p) {
+        del = max(left + open, del + ext);
+        const int h = Hp[p] < del ? del : Hp[p];
+        del = max(del, 0);
+        H[p] = h;
+        left = h;
+        if (h > best) best = h, bi = i, bj = p;
+      }
+    }
+  } else {
+    // scalar kernel: H holds the previous row (index p+1 = column p), Hp the current row, E the vertical gap
+    for (int p = 0; p <= nb; ++p) H[p] = 0, Hp[p] = 0, E[p] = 0;
+    for (int i = 0; i < na; ++i) {
+      const int ci = sa(i);
+      int e = 0;
+      for (int j = 1; j <= nb; ++j) {
+        e = max(open + Hp[j - 1], ext + e);
+        E[j] = max(open + H[j], ext + E[j]);
+        int v = max(score_of(ci, sb(j - 1), match, mismatch) + H[j - 1], e);
+        v = max(v, E[j]);
+        Hp[j] = max(v, 0);
+        E[j] = max(E[j], 0);
+        e = max(e, 0);
+        if (v > best) best = v, bi = i, bj = j - 1;
+      }
+      for (int j = 0; j <= nb; ++j) {
+        const int tmp = H[j];
+        H[j] = Hp[j];
+        Hp[j] = tmp;
+      }
+    }
+  }
+}
+
+// The reference's kernel choice for an (nref x nread) call (impl/sequenceAlignment3.cpp:223-225, :338-339).
+__host__ __device__ inline bool striped_for(int nref, int nread, int open, int ext, int match) {
+  auto ok = [&](int lim) {
+    return ((-nref * ext - open) < lim || (-nread * ext - open) < lim) && (nref * match < lim || nread * match < lim);
+  };
+  return ok(125) || ok(32767);
+}
+
+__global__ void scan_generic_kernel(const ScanTask *__restrict__ tasks, const int *__restrict__ idx, int n,
+                                    const int64_t *__restrict__ seq_base, Arena ar, Params P,
+                                    unsigned long long *__restrict__ keys, int32_t *scratch, int64_t per_thread) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int ti = idx[k];
+  const ScanTask T = tasks[ti];
+  const int64_t b1 = seq_base[2 * T.pair], b2 = seq_base[2 * T.pair + 1];
+  int32_t *H = scratch + per_thread * k;
+  int32_t *Hp = H + (T.tw + 1);
+  int32_t *E = Hp + (T.tw + 1);
+  int best, bi, bj;
+  sw_one([&](int i) { return base_code(ar, b1 + T.lo + i); }, T.hi - T.lo,
+         [&](int p) { return base_code(ar, b2 + T.s2 + p); }, T.tw, P.open1, P.ext1, P.match, P.mismatch,
+         T.striped != 0, H, Hp, E, best, bi, bj);
+  keys[ti] = best > 0 ? scan_key(best, T.lo + bi, bj) : 0ull;
+}
+
+void launch_scan_generic(const ScanTask *tasks, const int *idx, int n, const int64_t *seq_base, Arena ar, Params p,
+                         unsigned long long *keys, int32_t *scratch, int64_t scratch_per_thread, cudaStream_t st) {
+  if (n <= 0) return;
+  scan_generic_kernel<<<(n + 127) / 128, 128, 0, st>>>(tasks, idx, n, seq_base, ar, p, keys, scratch,
+                                                       scratch_per_thread);
+}
+
+// ------------------------------------------------------------------ reverse scan -> seed start
+// For every task whose maximum reaches min_score: re-scan the reverse complements ending at the maximum,
+// e1 = min(end1_local + 1, tw + window) reference bases by e2 = min(end2_local + 1, tw + window) query bases
+// (getSeeds :150-166); start = end - (reverse end).
+constexpr int kRevMax = 128;
+
+__global__ void reverse_kernel(ScanTask *__restrict__ tasks, int first, int n,
+                               const unsigned long long *__restrict__ keys, const int64_t *__restrict__ seq_base,
+                               Arena ar, Params P) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  ScanTask &T = tasks[first + k];
+  int score = 0, row = -1, col = -1;
+  const unsigned long long key = keys[first + k];
+  if (key) scan_unkey(key, score, row, col);
+  T.score = score;
+  T.end1 = score > 0 ? row : -1;
+  T.end2 = score > 0 ? T.s2 + col : -1;
+  T.start1 = -1;
+  T.start2 = -1;
+  if (score < P.min_score) return;
+  const int lim = T.tw + P.window;
+  const int e1 = min(row - T.lo + 1, lim), e2 = min(col + 1, lim);
+  const int64_t b1 = seq_base[2 * T.pair], b2 = seq_base[2 * T.pair + 1];
+  const int end1 = row, end2 = T.s2 + col;
+  int32_t H[kRevMax + 1], Hp[kRevMax + 1], E[kRevMax + 1];
+  int best, bi, bj;
+  if (e2 > kRevMax) return;  // windows wider than kRevMax are rejected by the host before launch
+  sw_one([&](int i) { return 4 - base_code(ar, b1 + end1 - i); }, e1,
+         [&](int p) { return 4 - base_code(ar, b2 + end2 - p); }, e2, P.open1, P.ext1, P.match, P.mismatch,
+         striped_for(e1, e2, P.open1, P.ext1, P.match), H, Hp, E, best, bi, bj);
+  T.start1 = end1 - bi;
+  T.start2 = end2 - bj;
+}
+
+void launch_reverse(ScanTask *tasks, int first, int n, const unsigned long long *keys, const int64_t *pair_base,
+                    const int32_t *pair_len, Arena ar, Params p, cudaStream_t st) {
+  (void)pair_len;
+  if (n <= 0) return;
+  reverse_kernel<<<(n + 127) / 128, 128, 0, st>>>(tasks, first, n, keys, pair_base, ar, p);
+}
+
+}  // namespace dcns
+
+namespace dcns {
+// Resident blocks per SM of the fast scan kernel at 128 threads (sizes the persistent grid).
+int scan_occupancy_impl() {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, scan_kernel<kScanW>, 128, 0) != cudaSuccess) {
+    (void)cudaGetLastError();
+    nb = 1;
+  }
+  return nb > 0 ? nb : 1;
+}
+}  // namespace dcns

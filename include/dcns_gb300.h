@@ -1,0 +1,144 @@
+/* dcns_gb300 — C ABI of the GB300 pairwise CNS alignment engine (one process, one GPU).
+ *
+ * Drop-in boundary for dCNS's pairwise conserved-sequence alignment path.  Each entry point replaces one reference
+ * interface (paths inside the dCNS project):
+ *
+ *   dcns_align_pairs(..., DCNS_MODE_ONE_GAP)   findSimilarFragmentsForPairedSequence, 1-gap overload
+ *                                              impl/findSimilarFragmentsForPairedSequence.h:26-32
+ *                                              (impl/findSimilarFragmentsForPairedSequence4.cpp:433; called by
+ *                                              cut1Gap controlLayer4.cpp:1411, pairCnsXExtend :212, multCns
+ *                                              impl/getCnsForMultipleSpecies.cpp:135)
+ *   dcns_align_pairs(..., DCNS_MODE_TWO_GAP)   findSimilarFragmentsForPairedSequence, 2-gap overload
+ *                                              impl/findSimilarFragmentsForPairedSequence.h:34-42
+ *                                              (impl/findSimilarFragmentsForPairedSequence4.cpp:752; cut2Gaps
+ *                                              controlLayer4.cpp:1584, pairCns2Gaps :355)
+ *   dcns_smith_waterman_batch                  SmithWaterman(..., bool &positions)  impl/sequenceAlignment.h:26-28
+ *   dcns_xextend_batch                         SemiGlobal_xextend (both overloads)  impl/sequenceAlignment.h:72-81
+ *   dcns_semiglobal_batch                      SemiGlobal (2-piece affine)          impl/sequenceAlignment.h:52-56
+ *   dcns_sliding_window                        slidingWindowAlignment    impl/slidingWindowAlignment.h:21-24
+ *
+ * Sequences cross the boundary as dCNS integer codes (int8: A=0 C=1 N=2 G=3 T=4, the output of
+ * SequenceCharToUInt8::seq_to_int8, with lower-case 'n' already removed as the reference's drivers do); reverse
+ * complements are derived on the device.  All pointers are host pointers owned by the caller unless stated.
+ * Fragment coordinates are 1-based and CIGAR words are packed (length << 4 | op), op 0=M 1=I 2=D, exactly as
+ * PairedSimilarFragment (model/PairedSimilarFragment.h:14-68).
+ *
+ * Errors: every call returns DCNS_OK (0) or a negative status; dcns_last_error() describes the last failure of the
+ * context.  There is no CPU fallback: without a usable GPU, dcns_ctx_create fails with DCNS_ERR_DEVICE.
+ * Threading: a context is single-stream and thread-compatible (one host thread per context at a time).
+ */
+#ifndef DCNS_GB300_H
+#define DCNS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DCNS_OK 0
+#define DCNS_ERR_INVALID (-1)   /* bad argument (codes outside 0..4, unsupported parameter range, NULL) */
+#define DCNS_ERR_NOMEM (-2)     /* device memory or memory budget exhausted */
+#define DCNS_ERR_DEVICE (-3)    /* CUDA error or no device */
+#define DCNS_ERR_TIMEOUT (-4)   /* a serving request did not finish in time */
+#define DCNS_ERR_NOTFOUND (-5)  /* unknown request ticket */
+#define DCNS_ERR_BUSY (-6)      /* serving queue full */
+
+#define DCNS_MODE_ONE_GAP 1
+#define DCNS_MODE_TWO_GAP 2
+
+typedef struct dcns_ctx dcns_ctx;
+
+/* Scoring and search parameters; defaults (dcns_params_default) are the reference's globals, controlLayer4.cpp:28-52. */
+typedef struct {
+  int32_t match, mismatch;          /* 2, -3 */
+  int32_t open1, ext1;              /* -4, -2 */
+  int32_t open2, ext2;              /* -45, 0  (second gap piece; 2-gap mode only) */
+  int32_t window, min_score, step;  /* 38, 40, 8 */
+  int32_t w, xdrop;                 /* 10, 20   x-drop band half-width and drop */
+  int32_t zdrop, bandwidth;         /* 50, 20000 */
+  int32_t max_align_len;            /* 0 = unlimited (cut2Gaps2's maximumAlignLength) */
+  double pvalue, lambda, kvalue;    /* 0.1, 0.382291, 0.006662 */
+} dcns_params;
+
+typedef struct {
+  const int8_t *seq1; /* reference codes */
+  int32_t len1;
+  const int8_t *seq2; /* query codes */
+  int32_t len2;
+} dcns_pair;
+
+/* Algorithmic DP cells (counted identically for CPU and GPU) and stage timings of the last call. */
+typedef struct {
+  int64_t cells_scan, cells_scan_reverse, cells_xdrop, cells_semiglobal;
+  int64_t tasks_scan, tasks_scan_speculative, seeds, xdrop_passes, semiglobal_dps;
+  double ms_upload, ms_scan, ms_replay, ms_xdrop, ms_semiglobal, ms_download, ms_total;
+  double ms_scan_kernel;  /* device time of the seed-scan kernel launches (CUDA events) */
+  int32_t scan_launches, kernel_launches;
+} dcns_stats;
+
+/* Results of one dcns_align_pairs call; owned by the library until dcns_results_free. */
+typedef struct {
+  int64_t n_pairs, n_fragments, n_cigar;
+  const int64_t *pair_offset;  /* [n_pairs + 1]: fragments of pair k are [pair_offset[k], pair_offset[k+1]) */
+  const int64_t *frag;         /* [n_fragments * 7]: start1, end1, start2, end2, score, cigar_offset, cigar_len */
+  const double *pvalue;        /* [n_fragments] */
+  const double *evalue;        /* [n_fragments] */
+  const uint32_t *cigar;       /* [n_cigar] */
+  dcns_stats stats;
+} dcns_results;
+
+void dcns_params_default(dcns_params *p);
+
+/* device: CUDA ordinal.  mem_budget: bytes of device memory the context may hold (0 = 80% of free memory). */
+int dcns_ctx_create(int device, size_t mem_budget, dcns_ctx **out);
+void dcns_ctx_destroy(dcns_ctx *ctx);
+const char *dcns_last_error(const dcns_ctx *ctx);
+/* The CUDA stream (cudaStream_t) all of the context's work is issued on. */
+void *dcns_ctx_stream(dcns_ctx *ctx);
+
+/* Batched pair alignment: every pair is aligned independently, as one call of the reference overload per pair. */
+int dcns_align_pairs(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, const dcns_params *params, int mode,
+                     dcns_results **out);
+void dcns_results_free(dcns_results *res);
+
+/* Stats of the context's last dcns_align_pairs call. */
+int dcns_last_stats(const dcns_ctx *ctx, dcns_stats *out);
+
+/* SmithWaterman(ref, read, ...) for n independent (ref, read) tasks.  out[3*k] = maxScore, out[3*k+1..2] = the
+ * 0-based first argmax (endPosition1, endPosition2); positions are -1 when maxScore is 0. */
+int dcns_smith_waterman_batch(dcns_ctx *ctx, const dcns_pair *tasks, int64_t n, const dcns_params *params,
+                              int32_t *out);
+
+/* SemiGlobal_xextend for n (seq1, seq2) tasks with the params' w and xdrop.  out[6*k..] = maxScore, endPosition1,
+ * endPosition2 (0-based), iii, jjj, cigar_len.  With want_cigar, CIGAR words go to cigar[cigar_offset[k] ..] where
+ * cigar_offset (n+1 entries) is filled by the call; cigar_cap bounds the total (DCNS_ERR_NOMEM when exceeded). */
+int dcns_xextend_batch(dcns_ctx *ctx, const dcns_pair *tasks, int64_t n, const dcns_params *params, int want_cigar,
+                       int32_t *out, uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_offset);
+
+/* SemiGlobal (2-piece affine, z-drop, band) for n tasks.  out[4*k..] = maxScore, endPosition1, endPosition2,
+ * cigar_len; CIGAR layout as for dcns_xextend_batch. */
+int dcns_semiglobal_batch(dcns_ctx *ctx, const dcns_pair *tasks, int64_t n, const dcns_params *params,
+                          int want_cigar, int32_t *out, uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_offset);
+
+/* slidingWindowAlignment for one reference (seqs[0]) against n_seqs-1 others: for window k (start k*step) and
+ * sequence i, score[(i-1) * n_windows + k] = maxScore / (min(window_len, len_i) * match) and max_out the integer
+ * maxima.  n_windows = ceil(len_0 / step); both outputs are caller-allocated. */
+int dcns_sliding_window(dcns_ctx *ctx, const int8_t *const *seqs, const int32_t *lens, int32_t n_seqs,
+                        const dcns_params *params, double *score, int32_t *max_out);
+
+/* Serving loop: continuous batching.  dcns_submit copies the pair and returns a ticket at once; requests are
+ * admitted to the device as memory allows and overlap with work already running.  dcns_poll returns DCNS_OK with
+ * the result when done, DCNS_ERR_BUSY while pending.  dcns_serve_wait blocks up to timeout_ms. */
+int dcns_serve_start(dcns_ctx *ctx, const dcns_params *params, int mode, int max_inflight_pairs);
+int dcns_submit(dcns_ctx *ctx, const dcns_pair *pair, uint64_t *ticket);
+int dcns_poll(dcns_ctx *ctx, uint64_t ticket, dcns_results **out);
+int dcns_serve_wait(dcns_ctx *ctx, uint64_t ticket, int64_t timeout_ms, dcns_results **out);
+int dcns_serve_stop(dcns_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DCNS_GB300_H */
