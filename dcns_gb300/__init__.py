@@ -158,6 +158,10 @@ def _bind(lib):
                                        _I64P]
     lib.dcns_semiglobal_batch.argtypes = lib.dcns_xextend_batch.argtypes
     lib.dcns_sliding_window.argtypes = [C.c_void_p, P(_I8P), _I32P, C.c_int32, P(Params), _F64P, _I32P]
+    lib.dcns_batch_upload.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(C.c_void_p)]
+    lib.dcns_align_batch.argtypes = [C.c_void_p, C.c_void_p, P(Params), C.c_int, P(P(Results))]
+    lib.dcns_batch_free.argtypes = [C.c_void_p, C.c_void_p]
+    lib.dcns_measure_scan_roofline.argtypes = [C.c_void_p, P(C.c_double)]
     lib.dcns_serve_start.argtypes = [C.c_void_p, P(Params), C.c_int, C.c_int]
     lib.dcns_submit.argtypes = [C.c_void_p, P(Pair), P(C.c_uint64)]
     lib.dcns_poll.argtypes = [C.c_void_p, C.c_uint64, P(P(Results))]
@@ -275,6 +279,32 @@ class Engine:
             return _unpack(res)
         finally:
             self.lib.dcns_results_free(res)
+
+    def upload(self, pairs):
+        """Pack pairs into device memory once; returns a handle for align_resident."""
+        arr, keep = _pairs(pairs)
+        b = C.c_void_p()
+        self._check(self.lib.dcns_batch_upload(self.h, arr, len(keep), C.byref(b)))
+        return b
+
+    def align_resident(self, batch, mode=MODE_ONE_GAP, **kw):
+        """align_pairs on sequences already resident on the device (upload())."""
+        p = params(**kw)
+        res = C.POINTER(Results)()
+        self._check(self.lib.dcns_align_batch(self.h, batch, C.byref(p), mode, C.byref(res)))
+        try:
+            return _unpack(res)
+        finally:
+            self.lib.dcns_results_free(res)
+
+    def free_batch(self, batch):
+        self.lib.dcns_batch_free(self.h, batch)
+
+    def measure_scan_roofline(self) -> float:
+        """GCUPS ceiling of the seed scan's instruction mix on this GPU, measured live."""
+        g = C.c_double()
+        self._check(self.lib.dcns_measure_scan_roofline(self.h, C.byref(g)))
+        return float(g.value)
 
     def findSimilarFragmentsForPairedSequence(self, seq1, seq2, two_gap=False, **kw):
         """One pair, the reference's 1-gap (default) or 2-gap overload."""

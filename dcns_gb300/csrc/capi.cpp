@@ -80,6 +80,10 @@ struct dcns_ctx {
   std::unique_ptr<Server> srv;
 };
 
+struct dcns_batch {
+  Batch B;
+};
+
 namespace {
 
 int fail(dcns_ctx *ctx, const Error &e) {
@@ -257,6 +261,50 @@ int dcns_align_pairs(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, con
 }
 
 void dcns_results_free(dcns_results *res) { delete reinterpret_cast<ResultsImpl *>(res); }
+
+int dcns_batch_upload(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, dcns_batch **out) {
+  if (!ctx || !out) return DCNS_ERR_INVALID;
+  *out = nullptr;
+  auto *b = new dcns_batch;
+  int rc = guarded(ctx, [&] { batch_upload(ctx->C, to_pairs(pairs, n_pairs), b->B); });
+  if (rc != DCNS_OK) {
+    dcns_batch_free(ctx, b);
+    return rc;
+  }
+  *out = b;
+  return DCNS_OK;
+}
+
+int dcns_align_batch(dcns_ctx *ctx, dcns_batch *batch, const dcns_params *params, int mode, dcns_results **out) {
+  if (!ctx || !batch || !params || !out) return DCNS_ERR_INVALID;
+  *out = nullptr;
+  return guarded(ctx, [&] {
+    std::vector<std::vector<FragOut>> fr;
+    align_batch(ctx->C, batch->B, to_params(params), mode, fr);
+    auto *R = new ResultsImpl;
+    R->finish(fr, ctx->C.stats);
+    *out = &R->pub;
+  });
+}
+
+void dcns_batch_free(dcns_ctx *ctx, dcns_batch *batch) {
+  if (!batch) return;
+  if (ctx) {
+    batch->B.pk.release(ctx->C);
+    batch->B.nm.release(ctx->C);
+    batch->B.sb.release(ctx->C);
+  }
+  delete batch;
+}
+
+int dcns_measure_scan_roofline(dcns_ctx *ctx, double *gcups) {
+  if (!ctx || !gcups) return DCNS_ERR_INVALID;
+  return guarded(ctx, [&] {
+    const double pairs_per_s = measure_issue_rate(ctx->C.nsm, ctx->C.st);
+    DCNS_CK(cudaGetLastError());
+    *gcups = 2.0 * pairs_per_s / 1e9;
+  });
+}
 
 int dcns_last_stats(const dcns_ctx *ctx, dcns_stats *out) {
   if (!ctx || !out) return DCNS_ERR_INVALID;

@@ -175,9 +175,10 @@ bool striped_for_host(int nref, int nread, int open, int ext, int match) {
 }
 
 // ------------------------------------------------------------------ 1. upload + pack
-void upload(Context &C, const std::vector<PairIn> &pairs) {
+void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, DevBuf &d_nm, DevBuf &d_sb,
+                 std::vector<int64_t> &seq_base, Arena &arena) {
   const int64_t np = (int64_t)pairs.size(), ns = 2 * np;
-  C.seq_base.assign(ns, 0);
+  seq_base.assign(ns, 0);
   std::vector<int64_t> src_off(ns);
   std::vector<int32_t> len(ns);
   int64_t total_src = 0, total_dst = 0;
@@ -187,7 +188,7 @@ void upload(Context &C, const std::vector<PairIn> &pairs) {
       if (n < 0) throw Error(DCNS_ERR_INVALID, "negative sequence length");
       len[2 * k + h] = n;
       src_off[2 * k + h] = total_src;
-      C.seq_base[2 * k + h] = total_dst;
+      seq_base[2 * k + h] = total_dst;
       total_src += n;
       total_dst += ((int64_t)n + 63) / 64 * 64;
     }
@@ -204,22 +205,22 @@ void upload(Context &C, const std::vector<PairIn> &pairs) {
   C.d_srcoff.ensure(C, sizeof(int64_t) * ns + 8);
   C.d_dstbase.ensure(C, sizeof(int64_t) * ns + 8);
   C.d_len.ensure(C, sizeof(int32_t) * ns + 8);
-  C.d_seqbase.ensure(C, sizeof(int64_t) * ns + 8);
-  C.d_pk.ensure(C, sizeof(uint32_t) * (total_dst / 16));
-  C.d_nm.ensure(C, sizeof(uint32_t) * (total_dst / 32));
+  d_sb.ensure(C, sizeof(int64_t) * ns + 8);
+  d_pk.ensure(C, sizeof(uint32_t) * (total_dst / 16));
+  d_nm.ensure(C, sizeof(uint32_t) * (total_dst / 32));
   C.d_flag.ensure(C, 64);
   h2d(C, C.d_codes, stage, (size_t)total_src);
   h2d(C, C.d_srcoff, src_off.data(), ns);
-  h2d(C, C.d_dstbase, C.seq_base.data(), ns);
+  h2d(C, C.d_dstbase, seq_base.data(), ns);
   h2d(C, C.d_len, len.data(), ns);
-  h2d(C, C.d_seqbase, C.seq_base.data(), ns);
-  DCNS_CK(cudaMemsetAsync(C.d_pk.p, 0, sizeof(uint32_t) * (total_dst / 16), C.st));
-  DCNS_CK(cudaMemsetAsync(C.d_nm.p, 0, sizeof(uint32_t) * (total_dst / 32), C.st));
+  h2d(C, d_sb, seq_base.data(), ns);
+  DCNS_CK(cudaMemsetAsync(d_pk.p, 0, sizeof(uint32_t) * (total_dst / 16), C.st));
+  DCNS_CK(cudaMemsetAsync(d_nm.p, 0, sizeof(uint32_t) * (total_dst / 32), C.st));
   launch_pack(C.d_codes.as<int8_t>(), C.d_srcoff.as<int64_t>(), C.d_dstbase.as<int64_t>(), C.d_len.as<int32_t>(),
-              (int)ns, C.d_pk.as<uint32_t>(), C.d_nm.as<uint32_t>(), C.st);
+              (int)ns, d_pk.as<uint32_t>(), d_nm.as<uint32_t>(), C.st);
   C.stats.kernel_launches += 1;
-  C.arena.pk = C.d_pk.as<uint32_t>();
-  C.arena.nm = C.d_nm.as<uint32_t>();
+  arena.pk = d_pk.as<uint32_t>();
+  arena.nm = d_nm.as<uint32_t>();
   // the reference indexes its 5x5 score table with the codes: anything outside 0..4 is rejected up front
   std::atomic<bool> badcode(false);
   parallel_for((total_src + (1 << 20) - 1) >> 20, [&](int64_t b) {
@@ -231,6 +232,12 @@ void upload(Context &C, const std::vector<PairIn> &pairs) {
       }
   });
   if (badcode) throw Error(DCNS_ERR_INVALID, "sequence codes must be dCNS codes 0..4 (A C N G T)");
+}
+
+// Uploads into the context's own buffers and makes them the current arena.
+void upload(Context &C, const std::vector<PairIn> &pairs) {
+  upload_into(C, pairs, C.d_pk, C.d_nm, C.d_seqbase, C.seq_base, C.arena);
+  C.seqbase_dev = C.d_seqbase.as<int64_t>();
 }
 
 // ------------------------------------------------------------------ 2./3. seed scan with recursion replay
@@ -362,12 +369,12 @@ void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
     C.d_idx.ensure(C, sizeof(int32_t) * generic.size());
     C.d_scratch.ensure(C, sizeof(int32_t) * per * generic.size());
     h2d(C, C.d_idx, generic.data(), generic.size());
-    launch_scan_generic(C.d_tasks.as<ScanTask>(), C.d_idx.as<int>(), (int)generic.size(), C.d_seqbase.as<int64_t>(),
+    launch_scan_generic(C.d_tasks.as<ScanTask>(), C.d_idx.as<int>(), (int)generic.size(), C.seqbase_dev,
                         C.arena, P, C.d_keys.as<unsigned long long>(), C.d_scratch.as<int32_t>(), per, C.st);
     C.stats.kernel_launches += 1;
   }
   launch_reverse(C.d_tasks.as<ScanTask>(), (int)first, (int)n, C.d_keys.as<unsigned long long>(),
-                 C.d_seqbase.as<int64_t>(), nullptr, C.arena, P, C.st);
+                 C.seqbase_dev, nullptr, C.arena, P, C.st);
   C.stats.kernel_launches += 1;
   d2h(C, S.tasks.data() + first, C.d_tasks, (size_t)n, (size_t)first);
   sync(C);
@@ -969,6 +976,9 @@ void two_gap_stage(Context &C, const std::vector<PairIn> &pairs, const Params &P
 }  // namespace
 
 // ------------------------------------------------------------------ entry points
+void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
+                std::vector<std::vector<FragOut>> &out);
+
 void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
                  std::vector<std::vector<FragOut>> &out) {
   validate(P);
@@ -979,12 +989,41 @@ void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, 
   }
   auto t0 = Clock::now();
   C.stats = dcns_stats{};
-  const int64_t np = (int64_t)pairs.size();
-  out.assign(np, {});
-  if (np == 0) return;
+  out.assign(pairs.size(), {});
+  if (pairs.empty()) return;
   auto tu = Clock::now();
   upload(C, pairs);
   C.stats.ms_upload = ms_since(tu);
+  align_core(C, pairs, P, mode, out);
+  C.stats.ms_total = ms_since(t0);
+}
+
+void batch_upload(Context &C, const std::vector<PairIn> &pairs, Batch &B) {
+  for (const PairIn &p : pairs)
+    if (p.n1 >= (1 << 24) - 2 || p.n2 >= (1 << 24) - 2) throw Error(DCNS_ERR_INVALID, "sequences must be < 16M bases");
+  upload_into(C, pairs, B.pk, B.nm, B.sb, B.seq_base, B.arena);
+  sync(C);
+  B.lens.clear();
+  for (const PairIn &p : pairs) B.lens.push_back(PairIn{nullptr, p.n1, nullptr, p.n2});
+}
+
+void align_batch(Context &C, Batch &B, const Params &P, int mode, std::vector<std::vector<FragOut>> &out) {
+  validate(P);
+  if (mode != DCNS_MODE_ONE_GAP && mode != DCNS_MODE_TWO_GAP) throw Error(DCNS_ERR_INVALID, "mode must be 1 or 2");
+  auto t0 = Clock::now();
+  C.stats = dcns_stats{};
+  out.assign(B.lens.size(), {});
+  if (B.lens.empty()) return;
+  C.arena = B.arena;
+  C.seq_base = B.seq_base;
+  C.seqbase_dev = B.sb.as<int64_t>();
+  align_core(C, B.lens, P, mode, out);
+  C.stats.ms_total = ms_since(t0);
+}
+
+void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
+                std::vector<std::vector<FragOut>> &out) {
+  const int64_t np = (int64_t)pairs.size();
   const bool one_gap = mode == DCNS_MODE_ONE_GAP;
   std::vector<std::vector<Seed4>> linked;
   scan_and_link(C, pairs, P, one_gap, linked);
@@ -1041,7 +1080,6 @@ void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, 
     }
     two_gap_stage(C, pairs, P, xs, out);
   }
-  C.stats.ms_total = ms_since(t0);
 }
 
 void smith_waterman_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, int32_t *out) {

@@ -97,9 +97,10 @@ struct Context {
   // pinned staging
   HostBuf h_codes, h_misc, h_out;
 
-  // arena layout of the current batch
+  // arena layout of the batch being aligned (the context's own upload buffers, or a resident batch)
   std::vector<int64_t> seq_base;  // 2 per pair
   Arena arena{};
+  const int64_t *seqbase_dev = nullptr;
 
   ~Context();
 };
@@ -107,9 +108,20 @@ struct Context {
 Params to_params(const dcns_params *p);
 void validate(const Params &P);
 
+// Sequences packed and resident on the device (dcns_batch_upload).
+struct Batch {
+  DevBuf pk, nm, sb;
+  std::vector<int64_t> seq_base;
+  std::vector<PairIn> lens;  // lengths only (sequence pointers are not kept)
+  Arena arena{};
+};
+
 // Whole-path entry points (engine.cpp)
 void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
                  std::vector<std::vector<FragOut>> &out);
+void batch_upload(Context &C, const std::vector<PairIn> &pairs, Batch &B);
+void align_batch(Context &C, Batch &B, const Params &P, int mode, std::vector<std::vector<FragOut>> &out);
+double measure_issue_rate(int nsm, cudaStream_t st);
 void smith_waterman_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, int32_t *out);
 void xextend_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, bool want_cigar, int32_t *out,
                    std::vector<std::vector<uint32_t>> &cigars);

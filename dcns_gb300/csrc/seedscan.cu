@@ -373,3 +373,58 @@ int scan_occupancy_impl() {
   return nb > 0 ? nb : 1;
 }
 }  // namespace dcns
+
+namespace dcns {
+// ------------------------------------------------------------------ integer-issue roofline probe
+// Runs the scan kernel's per-cell instruction sequence (prmt lookup, fused add-max-relu, E and F updates, H merge,
+// row maximum every second column) on 8 independent chains per thread at full occupancy, so the only limit is
+// instruction issue.  Each chain step is one int16x2 cell pair of the scan; the result is an upper bound for the
+// scan's cells per second with exactly its instruction mix.
+__global__ void __launch_bounds__(256) issue_probe_kernel(uint32_t *out, int iters, uint32_t seed) {
+  constexpr int NC = 8;
+  uint32_t d[NC], e[NC], f[NC], u[NC], rm[NC];
+  const uint32_t T0 = 0xFDFD02FDu ^ seed, T1 = 0x0000FDFDu, open2 = pack2(-4), ext2 = pack2(-2);
+  uint32_t sel = 0x00009810u + (threadIdx.x & 3);
+#pragma unroll
+  for (int c = 0; c < NC; ++c) d[c] = seed * (c + 1), e[c] = 0, f[c] = 0, u[c] = open2, rm[c] = 0;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const uint32_t s = prmt(T0, T1, sel + c);
+      const uint32_t hp = __viaddmax_s16x2_relu(d[c], s, e[c]);
+      e[c] = __viaddmax_s16x2(e[c], ext2, __vadd2(hp, open2));
+      f[c] = __viaddmax_s16x2(f[c], ext2, u[c]);
+      const uint32_t h = __vmaxs2(hp, f[c]);
+      u[c] = __vadd2(h, open2);
+      if (c & 1) rm[c] = __vimax3_s16x2(rm[c], d[c], h);
+      d[c] = h;
+    }
+  }
+  uint32_t acc = 0;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) acc ^= d[c] ^ e[c] ^ rm[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
+// Returns int16x2 cell pairs per second of the probe (each = one chain step).
+double measure_issue_rate(int nsm, cudaStream_t st) {
+  const int threads = 256, blocks = nsm * 8, iters = 1 << 14;
+  uint32_t *out = nullptr;
+  if (cudaMalloc(&out, sizeof(uint32_t) * threads * blocks) != cudaSuccess) return 0;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  issue_probe_kernel<<<blocks, threads, 0, st>>>(out, 256, 1u);  // warm-up
+  cudaEventRecord(a, st);
+  issue_probe_kernel<<<blocks, threads, 0, st>>>(out, iters, 7u);
+  cudaEventRecord(b, st);
+  cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  if (ms <= 0) return 0;
+  return (double)threads * blocks * iters * 8 / (ms * 1e-3);
+}
+}  // namespace dcns

@@ -36,39 +36,48 @@ def random_seq(rng: np.random.Generator, n: int, gc: float = 0.5) -> bytearray:
 
 
 def mutate(rng, seg: bytes, identity: float, indel_rate: float) -> bytes:
-    out = bytearray()
-    i = 0
-    n = len(seg)
-    while i < n:
-        if indel_rate > 0 and rng.random() < indel_rate:
-            k = int(rng.integers(1, 6))
-            if rng.random() < 0.5:
-                i += k  # deletion
-                continue
-            out += random_seq(rng, k)  # insertion
-        b = seg[i]
-        if rng.random() > identity:
-            b = _BASES[(np.searchsorted(_BASES, b) + int(rng.integers(1, 4))) % 4]
-        out.append(int(b))
-        i += 1
-    return bytes(out)
+    """Uniform substitutions to `identity`, then 1-5 bp insertions/deletions starting at rate `indel_rate`."""
+    arr = np.frombuffer(seg, dtype=np.uint8).copy()
+    n = len(arr)
+    sub = rng.random(n) > identity
+    if sub.any():
+        idx = np.searchsorted(_BASES, arr[sub])
+        arr[sub] = _BASES[(idx + rng.integers(1, 4, int(sub.sum()))) % 4]
+    if indel_rate <= 0:
+        return arr.tobytes()
+    parts, prev = [], 0
+    for p in np.nonzero(rng.random(n) < indel_rate)[0]:
+        if p < prev:
+            continue
+        parts.append(arr[prev:p].tobytes())
+        k = int(rng.integers(1, 6))
+        if rng.random() < 0.5:
+            prev = int(p) + k  # deletion
+        else:
+            parts.append(bytes(random_seq(rng, k)))  # insertion
+            prev = int(p)
+    parts.append(arr[prev:].tobytes())
+    return b"".join(parts)
 
 
 def mask_runs(rng, seq: bytearray, frac: float, lo: int, hi: int, soft: bool = False) -> None:
     """Mask about `frac` of the sequence in runs of lo..hi bp: 'n' (hard, deleted before alignment) or lower case."""
     n = len(seq)
+    arr = np.frombuffer(seq, dtype=np.uint8).copy()
+    upper = np.isin(arr, _BASES)
     target = int(frac * n)
     done = 0
-    guard = 0
-    while done < target and guard < 10000:
-        guard += 1
+    for _ in range(10000):
+        if done >= target:
+            break
         L = int(rng.integers(lo, hi + 1))
         s = int(rng.integers(0, max(1, n - L)))
-        for k in range(s, min(n, s + L)):
-            c = seq[k]
-            if c in b"ACGT":
-                seq[k] = ord(chr(c).lower()) if soft else ord("n")
-                done += 1
+        m = upper[s:s + L]
+        done += int(m.sum())
+        seg = arr[s:s + L]
+        seg[m] = (seg[m] + 32) if soft else ord("n")
+        upper[s:s + L] = False
+    seq[:] = arr.tobytes()
 
 
 def planted_pair(rng, n1: int, n2: int, nseg: int, seg_lo: int, seg_hi: int, id_lo: float, id_hi: float,

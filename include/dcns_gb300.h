@@ -103,6 +103,18 @@ int dcns_align_pairs(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, con
                      dcns_results **out);
 void dcns_results_free(dcns_results *res);
 
+/* Resident batches: dcns_batch_upload packs the pairs into device memory once; dcns_align_batch then runs the
+ * pipeline on the resident sequences (no sequence upload).  A batch belongs to the context that made it. */
+typedef struct dcns_batch dcns_batch;
+int dcns_batch_upload(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, dcns_batch **out);
+int dcns_align_batch(dcns_ctx *ctx, dcns_batch *batch, const dcns_params *params, int mode, dcns_results **out);
+void dcns_batch_free(dcns_ctx *ctx, dcns_batch *batch);
+
+/* Diagnostic: the integer-issue roofline of the seed scan on this device, measured live: the scan's exact per-cell
+ * instruction sequence (int16x2, two cells per instruction) run on independent chains at full occupancy.  Returns
+ * the GCUPS ceiling for that instruction mix at the clock the GPU ran during the probe. */
+int dcns_measure_scan_roofline(dcns_ctx *ctx, double *gcups);
+
 /* Stats of the context's last dcns_align_pairs call. */
 int dcns_last_stats(const dcns_ctx *ctx, dcns_stats *out);
 

@@ -240,3 +240,21 @@ def test_serving_same_alone_and_in_mix(eng):
     batch = eng.align_pairs(pairs, 1)
     for i in range(len(pairs)):
         assert frag_keys(res[i]) == frag_keys(batch[i]), i
+
+
+def test_resident_batch_matches_host_path(eng):
+    pairs = W.config2(n_pairs=64, seed=31)
+    b = eng.upload(pairs)
+    try:
+        r1 = eng.align_resident(b, 1)
+        r2 = eng.align_resident(b, 1)  # the batch stays resident and reusable
+    finally:
+        eng.free_batch(b)
+    ref = eng.align_pairs(pairs, 1)
+    for i in range(len(pairs)):
+        assert frag_keys(r1[i]) == frag_keys(ref[i]) == frag_keys(r2[i]), i
+
+
+def test_scan_roofline_probe_positive(eng):
+    g = eng.measure_scan_roofline()
+    assert 100.0 < g < 1e6
