@@ -103,7 +103,8 @@ class Stats(C.Structure):
                                          "tasks_scan", "tasks_scan_speculative", "seeds", "xdrop_passes",
                                          "semiglobal_dps")] + \
                [(n, C.c_double) for n in ("ms_upload", "ms_scan", "ms_replay", "ms_xdrop", "ms_semiglobal",
-                                          "ms_download", "ms_total", "ms_scan_kernel")] + \
+                                          "ms_download", "ms_total", "ms_scan_kernel", "ms_scan_prep",
+                                          "ms_scan_xfer", "ms_link")] + \
                [("scan_launches", C.c_int32), ("kernel_launches", C.c_int32)]
 
     def as_dict(self):
@@ -209,28 +210,53 @@ def _pairs(pairs):
     return arr, keep
 
 
-def _unpack(res, nonempty=True):
+class FragmentList:
+    """The fragments of one pair, materialised lazily from the flat result arrays."""
+
+    __slots__ = ("_frag", "_pv", "_ev", "_cg", "_lo", "_hi")
+
+    def __init__(self, frag, pv, ev, cg, lo, hi):
+        self._frag, self._pv, self._ev, self._cg, self._lo, self._hi = frag, pv, ev, cg, lo, hi
+
+    def __len__(self):
+        return self._hi - self._lo
+
+    def __getitem__(self, k):
+        if isinstance(k, slice):
+            return [self[i] for i in range(*k.indices(len(self)))]
+        if k < 0:
+            k += len(self)
+        if not 0 <= k < len(self):
+            raise IndexError(k)
+        i = self._lo + k
+        r = self._frag[i]
+        return Fragment(int(r[0]), int(r[1]), int(r[2]), int(r[3]), int(r[4]),
+                        self._cg[int(r[5]):int(r[5]) + int(r[6])].tolist(), float(self._pv[i]), float(self._ev[i]))
+
+    def __iter__(self):
+        return (self[k] for k in range(len(self)))
+
+    def __eq__(self, other):
+        return list(self) == list(other)
+
+    def __repr__(self):
+        return f"FragmentList({list(self)!r})"
+
+
+def _unpack(res):
+    """Copies the flat C results into numpy arrays; per-pair views build Fragment objects only when accessed."""
     R = res.contents
     n = int(R.n_pairs)
-    out = []
     if n == 0:
-        return out
+        return []
     off = np.ctypeslib.as_array(R.pair_offset, shape=(n + 1,)).copy()
     nf = int(R.n_fragments)
-    frag = np.ctypeslib.as_array(R.frag, shape=(max(nf, 1) * 7,))[:nf * 7].reshape(nf, 7).copy() if nf else \
-        np.zeros((0, 7), np.int64)
-    pv = np.ctypeslib.as_array(R.pvalue, shape=(max(nf, 1),))[:nf].copy() if nf else np.zeros(0)
-    ev = np.ctypeslib.as_array(R.evalue, shape=(max(nf, 1),))[:nf].copy() if nf else np.zeros(0)
     nc = int(R.n_cigar)
-    cg = np.ctypeslib.as_array(R.cigar, shape=(max(nc, 1),))[:nc].copy() if nc else np.zeros(0, np.uint32)
-    for k in range(n):
-        fr = []
-        for i in range(int(off[k]), int(off[k + 1])):
-            r = frag[i]
-            fr.append(Fragment(int(r[0]), int(r[1]), int(r[2]), int(r[3]), int(r[4]),
-                               [int(c) for c in cg[int(r[5]):int(r[5]) + int(r[6])]], float(pv[i]), float(ev[i])))
-        out.append(fr)
-    return out
+    frag = np.ctypeslib.as_array(R.frag, shape=(nf * 7,)).reshape(nf, 7).copy() if nf else np.zeros((0, 7), np.int64)
+    pv = np.ctypeslib.as_array(R.pvalue, shape=(nf,)).copy() if nf else np.zeros(0)
+    ev = np.ctypeslib.as_array(R.evalue, shape=(nf,)).copy() if nf else np.zeros(0)
+    cg = np.ctypeslib.as_array(R.cigar, shape=(nc,)).copy() if nc else np.zeros(0, np.uint32)
+    return [FragmentList(frag, pv, ev, cg, int(off[k]), int(off[k + 1])) for k in range(n)]
 
 
 class Engine:

@@ -14,8 +14,6 @@ namespace dcns {
 
 constexpr int32_t kOut = -536870912;  // score of cells outside a band (impl/sequenceAlignment3.cpp:34)
 constexpr int kScanW = 38;            // window width the fast seed-scan kernel is specialised for
-constexpr int kKillCode = 5;          // read-code slot whose score is kKillScore (pads short windows)
-constexpr int kKillScore = -128;
 
 struct Params {
   int32_t match, mismatch, open1, ext1, open2, ext2;
@@ -84,7 +82,6 @@ struct SgTask {
   int32_t dir, want_codes;
   int64_t tb_off;                      // byte offset of the direction-code store (want_codes)
   int64_t tb_bytes;
-  int64_t bnd_off;                     // scratch for the band boundary rows (int32 x 3 x (n2+1))
   // outputs
   int32_t score, end1, end2, rows;     // end1/end2 1-based (-1 when none) ; rows evaluated
   int32_t status, ncig;
@@ -104,8 +101,10 @@ void launch_reverse(ScanTask *tasks, int first, int n, const unsigned long long 
 void launch_xdrop(XTask *tasks, const int *idx, int n, Arena ar, Params p, uint32_t *tb, int wcap, int32_t *scratch,
                   int64_t scratch_per_thread, cudaStream_t st);
 void launch_xdrop_traceback(XTask *tasks, const int *idx, int n, const uint32_t *tb, uint32_t *cig, cudaStream_t st);
-void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p, uint8_t *tb, int32_t *bnd,
-                       int64_t bnd_stride, int *work_counter, int grid_warps, cudaStream_t st);
+void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p, uint8_t *tb, void *bnd,
+                       int max_n2, int *work_counter, int grid, cudaStream_t st);
+int sg_ctas_per_sm();
+int64_t sg_bnd_bytes(int grid, int max_n2);
 void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, uint32_t *cig,
                          cudaStream_t st);
 int64_t sg_tb_bytes(int n1, int n2, int w);

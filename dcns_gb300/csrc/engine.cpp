@@ -89,6 +89,8 @@ Context::~Context() {
   h_codes.release();
   h_misc.release();
   h_out.release();
+  h_tasks.release();
+  h_tiles.release();
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
   if (st) cudaStreamDestroy(st);
@@ -241,14 +243,23 @@ void upload(Context &C, const std::vector<PairIn> &pairs) {
 }
 
 // ------------------------------------------------------------------ 2./3. seed scan with recursion replay
+// Smith-Waterman tasks of one batch: level-0 windows live in pinned host memory (ids [0, n0), pair p owning the
+// contiguous range [wstart[p], wstart[p] + nwin[p])); recursion tasks follow in `more` (ids n0 + k).
 struct ScanState {
-  std::vector<ScanTask> tasks;
-  std::vector<int32_t> left, right;      // child task id, -1 none/not created
-  std::vector<std::vector<int32_t>> win;  // per pair: level-0 task ids in window order
-  std::vector<int32_t> pair_len1, pair_len2;
-  int64_t first_new = 0;                 // tasks [first_new, size) still to be computed
-  int64_t speculative = 0;
+  ScanTask *base = nullptr;
+  int64_t n0 = 0;
+  std::vector<ScanTask> more;
+  std::vector<int32_t> left, right;  // child task id, -1 none/not created
+  std::vector<int64_t> wstart;
+  std::vector<int32_t> nwin;
+  int64_t first_new = 0;  // tasks [first_new, size) still to be computed
+  ScanTask &task(int64_t i) { return i < n0 ? base[i] : more[i - n0]; }
+  const ScanTask &task(int64_t i) const { return i < n0 ? base[i] : more[i - n0]; }
+  int64_t size() const { return n0 + (int64_t)more.size(); }
 };
+
+// The fast kernel's table stores s - open in int8 and pads short windows with -16384 in int16 lanes.
+bool fast_scan_ok(const Params &P) { return P.window <= kScanW && P.match - P.open1 <= 127; }
 
 int warmup_rows(const Params &P, int tw) {
   // A positive-scoring local path over tw read columns spans at most tw diagonal rows plus fewer than
@@ -258,27 +269,202 @@ int warmup_rows(const Params &P, int tw) {
   return tw + (P.match * tw + g - 1) / g + 4;
 }
 
-// Computes tasks [S.first_new, size): fast int16x2 tiles where the reference's striped semantics and the int16 bound
-// hold, the generic int32 kernel otherwise; then the reverse scans.  Downloads the finished tasks.
-void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
-  const int64_t first = S.first_new, n = (int64_t)S.tasks.size() - first;
-  if (n <= 0) return;
-  S.first_new = (int64_t)S.tasks.size();
-  auto t0 = Clock::now();
+// Launches the scan over `tiles` plus the generic kernel over `generic`, then the reverse scans for tasks
+// [first, first+n); downloads those tasks.  The tasks must already be on the device.
+void run_scan_round(Context &C, ScanState &S, const Params &P, int64_t first, int64_t n, const ScanTile *tiles,
+                    int64_t ntiles, const std::vector<int32_t> &generic, ScanTask *host_dst) {
+  auto tx = Clock::now();
+  C.d_keys.ensure(C, sizeof(unsigned long long) * S.size());
+  DCNS_CK(cudaMemsetAsync(C.d_keys.as<unsigned long long>() + first, 0, sizeof(unsigned long long) * n, C.st));
+  if (ntiles > 0) {
+    C.d_tiles.ensure(C, sizeof(ScanTile) * ntiles);
+    C.d_counter.ensure(C, 64);
+    h2d(C, C.d_tiles, tiles, (size_t)ntiles);
+    DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int), C.st));
+    const int grid = (int)std::min<int64_t>((int64_t)C.nsm * C.scan_blocks_per_sm, (ntiles + 127) / 128);
+    DCNS_CK(cudaEventRecord(C.ev0, C.st));
+    launch_scan(C.d_tiles.as<ScanTile>(), (int)ntiles, C.arena, P, C.d_keys.as<unsigned long long>(),
+                C.d_counter.as<int>(), grid, C.st);
+    DCNS_CK(cudaEventRecord(C.ev1, C.st));
+    C.stats.scan_launches += 1;
+    C.stats.kernel_launches += 1;
+  }
+  if (!generic.empty()) {
+    int maxtw = 0;
+    for (int32_t k : generic) maxtw = std::max(maxtw, S.task(k).tw);
+    const int64_t per = 3 * ((int64_t)maxtw + 2);
+    C.d_idx.ensure(C, sizeof(int32_t) * generic.size());
+    C.d_scratch.ensure(C, sizeof(int32_t) * per * generic.size());
+    h2d(C, C.d_idx, generic.data(), generic.size());
+    launch_scan_generic(C.d_tasks.as<ScanTask>(), C.d_idx.as<int>(), (int)generic.size(), C.seqbase_dev, C.arena,
+                        P, C.d_keys.as<unsigned long long>(), C.d_scratch.as<int32_t>(), per, C.st);
+    C.stats.kernel_launches += 1;
+  }
+  launch_reverse(C.d_tasks.as<ScanTask>(), (int)first, (int)n, C.d_keys.as<unsigned long long>(), C.seqbase_dev,
+                 nullptr, C.arena, P, C.st);
+  C.stats.kernel_launches += 1;
+  d2h(C, host_dst, C.d_tasks, (size_t)n, (size_t)first);
+  sync(C);
+  C.stats.ms_scan_xfer += ms_since(tx);
+  if (ntiles > 0) {
+    float ms = 0;
+    DCNS_CK(cudaEventElapsedTime(&ms, C.ev0, C.ev1));
+    C.stats.ms_scan_kernel += ms;
+  }
+}
 
+// Level 0: every window of every pair against its whole reference.  Tasks and tiles are written in parallel straight
+// into pinned buffers; pairs are laid out by decreasing reference length so the persistent scan kernel's work queue
+// hands out the longest tiles first.
+void scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, const Params &P, bool one_gap) {
+  auto t0 = Clock::now();
+  const int64_t np = (int64_t)pairs.size();
+  S.wstart.assign(np, 0);
+  S.nwin.assign(np, 0);
+  auto count_windows = [&](int32_t n2) {
+    // window starts 0, step, ... as in :462-480 (1-gap stops once past the query end) / :376-390 (2-gap)
+    int32_t k = 0, s = 0;
+    while (true) {
+      ++k;
+      s += P.step;
+      if (one_gap && s > n2) break;
+      if (s + P.window > n2) {
+        ++k;
+        break;
+      }
+    }
+    return k;
+  };
+  int64_t n0 = 0;
+  for (int64_t p = 0; p < np; ++p) {
+    S.wstart[p] = n0;
+    S.nwin[p] = count_windows(pairs[p].n2);
+    n0 += S.nwin[p];
+  }
+  S.n0 = n0;
+  S.first_new = n0;
+  C.h_tasks.ensure(sizeof(ScanTask) * std::max<int64_t>(n0, 1));
+  S.base = C.h_tasks.as<ScanTask>();
+  const bool fast = fast_scan_ok(P);
+  // windows with tw > 0 pair up two per tile; tw <= 0 windows (a short tail can be empty) are never scanned
+  std::vector<int32_t> nfast(np, 0);
+  int64_t total_rows = 0, nduo = 0;
+  for (int64_t p = 0; p < np; ++p) {
+    int32_t cnt = 0;
+    for (int32_t k = 0; k < S.nwin[p]; ++k) {
+      const int32_t s2 = k * P.step;
+      const int32_t tw = (s2 + P.window) > pairs[p].n2 ? (pairs[p].n2 - s2) : P.window;
+      if (tw > 0 && pairs[p].n1 > 0) ++cnt;
+    }
+    nfast[p] = fast ? cnt : 0;
+    nduo += (nfast[p] + 1) / 2;
+    total_rows += (int64_t)((nfast[p] + 1) / 2) * pairs[p].n1;
+  }
+  const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * 128;
+  const int K = warmup_rows(P, kScanW);
+  int64_t chunk = INT64_MAX;
+  if (nduo < 8 * resident && K != INT_MAX && total_rows > 0)
+    chunk = std::max<int64_t>(4 * (int64_t)K, (total_rows + 8 * resident - 1) / (8 * resident));
+  std::vector<int64_t> order(np), tile_off(np + 1, 0);
+  for (int64_t p = 0; p < np; ++p) order[p] = p;
+  std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+    return pairs[a].n1 != pairs[b].n1 ? pairs[a].n1 > pairs[b].n1 : a < b;
+  });
+  auto nchunks = [&](int32_t n1) -> int64_t { return chunk == INT64_MAX ? 1 : (n1 + chunk - 1) / chunk; };
+  std::vector<int64_t> toff(np, 0);
+  int64_t ntiles = 0;
+  for (int64_t q = 0; q < np; ++q) {
+    const int64_t p = order[q];
+    toff[p] = ntiles;
+    ntiles += (int64_t)((nfast[p] + 1) / 2) * nchunks(pairs[p].n1);
+  }
+  C.h_tiles.ensure(sizeof(ScanTile) * std::max<int64_t>(ntiles, 1));
+  ScanTile *tiles = C.h_tiles.as<ScanTile>();
+  std::vector<std::vector<int32_t>> gen(np);
+  parallel_for(np, [&](int64_t p) {
+    const int32_t n1 = pairs[p].n1, n2 = pairs[p].n2;
+    ScanTask *T = S.base + S.wstart[p];
+    int32_t pending = -1;
+    int64_t to = toff[p];
+    auto emit = [&](int32_t a, int32_t b) {
+      ScanTile tl{};
+      tl.ref_base = C.seq_base[2 * p];
+      tl.qry_base = C.seq_base[2 * p + 1];
+      for (int h = 0; h < 2; ++h) {
+        const int32_t id = h == 0 ? a : b;
+        if (id >= 0) {
+          const ScanTask &x = S.base[id];
+          tl.s2[h] = x.s2, tl.tw[h] = x.tw, tl.lo[h] = 0, tl.hi[h] = n1, tl.task[h] = id;
+        } else {
+          tl.s2[h] = 0, tl.tw[h] = 0, tl.lo[h] = 0, tl.hi[h] = n1, tl.task[h] = -1;
+        }
+      }
+      for (int64_t c0 = 0; c0 < n1; c0 += chunk) {
+        ScanTile t = tl;
+        t.cnt_begin = (int32_t)c0;
+        t.row_end = (int32_t)std::min<int64_t>(n1, c0 + chunk);
+        t.row_begin = (int32_t)std::max<int64_t>(0, c0 - (c0 == 0 ? 0 : K));
+        tiles[to++] = t;
+        if (chunk == INT64_MAX) break;
+      }
+    };
+    for (int32_t k = 0; k < S.nwin[p]; ++k) {
+      ScanTask x{};
+      x.pair = (int32_t)p;
+      x.s2 = k * P.step;
+      x.tw = (x.s2 + P.window) > n2 ? (n2 - x.s2) : P.window;
+      x.lo = 0;
+      x.hi = n1;
+      x.striped = striped_for_host(n1, x.tw, P.open1, P.ext1, P.match) ? 1 : 0;
+      T[k] = x;
+      const int32_t id = (int32_t)(S.wstart[p] + k);
+      if (x.tw <= 0 || n1 <= 0) continue;
+      if (!fast) {
+        gen[p].push_back(id);
+        continue;
+      }
+      if (pending < 0) {
+        pending = id;
+      } else {
+        emit(pending, id);
+        pending = -1;
+      }
+    }
+    if (pending >= 0) emit(pending, -1);
+  });
+  std::vector<int32_t> generic;
+  for (auto &g : gen) generic.insert(generic.end(), g.begin(), g.end());
+  S.left.assign(n0, -1);
+  S.right.assign(n0, -1);
+  C.stats.ms_scan_prep += ms_since(t0);
+  C.d_tasks.ensure(C, sizeof(ScanTask) * std::max<int64_t>(n0, 1));
+  auto tx = Clock::now();
+  h2d(C, C.d_tasks, S.base, (size_t)n0);
+  C.stats.ms_scan_xfer += ms_since(tx);
+  run_scan_round(C, S, P, 0, n0, tiles, ntiles, generic, S.base);
+  C.stats.ms_scan += ms_since(t0);
+}
+
+// Recursion rounds: tasks [S.first_new, size) (all in `more`).  Fast tasks of one pair with similar row ranges are
+// paired into int16x2 tiles; the rest go to the generic kernel.
+void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
+  const int64_t first = S.first_new, n = S.size() - first;
+  if (n <= 0) return;
+  S.first_new = S.size();
+  auto t0 = Clock::now();
+  const bool fast_ok = fast_scan_ok(P);
   std::vector<int32_t> fast, generic;
   for (int64_t k = first; k < first + n; ++k) {
-    ScanTask &T = S.tasks[k];
+    ScanTask &T = S.task(k);
     T.striped = striped_for_host(T.hi - T.lo, T.tw, P.open1, P.ext1, P.match) ? 1 : 0;
     if (T.tw <= 0 || T.hi <= T.lo) continue;  // nothing to scan: key stays 0
-    if (T.striped && T.tw <= kScanW)
+    if (fast_ok && T.striped && T.tw <= kScanW)
       fast.push_back((int32_t)k);
     else
       generic.push_back((int32_t)k);
   }
-  // Pair consecutive fast tasks of one pair (same rows for level 0; similar ranges for recursion children).
   std::sort(fast.begin(), fast.end(), [&](int32_t a, int32_t b) {
-    const ScanTask &x = S.tasks[a], &y = S.tasks[b];
+    const ScanTask &x = S.task(a), &y = S.task(b);
     if (x.pair != y.pair) return x.pair < y.pair;
     if (x.lo != y.lo) return x.lo < y.lo;
     if (x.hi != y.hi) return x.hi < y.hi;
@@ -288,23 +474,21 @@ void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
     int32_t a, b;
   };
   std::vector<Half2> duo;
-  for (size_t i = 0; i < fast.size(); i += 2) {
+  for (size_t i = 0; i < fast.size();) {
     const int32_t a = fast[i];
-    int32_t b = -1;
-    if (i + 1 < fast.size() && S.tasks[fast[i + 1]].pair == S.tasks[a].pair) b = fast[i + 1];
-    if (b < 0 && i + 1 < fast.size()) {
+    if (i + 1 < fast.size() && S.task(fast[i + 1]).pair == S.task(a).pair) {
+      duo.push_back({a, fast[i + 1]});
+      i += 2;
+    } else {
       duo.push_back({a, -1});
-      i -= 1;  // fast[i+1] starts the next duo
-      continue;
+      i += 1;
     }
-    duo.push_back({a, b});
   }
-  // Row chunking: enough tiles for ~8 resident waves of threads, each tile at least 4 warm-up lengths long.
   int64_t total_rows = 0;
   for (const Half2 &d : duo) {
-    const ScanTask &A = S.tasks[d.a];
+    const ScanTask &A = S.task(d.a);
     int lo = A.lo, hi = A.hi;
-    if (d.b >= 0) lo = std::min(lo, S.tasks[d.b].lo), hi = std::max(hi, S.tasks[d.b].hi);
+    if (d.b >= 0) lo = std::min(lo, S.task(d.b).lo), hi = std::max(hi, S.task(d.b).hi);
     total_rows += hi - lo;
   }
   const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * 128;
@@ -317,13 +501,13 @@ void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
   tiles.reserve(duo.size() + 16);
   for (const Half2 &d : duo) {
     ScanTile tl{};
-    const ScanTask &A = S.tasks[d.a];
+    const ScanTask &A = S.task(d.a);
     tl.ref_base = C.seq_base[2 * A.pair];
     tl.qry_base = C.seq_base[2 * A.pair + 1];
     int lo = A.lo, hi = A.hi;
     tl.s2[0] = A.s2, tl.tw[0] = A.tw, tl.lo[0] = A.lo, tl.hi[0] = A.hi, tl.task[0] = d.a;
     if (d.b >= 0) {
-      const ScanTask &B = S.tasks[d.b];
+      const ScanTask &B = S.task(d.b);
       tl.s2[1] = B.s2, tl.tw[1] = B.tw, tl.lo[1] = B.lo, tl.hi[1] = B.hi, tl.task[1] = d.b;
       lo = std::min(lo, B.lo);
       hi = std::max(hi, B.hi);
@@ -343,49 +527,14 @@ void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
   std::sort(tiles.begin(), tiles.end(), [](const ScanTile &a, const ScanTile &b) {
     return (a.row_end - a.row_begin) > (b.row_end - b.row_begin);
   });
-
-  // device: tasks segment, keys, tiles
-  C.d_tasks.ensure(C, sizeof(ScanTask) * S.tasks.size());
-  C.d_keys.ensure(C, sizeof(unsigned long long) * S.tasks.size());
-  h2d(C, C.d_tasks, S.tasks.data() + first, (size_t)n, (size_t)first);
-  DCNS_CK(cudaMemsetAsync(C.d_keys.as<unsigned long long>() + first, 0, sizeof(unsigned long long) * n, C.st));
-  if (!tiles.empty()) {
-    C.d_tiles.ensure(C, sizeof(ScanTile) * tiles.size());
-    C.d_counter.ensure(C, 64);
-    h2d(C, C.d_tiles, tiles.data(), tiles.size());
-    DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int), C.st));
-    const int grid = (int)std::min<int64_t>((int64_t)C.nsm * C.scan_blocks_per_sm, ((int64_t)tiles.size() + 127) / 128);
-    DCNS_CK(cudaEventRecord(C.ev0, C.st));
-    launch_scan(C.d_tiles.as<ScanTile>(), (int)tiles.size(), C.arena, P, C.d_keys.as<unsigned long long>(),
-                C.d_counter.as<int>(), grid, C.st);
-    DCNS_CK(cudaEventRecord(C.ev1, C.st));
-    C.stats.scan_launches += 1;
-    C.stats.kernel_launches += 1;
-  }
-  if (!generic.empty()) {
-    int maxtw = 0;
-    for (int32_t k : generic) maxtw = std::max(maxtw, S.tasks[k].tw);
-    const int64_t per = 3 * ((int64_t)maxtw + 2);
-    C.d_idx.ensure(C, sizeof(int32_t) * generic.size());
-    C.d_scratch.ensure(C, sizeof(int32_t) * per * generic.size());
-    h2d(C, C.d_idx, generic.data(), generic.size());
-    launch_scan_generic(C.d_tasks.as<ScanTask>(), C.d_idx.as<int>(), (int)generic.size(), C.seqbase_dev,
-                        C.arena, P, C.d_keys.as<unsigned long long>(), C.d_scratch.as<int32_t>(), per, C.st);
-    C.stats.kernel_launches += 1;
-  }
-  launch_reverse(C.d_tasks.as<ScanTask>(), (int)first, (int)n, C.d_keys.as<unsigned long long>(),
-                 C.seqbase_dev, nullptr, C.arena, P, C.st);
-  C.stats.kernel_launches += 1;
-  d2h(C, S.tasks.data() + first, C.d_tasks, (size_t)n, (size_t)first);
-  sync(C);
-  if (!tiles.empty()) {
-    float ms = 0;
-    DCNS_CK(cudaEventElapsedTime(&ms, C.ev0, C.ev1));
-    C.stats.ms_scan_kernel += ms;
-  }
+  C.stats.ms_scan_prep += ms_since(t0);
+  C.d_tasks.ensure(C, sizeof(ScanTask) * S.size());
+  // tasks [first, first+n) are all recursion tasks: contiguous in `more`
+  h2d(C, C.d_tasks, S.more.data() + (first - S.n0), (size_t)n, (size_t)first);
+  run_scan_round(C, S, P, first, n, tiles.data(), (int64_t)tiles.size(), generic, S.more.data() + (first - S.n0));
   C.stats.ms_scan += ms_since(t0);
-  S.left.resize(S.tasks.size(), -1);
-  S.right.resize(S.tasks.size(), -1);
+  S.left.resize(S.size(), -1);
+  S.right.resize(S.size(), -1);
 }
 
 inline Seed4 seed_of(const ScanTask &T) { return Seed4{T.start1, T.end1, T.start2, T.end2}; }
@@ -401,7 +550,7 @@ struct ReplayCtx {
 // getSeeds' recursive variant (:61-128): the local set gets the seed, then the left subtree's seeds in their set
 // order, then the right subtree's.  Returns false when some child is not computed yet (requests it and continues).
 bool subtree(ReplayCtx &R, int32_t t, SeedSet &out) {
-  const ScanTask &T = R.S.tasks[t];
+  const ScanTask &T = R.S.task(t);
   R.visited++;
   R.cells += (int64_t)(T.hi - T.lo) * std::max(T.tw, 0);
   if (T.score < R.P.min_score) return true;
@@ -437,8 +586,8 @@ bool subtree(ReplayCtx &R, int32_t t, SeedSet &out) {
 // The set-gated window loop (:131-201 per window, :462-480 over windows).
 bool replay_pair(ReplayCtx &R, int64_t p, SeedSet &global) {
   bool ok = true;
-  for (int32_t t : R.S.win[p]) {
-    const ScanTask &T = R.S.tasks[t];
+  for (int64_t t = R.S.wstart[p]; t < R.S.wstart[p] + R.S.nwin[p]; ++t) {
+    const ScanTask &T = R.S.task(t);
     R.visited++;
     R.cells += (int64_t)(T.hi - T.lo) * std::max(T.tw, 0);
     if (T.score < R.P.min_score) continue;
@@ -526,28 +675,13 @@ void scan_and_link(Context &C, const std::vector<PairIn> &pairs, const Params &P
                    std::vector<std::vector<Seed4>> &linked) {
   const int64_t np = (int64_t)pairs.size();
   ScanState S;
-  S.win.resize(np);
-  std::vector<int32_t> starts;
-  for (int64_t p = 0; p < np; ++p) {
-    window_starts(pairs[p].n2, P, one_gap, starts);
-    for (int32_t s : starts) {
-      ScanTask T{};
-      T.pair = (int32_t)p;
-      T.s2 = s;
-      T.tw = (s + P.window) > pairs[p].n2 ? (pairs[p].n2 - s) : P.window;
-      T.lo = 0;
-      T.hi = pairs[p].n1;
-      T.score = 0;
-      S.win[p].push_back((int32_t)S.tasks.size());
-      S.tasks.push_back(T);
-    }
-  }
+  scan_level0(C, S, pairs, P, one_gap);
   const int mini = P.min_score / P.match;
   std::vector<SeedSet> sets(np);
   std::vector<uint8_t> done(np, 0);
   int64_t cells = 0, cells_rev = 0, visited_final = 0;
   for (int round = 0;; ++round) {
-    compute_scan_tasks(C, S, P);
+    if (round > 0) compute_scan_tasks(C, S, P);
     auto t0 = Clock::now();
     std::vector<ReplayCtx> rc;
     std::vector<std::vector<std::pair<int32_t, int32_t>>> reqs(np);
@@ -579,7 +713,7 @@ void scan_and_link(Context &C, const std::vector<PairIn> &pairs, const Params &P
         const int32_t t = rq.first;
         int32_t &slot = rq.second == 0 ? S.left[t] : S.right[t];
         if (slot >= 0) continue;
-        const ScanTask &P0 = S.tasks[t];
+        const ScanTask P0 = S.task(t);
         ScanTask ch{};
         ch.pair = P0.pair;
         ch.s2 = P0.s2;
@@ -591,13 +725,13 @@ void scan_and_link(Context &C, const std::vector<PairIn> &pairs, const Params &P
           ch.lo = P0.end1 + 1;
           ch.hi = P0.hi;
         }
-        slot = (int32_t)S.tasks.size();
-        S.tasks.push_back(ch);
+        slot = (int32_t)S.size();
+        S.more.push_back(ch);
         ++nreq;
       }
     }
-    S.left.resize(S.tasks.size(), -1);
-    S.right.resize(S.tasks.size(), -1);
+    S.left.resize(S.size(), -1);
+    S.right.resize(S.size(), -1);
     C.stats.ms_replay += ms_since(t0);
     if (nreq == 0) break;
     if (round > 100000) throw Error(DCNS_ERR_DEVICE, "seed recursion did not converge");
@@ -605,21 +739,35 @@ void scan_and_link(Context &C, const std::vector<PairIn> &pairs, const Params &P
   C.stats.cells_scan += cells;
   C.stats.cells_scan_reverse += cells_rev;
   C.stats.tasks_scan += visited_final;
-  C.stats.tasks_scan_speculative += (int64_t)S.tasks.size() - visited_final;
+  C.stats.tasks_scan_speculative += S.size() - visited_final;
   auto t0 = Clock::now();
   linked.assign(np, {});
   parallel_for(np, [&](int64_t p) {
     link_seeds(sets[p]);
     linked[p].assign(sets[p].begin(), sets[p].end());
   });
-  C.stats.ms_replay += ms_since(t0);
+  C.stats.ms_link += ms_since(t0);
 }
 
 // ------------------------------------------------------------------ 5. x-drop passes
+// Sum over rows i = 1..rows of the band width max(0, min(i+w, n2) - max(i-w, 1) + 1), in closed form: the width is
+// linear between the breakpoints where either clamp switches or the band empties.
 int64_t band_cells(int rows, int w, int n2) {
-  int64_t c = 0;
-  for (int i = 1; i <= rows; ++i) c += std::max(0, std::min(i + w, n2) - std::max(i - w, 1) + 1);
-  return c;
+  if (rows <= 0 || n2 <= 0) return 0;
+  const int64_t W = w, N = n2, R = rows;
+  auto width = [&](int64_t i) {
+    return std::max<int64_t>(0, std::min(i + W, N) - std::max<int64_t>(i - W, 1) + 1);
+  };
+  int64_t bp[] = {1, W + 1, W + 2, N - W, N - W + 1, N + W, N + W + 1, R + 1};
+  std::sort(std::begin(bp), std::end(bp));
+  int64_t total = 0;
+  for (int k = 0; k + 1 < 8; ++k) {
+    const int64_t lo = std::max<int64_t>(bp[k], 1), hi = std::min<int64_t>(bp[k + 1], R + 1);  // [lo, hi)
+    if (lo >= hi) continue;
+    const int64_t cnt = hi - lo;
+    total += cnt * (width(lo) + width(hi - 1)) / 2;
+  }
+  return total;
 }
 
 int wpr_of(int w) { return (2 * w + 1 + 7) / 8; }
@@ -644,7 +792,8 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
   for (int64_t k = 0; k < n; ++k) pend[k] = (int32_t)k;
   C.d_x.ensure(C, sizeof(XTask) * n);
   while (!pend.empty()) {
-    // traceback slots for this round, laid out from offset 0
+    // Only the pending passes travel: gathered into a compact pinned array, indexed 0..m-1 on the device.
+    const int64_t m = (int64_t)pend.size();
     int64_t words = 0;
     if (want_codes)
       for (int32_t k : pend) {
@@ -653,18 +802,22 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
         words += X[k].tb_cap;
       }
     if (want_codes) C.d_tb.ensure(C, sizeof(uint32_t) * std::max<int64_t>(words, 1));
-    h2d(C, C.d_x, X.data(), (size_t)n);
+    C.h_misc.ensure(sizeof(XTask) * m);
+    XTask *Xc = C.h_misc.as<XTask>();
+    for (int64_t q = 0; q < m; ++q) Xc[q] = X[pend[q]];
+    h2d(C, C.d_x, Xc, (size_t)m);
     std::vector<int32_t> g10, g20, gw;
     int maxw = 0;
-    for (int32_t k : pend) {
-      if (X[k].w <= 10)
-        g10.push_back(k);
-      else if (X[k].w <= 20)
-        g20.push_back(k);
+    for (int64_t q = 0; q < m; ++q) {
+      const int w = Xc[q].w;
+      if (w <= 10)
+        g10.push_back((int32_t)q);
+      else if (w <= 20)
+        g20.push_back((int32_t)q);
       else
-        gw.push_back(k), maxw = std::max(maxw, X[k].w);
+        gw.push_back((int32_t)q), maxw = std::max(maxw, w);
     }
-    C.d_idx.ensure(C, sizeof(int32_t) * pend.size());
+    C.d_idx.ensure(C, sizeof(int32_t) * m);
     size_t off = 0;
     auto launch_group = [&](std::vector<int32_t> &g, int wcap) {
       if (g.empty()) return;
@@ -685,39 +838,43 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
     launch_group(g10, 10);
     launch_group(g20, 20);
     launch_group(gw, 0);
-    d2h(C, X.data(), C.d_x, (size_t)n);
+    d2h(C, Xc, C.d_x, (size_t)m);
     sync(C);
-    std::vector<int32_t> next, finished;
-    for (int32_t k : pend) {
-      if (X[k].status == 1) {
+    std::vector<int32_t> next, fin_c;  // fin_c: compact indices of finished passes
+    for (int64_t q = 0; q < m; ++q) {
+      const int32_t k = pend[q];
+      X[k] = Xc[q];
+      if (Xc[q].status == 1) {
         X[k].w *= 2;  // the reference restarts the whole pass with twice the band (:1272-1276)
         next.push_back(k);
-      } else if (X[k].status == 2) {
+      } else if (Xc[q].status == 2) {
         rows_cap[k] = X[k].n1;
         next.push_back(k);
       } else {
-        finished.push_back(k);
+        fin_c.push_back((int32_t)q);
       }
     }
-    if (want_codes && !finished.empty()) {
+    if (want_codes && !fin_c.empty()) {
       int64_t cw = 0;
-      for (int32_t k : finished) {
-        X[k].cig_off = cw;
-        X[k].cig_cap = X[k].end1 + X[k].end2 + 2;
-        cw += X[k].cig_cap;
+      for (int32_t q : fin_c) {
+        Xc[q].cig_off = cw;
+        Xc[q].cig_cap = Xc[q].end1 + Xc[q].end2 + 2;
+        cw += Xc[q].cig_cap;
       }
       C.d_cig.ensure(C, sizeof(uint32_t) * std::max<int64_t>(cw, 1));
-      h2d(C, C.d_x, X.data(), (size_t)n);
-      h2d(C, C.d_idx, finished.data(), finished.size());
-      launch_xdrop_traceback(C.d_x.as<XTask>(), C.d_idx.as<int>(), (int)finished.size(), C.d_tb.as<uint32_t>(),
+      h2d(C, C.d_x, Xc, (size_t)m);
+      h2d(C, C.d_idx, fin_c.data(), fin_c.size());
+      launch_xdrop_traceback(C.d_x.as<XTask>(), C.d_idx.as<int>(), (int)fin_c.size(), C.d_tb.as<uint32_t>(),
                              C.d_cig.as<uint32_t>(), C.st);
       C.stats.kernel_launches += 1;
       C.h_out.ensure(sizeof(uint32_t) * std::max<int64_t>(cw, 1));
-      d2h(C, X.data(), C.d_x, (size_t)n);
+      d2h(C, Xc, C.d_x, (size_t)m);
       d2h(C, C.h_out.as<uint32_t>(), C.d_cig, (size_t)cw);
       sync(C);
       const uint32_t *hc = C.h_out.as<uint32_t>();
-      for (int32_t k : finished) {
+      for (int32_t q : fin_c) {
+        const int32_t k = pend[q];
+        X[k] = Xc[q];
         if (X[k].status == 3) throw Error(DCNS_ERR_DEVICE, "x-drop traceback exceeded its CIGAR slot");
         (*cigars)[k].assign(hc + X[k].cig_off, hc + X[k].cig_off + X[k].ncig);
       }
@@ -811,11 +968,7 @@ void extend_seeds(Context &C, const std::vector<PairIn> &pairs, const Params &P,
 }
 
 // ------------------------------------------------------------------ 2-gap stage (:532-616)
-int64_t sg_band_cells(int rows, int w, int n2) {
-  int64_t c = 0;
-  for (int i = 1; i <= rows; ++i) c += std::max(0, std::min(i + w, n2) - std::max(i - w, 1) + 1);
-  return c;
-}
+int64_t sg_band_cells(int rows, int w, int n2) { return band_cells(rows, w, n2); }
 
 
 // Runs 2-piece semi-global DPs; with codes, bounded by the memory budget per launch (admission by traceback bytes).
@@ -825,8 +978,6 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
   auto t0 = Clock::now();
   const int64_t n = (int64_t)G.size();
   if (cigars) cigars->assign(n, {});
-  int maxn2 = 1;
-  for (auto &g : G) maxn2 = std::max(maxn2, g.n2);
   // device work split into batches whose direction-code stores fit a fraction of the budget
   const size_t free_budget = C.budget > C.used ? C.budget - C.used : 0;
   const int64_t cap_bytes = std::max<int64_t>((int64_t)(free_budget / 2), (int64_t)64 << 20);
@@ -845,19 +996,25 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
     }
     const int64_t m = k1 - k0;
     if (want_codes) C.d_sgtb.ensure(C, (size_t)std::max<int64_t>(bytes, 1));
-    // whole blocks of 4 warps; every warp of the grid owns a boundary-row slot
-    const int grid_warps = (int)((std::min<int64_t>(m, (int64_t)C.nsm * 16) + 3) / 4 * 4);
-    const int64_t bnd_stride = (int64_t)maxn2 + 2;
-    C.d_bnd.ensure(C, sizeof(int32_t) * 3 * bnd_stride * grid_warps);
+    const int grid = (int)std::min<int64_t>(m, (int64_t)C.nsm * sg_ctas_per_sm());
+    int maxn2 = 1;
+    for (int64_t q = k0; q < k1; ++q) maxn2 = std::max(maxn2, G[q].n2);
+    C.d_bnd.ensure(C, (size_t)sg_bnd_bytes(grid, maxn2));
     C.d_counter.ensure(C, 64);
     DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int), C.st));
+    // largest DPs first: the CTA work queue then finishes with the small ones
     std::vector<int32_t> idx(m);
     for (int64_t q = 0; q < m; ++q) idx[q] = (int32_t)(k0 + q);
+    std::sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) {
+      const int64_t ca = (int64_t)G[a].n1 * std::min(G[a].n2, 2 * P.bandwidth + 1);
+      const int64_t cb = (int64_t)G[b].n1 * std::min(G[b].n2, 2 * P.bandwidth + 1);
+      return ca != cb ? ca > cb : a < b;
+    });
     C.d_idx.ensure(C, sizeof(int32_t) * m);
     h2d(C, C.d_idx, idx.data(), (size_t)m);
     h2d(C, C.d_sg, G.data(), (size_t)n);
     launch_semiglobal(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, C.d_sgtb.as<uint8_t>(),
-                      C.d_bnd.as<int32_t>(), bnd_stride, C.d_counter.as<int>(), grid_warps, C.st);
+                      C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, C.st);
     C.stats.kernel_launches += 1;
     C.stats.semiglobal_dps += m;
     if (want_codes) {
@@ -1096,13 +1253,13 @@ void smith_waterman_batch(Context &C, const std::vector<PairIn> &tasks, const Pa
     T.tw = tasks[k].n2;
     T.lo = 0;
     T.hi = tasks[k].n1;
-    S.tasks.push_back(T);
+    S.more.push_back(T);
   }
   Params Q = P;
   Q.min_score = INT_MAX;  // maxima and positions only: no reverse scans
   compute_scan_tasks(C, S, Q);
   for (int64_t k = 0; k < n; ++k) {
-    const ScanTask &T = S.tasks[k];
+    const ScanTask &T = S.task(k);
     out[3 * k] = T.score;
     out[3 * k + 1] = T.score > 0 ? T.end1 : -1;
     out[3 * k + 2] = T.score > 0 ? T.end2 : -1;
@@ -1196,14 +1353,14 @@ void sliding_window(Context &C, const int8_t *const *seqs, const int32_t *lens, 
       T.tw = tw_of[k];
       T.lo = 0;
       T.hi = lens[i];
-      S.tasks.push_back(T);
+      S.more.push_back(T);
     }
   Params Q = P;
   Q.min_score = INT_MAX;
   compute_scan_tasks(C, S, Q);
   for (int32_t i = 1; i < n; ++i)
     for (int32_t k = 0; k < nw; ++k) {
-      const ScanTask &T = S.tasks[(int64_t)(i - 1) * nw + k];
+      const ScanTask &T = S.task((int64_t)(i - 1) * nw + k);
       const int32_t md = std::min(tw_of[k], lens[i]) * P.match;
       score[(int64_t)(i - 1) * nw + k] = double(T.score) / double(md);
       max_out[(int64_t)(i - 1) * nw + k] = T.score;

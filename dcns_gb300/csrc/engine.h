@@ -95,7 +95,7 @@ struct Context {
   DevBuf d_tasks, d_keys, d_tiles, d_counter, d_idx, d_scratch;
   DevBuf d_x, d_tb, d_cig, d_sg, d_sgtb, d_bnd;
   // pinned staging
-  HostBuf h_codes, h_misc, h_out;
+  HostBuf h_codes, h_misc, h_out, h_tasks, h_tiles;
 
   // arena layout of the batch being aligned (the context's own upload buffers, or a resident batch)
   std::vector<int64_t> seq_base;  // 2 per pair

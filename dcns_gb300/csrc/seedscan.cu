@@ -5,7 +5,7 @@
 // Kernels
 //   pack_kernel         int8 dCNS codes -> 2-bit + N-mask arena (64-base aligned sequences)
 //   scan_kernel<W>      the hot loop: one thread owns two window tasks of one pair as the two int16 halves of every
-//                       register, scanning the same absolute reference rows; per cell 7.5 DPX/ALU ops for 2 cells
+//                       register, scanning the same absolute reference rows; 6.5 DPX/ALU instructions per 2 cells
 //   scan_generic_kernel int32 lanes, any window width, both reference semantics (striped / scalar); used where the
 //                       fast kernel's static int16 bound or width does not hold
 //   reverse_kernel      the reverse-complement re-scan that fixes each seed's start (getSeeds :156-166)
@@ -89,39 +89,44 @@ template <int W>
 __global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ tiles, int ntiles, Arena ar, int open,
                                                    int ext, int match, int mismatch,
                                                    unsigned long long *__restrict__ keys, int *__restrict__ counter) {
-  // Score table per reference symbol (index = 2-bit code | N << 2): bytes 0..4 = s(ref, read code 0..4),
-  // byte 5 = the kill score used by padding columns, bytes 6..7 = 0.
+  // Score table per reference symbol (index = 2-bit code | N << 2): bytes 0..4 = s(ref, read code 0..4) - open,
+  // byte 5 = 0xC0 and byte 6 = 0x00, which the padding selector (6, 5) turns into the lane value -16384.
   __shared__ uint32_t tab[16];
   if (threadIdx.x < 8) {
     const int idx = threadIdx.x;
     const int c = (idx & 4) ? 2 : ((idx & 3) + ((idx & 3) >> 1));
     uint32_t lo = 0, hi = 0;
     for (int r = 0; r < 5; ++r) {
-      const uint32_t b = (uint32_t)(uint8_t)(int8_t)score_of(c, r, match, mismatch);
+      const uint32_t b = (uint32_t)(uint8_t)(int8_t)(score_of(c, r, match, mismatch) - open);
       if (r < 4)
         lo |= b << (8 * r);
       else
         hi |= b;
     }
-    hi |= (uint32_t)(uint8_t)(int8_t)kKillScore << 8;
+    hi |= 0xC0u << 8;
     tab[2 * idx] = lo;
     tab[2 * idx + 1] = hi;
   }
   __syncthreads();
   const uint32_t open2 = pack2(open), ext2 = pack2(ext);
+  const uint32_t open_lo = open2 & 0xFFFFu, open_hi = open2 & 0xFFFF0000u;
 
   for (;;) {
     const int t = atomicAdd(counter, 1);
     if (t >= ntiles) break;
     const ScanTile tl = tiles[t];
 
-    uint32_t sel[W], H[W], E[W];
+    // Registers hold G = H + open (not H): then the diagonal term H + s is G + (s - open) from the table, the
+    // horizontal candidate H + open is G itself, and H + open = max(F + open, Hpre + open) is one fused op.
+    uint32_t sel[W], G[W], E[W];
 #pragma unroll
     for (int p = 0; p < W; ++p) {
-      const int ra = p < tl.tw[0] ? base_code(ar, tl.qry_base + tl.s2[0] + p) : kKillCode;
-      const int rb = p < tl.tw[1] ? base_code(ar, tl.qry_base + tl.s2[1] + p) : kKillCode;
-      sel[p] = (uint32_t)(ra | ((ra | 8) << 4) | (rb << 8) | ((rb | 8) << 12));
-      H[p] = 0;
+      const uint32_t ra = p < tl.tw[0] ? (uint32_t)base_code(ar, tl.qry_base + tl.s2[0] + p) : 0u;
+      const uint32_t rb = p < tl.tw[1] ? (uint32_t)base_code(ar, tl.qry_base + tl.s2[1] + p) : 0u;
+      const uint32_t sa = p < tl.tw[0] ? (ra | ((ra | 8u) << 4)) : 0x56u;  // padding column: -16384
+      const uint32_t sb = p < tl.tw[1] ? (rb | ((rb | 8u) << 4)) : 0x56u;
+      sel[p] = sa | (sb << 8);
+      G[p] = open2;
       E[p] = 0;
     }
 
@@ -133,7 +138,8 @@ __global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ 
     int cs1 = max(tl.lo[1], tl.cnt_begin), ce1 = min(tl.hi[1], tl.row_end);
     if (tl.task[0] < 0 || cs0 >= ce0) cs0 = ce0 = INT_MAX;
     if (tl.task[1] < 0 || cs1 >= ce1) cs1 = ce1 = INT_MAX;
-    uint32_t cmpb = 0x7FFF7FFFu;  // per-half threshold: the running best while counting, unreachable otherwise
+    // per-half threshold in G units: best + open while counting, unreachable (0x7FFF) otherwise
+    uint32_t cmpb = 0x7FFF7FFFu;
     int best0 = 0, best1 = 0, brow0 = -1, brow1 = -1, bcol0 = -1, bcol1 = -1;
 
     int r = tl.row_begin;
@@ -147,20 +153,20 @@ __global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ 
         if (zr0 == r) {
 #pragma unroll
           for (int p = 0; p < W; ++p) {
-            H[p] &= 0xFFFF0000u;
+            G[p] = (G[p] & 0xFFFF0000u) | open_lo;
             E[p] &= 0xFFFF0000u;
           }
         }
         if (zr1 == r) {
 #pragma unroll
           for (int p = 0; p < W; ++p) {
-            H[p] &= 0x0000FFFFu;
+            G[p] = (G[p] & 0x0000FFFFu) | open_hi;
             E[p] &= 0x0000FFFFu;
           }
         }
-        if (cs0 == r) cmpb = (cmpb & 0xFFFF0000u) | (uint32_t)(uint16_t)best0;
-        if (ce0 == r) cmpb |= 0x7FFFu;
-        if (cs1 == r) cmpb = (cmpb & 0x0000FFFFu) | ((uint32_t)(uint16_t)best1 << 16);
+        if (cs0 == r) cmpb = (cmpb & 0xFFFF0000u) | (uint32_t)(uint16_t)(best0 + open);
+        if (ce0 == r) cmpb = (cmpb & 0xFFFF0000u) | 0x7FFFu;
+        if (cs1 == r) cmpb = (cmpb & 0x0000FFFFu) | ((uint32_t)(uint16_t)(best1 + open) << 16);
         if (ce1 == r) cmpb = (cmpb & 0x0000FFFFu) | 0x7FFF0000u;
         nev = min_above(r, zr0, zr1, cs0, ce0, cs1, ce1);
       }
@@ -172,23 +178,24 @@ __global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ 
       if ((rk & 15) == 0) wcur = __ldg(ar.pk + (rk >> 4));
       if ((rk & 31) == 0) ncur = __ldg(ar.nm + (rk >> 5));
 
-      uint32_t diag = 0, F = 0, u = open2, rmax = 0, hprev = 0;
+      uint32_t gd = open2, F = 0, gl = open2, rmax = open2, gprev = open2;
 #pragma unroll
       for (int p = 0; p < W; ++p) {
         const uint32_t s = prmt(T0, T1, sel[p]);
-        const uint32_t hp = __viaddmax_s16x2_relu(diag, s, E[p]);
-        diag = H[p];
-        E[p] = __viaddmax_s16x2(E[p], ext2, __vadd2(hp, open2));
-        F = __viaddmax_s16x2(F, ext2, u);
-        const uint32_t h = __vmaxs2(hp, F);
-        H[p] = h;
-        u = __vadd2(h, open2);
+        const uint32_t hp = __viaddmax_s16x2_relu(gd, s, E[p]);  // max(H[i-1][p-1] + s, E, 0)
+        gd = G[p];
+        const uint32_t tv = __vadd2(hp, open2);
+        E[p] = __viaddmax_s16x2(E[p], ext2, tv);  // max(E + ext, Hpre + open)
+        F = __viaddmax_s16x2(F, ext2, gl);        // max(F + ext, H[i][p-1] + open)
+        const uint32_t g = __viaddmax_s16x2(F, open2, tv);  // max(F, Hpre) + open
+        G[p] = g;
+        gl = g;
         if (p & 1)
-          rmax = __vimax3_s16x2(rmax, hprev, h);
+          rmax = __vimax3_s16x2(rmax, gprev, g);
         else if (p == W - 1)
-          rmax = __vmaxs2(rmax, h);
+          rmax = __vmaxs2(rmax, g);
         else
-          hprev = h;
+          gprev = g;
       }
       const uint32_t gt = __vcmpgts2(rmax, cmpb);
       if (gt) {
@@ -197,8 +204,8 @@ __global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ 
           int col = W - 1;
 #pragma unroll
           for (int p = W - 1; p >= 0; --p)
-            if (half_s16(H[p], 0) == v) col = p;
-          best0 = v;
+            if (half_s16(G[p], 0) == v) col = p;
+          best0 = v - open;
           brow0 = r;
           bcol0 = col;
           cmpb = (cmpb & 0xFFFF0000u) | (uint32_t)(uint16_t)v;
@@ -208,8 +215,8 @@ __global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ 
           int col = W - 1;
 #pragma unroll
           for (int p = W - 1; p >= 0; --p)
-            if (half_s16(H[p], 1) == v) col = p;
-          best1 = v;
+            if (half_s16(G[p], 1) == v) col = p;
+          best1 = v - open;
           brow1 = r;
           bcol1 = col;
           cmpb = (cmpb & 0x0000FFFFu) | ((uint32_t)(uint16_t)v << 16);
@@ -376,8 +383,8 @@ int scan_occupancy_impl() {
 
 namespace dcns {
 // ------------------------------------------------------------------ integer-issue roofline probe
-// Runs the scan kernel's per-cell instruction sequence (prmt lookup, fused add-max-relu, E and F updates, H merge,
-// row maximum every second column) on 8 independent chains per thread at full occupancy, so the only limit is
+// Runs the scan kernel's per-cell instruction sequence (prmt lookup, fused add-max-relu, E and F updates, fused
+// H merge, row maximum every second column) on 8 independent chains per thread at full occupancy, so the only limit is
 // instruction issue.  Each chain step is one int16x2 cell pair of the scan; the result is an upper bound for the
 // scan's cells per second with exactly its instruction mix.
 __global__ void __launch_bounds__(256) issue_probe_kernel(uint32_t *out, int iters, uint32_t seed) {
@@ -392,12 +399,13 @@ __global__ void __launch_bounds__(256) issue_probe_kernel(uint32_t *out, int ite
     for (int c = 0; c < NC; ++c) {
       const uint32_t s = prmt(T0, T1, sel + c);
       const uint32_t hp = __viaddmax_s16x2_relu(d[c], s, e[c]);
-      e[c] = __viaddmax_s16x2(e[c], ext2, __vadd2(hp, open2));
+      const uint32_t tv = __vadd2(hp, open2);
+      e[c] = __viaddmax_s16x2(e[c], ext2, tv);
       f[c] = __viaddmax_s16x2(f[c], ext2, u[c]);
-      const uint32_t h = __vmaxs2(hp, f[c]);
-      u[c] = __vadd2(h, open2);
-      if (c & 1) rm[c] = __vimax3_s16x2(rm[c], d[c], h);
-      d[c] = h;
+      const uint32_t g = __viaddmax_s16x2(f[c], open2, tv);
+      if (c & 1) rm[c] = __vimax3_s16x2(rm[c], d[c], g);
+      u[c] = g;
+      d[c] = g;
     }
   }
   uint32_t acc = 0;

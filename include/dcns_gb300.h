@@ -75,6 +75,9 @@ typedef struct {
   int64_t tasks_scan, tasks_scan_speculative, seeds, xdrop_passes, semiglobal_dps;
   double ms_upload, ms_scan, ms_replay, ms_xdrop, ms_semiglobal, ms_download, ms_total;
   double ms_scan_kernel;  /* device time of the seed-scan kernel launches (CUDA events) */
+  double ms_scan_prep;    /* host: task and tile generation */
+  double ms_scan_xfer;    /* task/tile/result transfers and the synchronising wait of the scan rounds */
+  double ms_link;         /* host: link_seeds */
   int32_t scan_launches, kernel_launches;
 } dcns_stats;
 

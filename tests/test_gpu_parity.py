@@ -258,3 +258,20 @@ def test_resident_batch_matches_host_path(eng):
 def test_scan_roofline_probe_positive(eng):
     g = eng.measure_scan_roofline()
     assert 100.0 < g < 1e6
+
+
+def test_semiglobal_multiwarp_vs_oracle(eng, oracle):
+    """Long DPs (many 32-row stripes across the CTA's warps, FIFO wrap-around), narrow bands, empty-band tails
+    (rows past n2 + w) and early z-drop stops, with and without CIGAR."""
+    rng = np.random.default_rng(17)
+    cases = []
+    for n1, n2 in ((3000, 2000), (700, 4000), (5000, 300), (257, 257), (33, 1000), (1, 5)):
+        x, y = W.planted_pair(rng, n1, n2, 3, 40, 200, 0.8, 0.95, 0.01, 0.0)
+        cases.append((W.prepare(x), W.prepare(y)))
+    for bw, zd, o2, e2 in ((20000, 50, -45, 0), (100, 50, -45, 0), (7, 30, -20, -1), (300, 10, -80, -1)):
+        for cig in (False, True):
+            out, cigars = eng.SemiGlobal(cases, cigar=cig, bandwidth=bw, zdrop=zd, open2=o2, ext2=e2)
+            for k, (a, b) in enumerate(cases):
+                exp = oracle.semiglobal(a, b, cigar=cig, bandwidth=bw, zdrop=zd, open2=o2, ext2=e2)
+                assert tuple(int(v) for v in out[k, :3]) == (exp["score"], exp["end1"], exp["end2"]), (k, bw, zd)
+                assert cigars[k] == exp["cigar"], (k, bw, zd, cig)
