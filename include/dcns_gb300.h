@@ -143,6 +143,19 @@ int dcns_semiglobal_batch(dcns_ctx *ctx, const dcns_pair *tasks, int64_t n, cons
 int dcns_sliding_window(dcns_ctx *ctx, const int8_t *const *seqs, const int32_t *lens, int32_t n_seqs,
                         const dcns_params *params, double *score, int32_t *max_out);
 
+/* No counterpart in the reference.  SemiGlobal's score and end position (the 2-piece affine DP of
+ * dcns_semiglobal_batch without CIGAR) for one pair, for callers that must not allocate device memory at call time:
+ * processes whose device memory belongs to another allocator or budget, and latency-bound threads that cannot afford
+ * the device-wide synchronisation of cudaMalloc/cudaFree.  The caller passes device buffers: the two code sequences
+ * (at most 16384 bases each; longer inputs return DCNS_ERR_INVALID) and d_out (4 int32: maxScore, endPosition1,
+ * endPosition2 (0-based), status 0 ok / 1 a code outside 0..4).  Work is queued on `stream` (a cudaStream_t; NULL =
+ * the legacy default stream); read d_out after synchronising it.  All scratch is one fixed device array of about
+ * 1.6 MB per GPU that holds the library, shared by every call: calls that overlap on the GPU race, calls ordered on
+ * one stream do not.  The first call on each device resolves the array's address (cudaGetSymbolAddress, with that
+ * device current); make it before any stream capture. */
+int dcns_semiglobal_noalloc(const int8_t *d_seq1, int32_t len1, const int8_t *d_seq2, int32_t len2,
+                            const dcns_params *params, int32_t *d_out, void *stream);
+
 /* Serving loop: continuous batching.  dcns_submit copies the pair and returns a ticket at once; requests are
  * admitted to the device as memory allows and overlap with work already running.  dcns_poll returns DCNS_OK with
  * the result when done, DCNS_ERR_BUSY while pending.  dcns_serve_wait blocks up to timeout_ms. */
