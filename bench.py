@@ -202,6 +202,7 @@ def main():
             scan_ms += st["ms_scan_kernel"]
             scan_cells += st["cells_scan"]
             nfrag = sum(len(f) for f in res)
+            last_stats = st
     tot_ms = sum(ms)
     if dist:
         tt = torch.tensor([tot_ms], device="cuda")
@@ -288,6 +289,9 @@ def main():
                 "pairs_per_s": round(world * n * args.steps / (e2e_tot * 1e-3), 2),
                 "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h},
         "roofline": roofline, "cpu_baseline": cb, "gpu_launches": launches, "clocks": clk.summary(),
+        "stages_ms": {k: round(last_stats[k], 2) for k in ("ms_scan_kernel", "ms_scan_prep", "ms_scan_xfer",
+                                                            "ms_replay", "ms_link", "ms_xdrop", "ms_semiglobal",
+                                                            "ms_total")},
     }
     line.update(extras)
     print(json.dumps(line), flush=True)

@@ -824,7 +824,7 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
       h2d(C, C.d_idx, g.data(), g.size(), off);
       int32_t *scratch = nullptr;
       int64_t per = 0;
-      if (wcap == 0) {
+      if (wcap == 0) {  // warp per pass: M and F of 2w+2 cells each
         per = 2 * (2 * (int64_t)maxw + 2);
         C.d_scratch.ensure(C, sizeof(int32_t) * per * g.size());
         scratch = C.d_scratch.as<int32_t>();

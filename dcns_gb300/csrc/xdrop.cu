@@ -128,6 +128,155 @@ __global__ void __launch_bounds__(128) xdrop_kernel(XTask *__restrict__ tasks, c
   xdrop_pass<WC>(T, ar, P, tb, Ms, Fs);
 }
 
+// ------------------------------------------------------------------ wide bands: one warp per pass
+// Lanes own consecutive band cells, 4 per lane in segments of 128.  The horizontal gap chain of a row,
+//   e_{j+1} = max(e_j + g, A_j + open),  g = max(ext, open),  A_j = max(s + diag, F_above)
+// (the value form of e += ext; e = max(e, M + open) with M = max(A, e)), is an affine map in max-plus algebra,
+// f(e) = max(e + a, b); a lane's cells compose into one map, an exclusive warp scan of the maps gives every lane its
+// incoming e, and the lane then replays its cells with the reference's exact comparisons.  Cells left of the row's
+// first column reset e to OUT, as the reference starts each row with e = OUT.
+constexpr int kXwSeg = 4;
+constexpr int32_t kNegInf = -(1 << 30);
+
+struct AffMax {
+  int32_t a, b;  // e -> max(e + a, b); a <= kNegInf means "independent of e"
+};
+
+__device__ __forceinline__ int32_t aff_apply(AffMax f, int32_t e) {
+  return f.a <= kNegInf ? f.b : max(e + f.a, f.b);
+}
+// g after f
+__device__ __forceinline__ AffMax aff_then(AffMax f, AffMax g) {
+  AffMax r;
+  r.a = (f.a <= kNegInf || g.a <= kNegInf) ? kNegInf : f.a + g.a;
+  r.b = (g.a <= kNegInf) ? g.b : max(f.b + g.a, g.b);
+  return r;
+}
+
+__global__ void __launch_bounds__(128) xdrop_warp_kernel(XTask *__restrict__ tasks, const int *__restrict__ idx,
+                                                         int n, Arena ar, Params P, uint32_t *__restrict__ tb,
+                                                         int32_t *__restrict__ scratch, int64_t per_warp) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (gw >= n) return;  // whole warp
+  XTask &T = tasks[idx[gw]];
+  const int w = T.w, n1 = T.n1, n2 = T.n2, nk = 2 * w + 1;
+  const int open = P.open1, ext = P.ext1, g = max(P.ext1, P.open1);
+  const SeqView s1{T.base1, T.a1, T.dir}, s2{T.base2, T.a2, T.dir};
+  int32_t *M = scratch + per_warp * gw;
+  int32_t *F = M + (nk + 1);
+  for (int k = lane; k <= nk; k += 32) M[k] = kOut, F[k] = kOut;
+  __syncwarp();
+  const int wpr = xd_words_per_row(w);
+  int score = 0, e1 = 0, e2 = 0, rows = 0, status = 0;
+  for (int i = 1; i <= n1; ++i) {
+    const int c0 = max(i - w, 1), c1 = min(i + w, n2);
+    if (T.want_codes && (int64_t)i * wpr > T.tb_cap) {
+      status = 2;
+      break;
+    }
+    const int ci = s1.at(ar, i - 1);
+    uint32_t *row_codes = tb + T.tb_off + (int64_t)(i - 1) * wpr;
+    int32_t ecarry = kOut;  // e entering the segment's first cell
+    int lbest = 0, lbestj = -1;
+    for (int seg = 0; seg < nk; seg += 32 * kXwSeg) {
+      const int k0 = seg + kXwSeg * lane;
+      int32_t Mk[kXwSeg], Fk[kXwSeg];
+#pragma unroll
+      for (int q = 0; q < kXwSeg; ++q) {
+        const int k = k0 + q;
+        Mk[q] = k < nk ? M[k] : kOut;
+        Fk[q] = k < nk ? F[k + 1] : kOut;
+      }
+      __syncwarp();  // every old value is read before any cell of this segment is rewritten
+      // this lane's cells as one affine map of the incoming e
+      AffMax f{0, kNegInf};
+      int32_t A[kXwSeg], sv[kXwSeg], fin[kXwSeg];
+      bool valid[kXwSeg], before[kXwSeg];
+#pragma unroll
+      for (int q = 0; q < kXwSeg; ++q) {
+        const int k = k0 + q, j = i - w + k;
+        valid[q] = k < nk && j >= c0 && j <= c1;
+        before[q] = k < nk && j < c0;
+        if (valid[q]) {
+          const int32_t dg = (j == 1) ? (i == 1 ? 0 : kOut) : Mk[q];
+          fin[q] = (j == c1) ? kOut : Fk[q];
+          sv[q] = score_of(ci, s2.at(ar, j - 1), P.match, P.mismatch) + dg;
+          A[q] = sv[q] > fin[q] ? sv[q] : fin[q];
+          f = aff_then(f, AffMax{g, A[q] + open});
+        } else if (before[q]) {
+          f = AffMax{kNegInf, kOut};
+        }
+      }
+      // exclusive scan of the lanes' maps
+      AffMax incl = f;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        AffMax o;
+        o.a = __shfl_up_sync(0xFFFFFFFFu, incl.a, d);
+        o.b = __shfl_up_sync(0xFFFFFFFFu, incl.b, d);
+        if (lane >= d) incl = aff_then(o, incl);
+      }
+      AffMax excl;
+      excl.a = __shfl_up_sync(0xFFFFFFFFu, incl.a, 1);
+      excl.b = __shfl_up_sync(0xFFFFFFFFu, incl.b, 1);
+      if (lane == 0) excl = AffMax{0, kNegInf};
+      int32_t e = aff_apply(excl, ecarry);
+      const AffMax all{__shfl_sync(0xFFFFFFFFu, incl.a, 31), __shfl_sync(0xFFFFFFFFu, incl.b, 31)};
+      const int32_t next_carry = aff_apply(all, ecarry);
+      // replay the cells with the reference's comparisons
+      uint32_t nib = 0;
+#pragma unroll
+      for (int q = 0; q < kXwSeg; ++q) {
+        const int k = k0 + q, j = i - w + k;
+        uint32_t cd = 0xFu;
+        if (valid[q]) {
+          uint32_t d = sv[q] > fin[q] ? 0u : 1u;
+          int32_t v = A[q];
+          if (!(v > e)) d = 2u, v = e;
+          if (v > lbest) lbest = v, lbestj = j;
+          const int32_t h = v + open, fx = fin[q] + ext;
+          if (fx >= h) d |= 4u;
+          e += ext;
+          if (e >= h) d |= 8u;
+          e = e >= h ? e : h;
+          M[k] = v;
+          F[k] = fx >= h ? fx : h;
+          cd = d;
+        } else if (before[q]) {
+          e = kOut;
+        }
+        nib |= cd << (4 * q);
+      }
+      ecarry = next_carry;
+      if (T.want_codes) {
+        // 4 nibbles per lane = half a word: even lanes write the word shared with the next lane
+        const uint32_t hi = __shfl_down_sync(0xFFFFFFFFu, nib, 1);
+        const int word = k0 >> 3;
+        if ((lane & 1) == 0 && word < wpr) row_codes[word] = nib | (hi << 16);
+      }
+      __syncwarp();
+    }
+    rows = i;
+    // the row's first maximum: largest value, then smallest column
+    const int best = __reduce_max_sync(0xFFFFFFFFu, lbest);
+    int bestj = __reduce_min_sync(0xFFFFFFFFu, (lbest == best && lbestj >= 0) ? lbestj : 0x7FFFFFFF);
+    if (best <= 0) bestj = -1;
+    if (bestj != n2 && bestj != 1 && (bestj == c0 || bestj == c1)) {
+      status = 1;
+      break;
+    }
+    if (best > score) score = best, e1 = i, e2 = bestj;
+    if (score - best > P.xdrop) break;
+    if (best <= 0) break;
+  }
+  if (lane == 0) {
+    T.status = status;
+    T.rows = rows;
+    if (status == 0) T.score = score, T.end1 = e1, T.end2 = e2;
+  }
+}
+
 void launch_xdrop(XTask *tasks, const int *idx, int n, Arena ar, Params p, uint32_t *tb, int wcap, int32_t *scratch,
                   int64_t scratch_per_thread, cudaStream_t st) {
   if (n <= 0) return;
@@ -136,8 +285,8 @@ void launch_xdrop(XTask *tasks, const int *idx, int n, Arena ar, Params p, uint3
     xdrop_kernel<10><<<g, 128, 0, st>>>(tasks, idx, n, ar, p, tb, scratch, 0);
   else if (wcap == 20)
     xdrop_kernel<20><<<g, 128, 0, st>>>(tasks, idx, n, ar, p, tb, scratch, 0);
-  else
-    xdrop_kernel<0><<<g, 128, 0, st>>>(tasks, idx, n, ar, p, tb, scratch, scratch_per_thread);
+  else  // wide band: one warp per pass, scratch_per_thread = ints per warp
+    xdrop_warp_kernel<<<(n + 3) / 4, 128, 0, st>>>(tasks, idx, n, ar, p, tb, scratch, scratch_per_thread);
 }
 
 // ------------------------------------------------------------------ traceback of the reverse pass
