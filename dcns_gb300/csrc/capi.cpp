@@ -107,32 +107,6 @@ int guarded(dcns_ctx *ctx, F f) {
   }
 }
 
-void init_context(Context &C, int device, size_t budget) {
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
-    (void)cudaGetLastError();
-    throw Error(DCNS_ERR_DEVICE, "no CUDA device available (this library has no CPU fallback)");
-  }
-  if (device < 0 || device >= ndev) throw Error(DCNS_ERR_INVALID, "device ordinal out of range");
-  DCNS_CK(cudaSetDevice(device));
-  cudaDeviceProp prop;
-  DCNS_CK(cudaGetDeviceProperties(&prop, device));
-  if (prop.major < 10) throw Error(DCNS_ERR_DEVICE, "this build targets sm_103a (GB300); found sm_" +
-                                                        std::to_string(prop.major * 10 + prop.minor));
-  C.device = device;
-  C.nsm = prop.multiProcessorCount;
-  C.scan_blocks_per_sm = scan_occupancy();
-  DCNS_CK(cudaStreamCreateWithFlags(&C.st, cudaStreamNonBlocking));
-  DCNS_CK(cudaEventCreate(&C.ev0));
-  DCNS_CK(cudaEventCreate(&C.ev1));
-  if (budget == 0) {
-    size_t fr = 0, tot = 0;
-    DCNS_CK(cudaMemGetInfo(&fr, &tot));
-    budget = fr / 10 * 8;
-  }
-  C.budget = budget;
-}
-
 std::vector<PairIn> to_pairs(const dcns_pair *pairs, int64_t n) {
   if (n < 0 || (n > 0 && !pairs)) throw Error(DCNS_ERR_INVALID, "bad pair array");
   std::vector<PairIn> v((size_t)n);

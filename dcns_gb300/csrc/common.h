@@ -37,6 +37,22 @@ struct ScanTile {
   int32_t task[2];  // result slot of each half, -1 when the half is unused
 };
 
+// Level-0 scan (every window of a pair against its whole reference), described per pair instead of per tile: tile t
+// belongs to the pair with tile_begin <= t < next tile_begin (pairs in longest-reference-first order), covers
+// windows 2d and 2d+1 of that pair (d = (t - tile_begin) / nch) and row chunk (t - tile_begin) % nch.
+struct L0Pair {
+  int64_t ref_base, qry_base, tile_begin, wstart;
+  int32_t n1, n2, nfast, nch;
+};
+struct L0Desc {
+  const L0Pair *pairs;
+  int32_t npairs, step, window, chunk, warm, pad;
+};
+// A level-0 window whose maximum reached min_score, compacted in task order.
+struct L0Rec {
+  int32_t task, score, end1, end2, start1, start2;
+};
+
 // Per Smith-Waterman task (window x reference range): the reduced maximum and, after the reverse scan, the seed.
 struct ScanTask {
   int32_t pair, s2, tw, lo, hi;
@@ -94,6 +110,13 @@ void launch_pack(const int8_t *codes, const int64_t *src_off, const int64_t *dst
                  uint32_t *pk, uint32_t *nm, cudaStream_t st);
 void launch_scan(const ScanTile *tiles, int ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
                  int grid, cudaStream_t st);
+void launch_scan_l0(L0Desc d, int64_t ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
+                    int grid, cudaStream_t st);
+// Compacts the level-0 tasks whose maximum reached min_score (in task order) and runs their reverse scans.
+// scratch: >= (n0 / 256 + 2) ints.  Returns nothing; the count is written to *count (device).
+void launch_l0_select(const unsigned long long *keys, int64_t n0, const int64_t *wstart, const int2 *plen, int np,
+                      const int64_t *seq_base, Arena ar, Params p, int *scratch, int *count, L0Rec *out,
+                      cudaStream_t st);
 void launch_scan_generic(const ScanTask *tasks, const int *idx, int n, const int64_t *seq_base, Arena ar, Params p,
                          unsigned long long *keys, int32_t *scratch, int64_t scratch_per_thread, cudaStream_t st);
 void launch_reverse(ScanTask *tasks, int first, int n, const unsigned long long *keys, const int64_t *pair_base,

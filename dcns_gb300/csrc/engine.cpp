@@ -20,6 +20,7 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <chrono>
 #include <climits>
@@ -94,6 +95,34 @@ Context::~Context() {
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
   if (st) cudaStreamDestroy(st);
+}
+
+void init_context(Context &C, int device, size_t budget) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    (void)cudaGetLastError();
+    throw Error(DCNS_ERR_DEVICE, "no CUDA device available (this library has no CPU fallback)");
+  }
+  if (device < 0 || device >= ndev) throw Error(DCNS_ERR_INVALID, "device ordinal out of range");
+  DCNS_CK(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  DCNS_CK(cudaGetDeviceProperties(&prop, device));
+  if (prop.major < 10)
+    throw Error(DCNS_ERR_DEVICE, "this build targets sm_103a (GB300); found sm_" + std::to_string(prop.major * 10 + prop.minor));
+  C.device = device;
+  C.nsm = prop.multiProcessorCount;
+  C.scan_blocks_per_sm = scan_occupancy();
+  DCNS_CK(cudaStreamCreateWithFlags(&C.st, cudaStreamNonBlocking));
+  DCNS_CK(cudaEventCreate(&C.ev0));
+  DCNS_CK(cudaEventCreate(&C.ev1));
+  if (budget == 0) {
+    size_t fr = 0, tot = 0;
+    DCNS_CK(cudaMemGetInfo(&fr, &tot));
+    budget = fr / 10 * 8;
+  }
+  C.budget = budget;
+  if (const char *e = std::getenv("DCNS_LANES")) C.max_lanes = std::max(1, std::min(8, std::atoi(e)));
+  if (const char *e = std::getenv("DCNS_BINS")) C.bins = std::max(1, std::min(64, std::atoi(e)));
 }
 
 Params to_params(const dcns_params *p) {
@@ -243,19 +272,18 @@ void upload(Context &C, const std::vector<PairIn> &pairs) {
 }
 
 // ------------------------------------------------------------------ 2./3. seed scan with recursion replay
-// Smith-Waterman tasks of one batch: level-0 windows live in pinned host memory (ids [0, n0), pair p owning the
-// contiguous range [wstart[p], wstart[p] + nwin[p])); recursion tasks follow in `more` (ids n0 + k).
+// Smith-Waterman tasks of one batch.  tasks[0, ns) are the level-0 windows the host needs (those whose maximum
+// reached min_score; every window when the generic kernel runs level 0), in pair and window order, pair p owning
+// [pbeg[p], pbeg[p+1]); recursion tasks follow (ids >= ns, device slot id - ns).
 struct ScanState {
-  ScanTask *base = nullptr;
-  int64_t n0 = 0;
-  std::vector<ScanTask> more;
+  std::vector<ScanTask> tasks;
+  int64_t ns = 0;
+  std::vector<int64_t> pbeg;
   std::vector<int32_t> left, right;  // child task id, -1 none/not created
-  std::vector<int64_t> wstart;
-  std::vector<int32_t> nwin;
-  int64_t first_new = 0;  // tasks [first_new, size) still to be computed
-  ScanTask &task(int64_t i) { return i < n0 ? base[i] : more[i - n0]; }
-  const ScanTask &task(int64_t i) const { return i < n0 ? base[i] : more[i - n0]; }
-  int64_t size() const { return n0 + (int64_t)more.size(); }
+  int64_t first_new = 0;             // recursion tasks [first_new, size) still to be computed
+  ScanTask &task(int64_t i) { return tasks[i]; }
+  const ScanTask &task(int64_t i) const { return tasks[i]; }
+  int64_t size() const { return (int64_t)tasks.size(); }
 };
 
 // The fast kernel's table stores s - open in int8 and pads short windows with -16384 in int16 lanes.
@@ -269,13 +297,14 @@ int warmup_rows(const Params &P, int tw) {
   return tw + (P.match * tw + g - 1) / g + 4;
 }
 
-// Launches the scan over `tiles` plus the generic kernel over `generic`, then the reverse scans for tasks
-// [first, first+n); downloads those tasks.  The tasks must already be on the device.
+// Launches the scan over `tiles` plus the generic kernel over `generic` (device slots), then the reverse scans for
+// recursion tasks [first, first+n) (device slots first - ns ...); downloads those tasks.
 void run_scan_round(Context &C, ScanState &S, const Params &P, int64_t first, int64_t n, const ScanTile *tiles,
-                    int64_t ntiles, const std::vector<int32_t> &generic, ScanTask *host_dst) {
+                    int64_t ntiles, const std::vector<int32_t> &generic) {
   auto tx = Clock::now();
-  C.d_keys.ensure(C, sizeof(unsigned long long) * S.size());
-  DCNS_CK(cudaMemsetAsync(C.d_keys.as<unsigned long long>() + first, 0, sizeof(unsigned long long) * n, C.st));
+  const int64_t d0 = first - S.ns;  // device slot of the first task
+  C.d_keys.ensure(C, sizeof(unsigned long long) * (S.size() - S.ns));
+  DCNS_CK(cudaMemsetAsync(C.d_keys.as<unsigned long long>() + d0, 0, sizeof(unsigned long long) * n, C.st));
   if (ntiles > 0) {
     C.d_tiles.ensure(C, sizeof(ScanTile) * ntiles);
     C.d_counter.ensure(C, 64);
@@ -291,7 +320,7 @@ void run_scan_round(Context &C, ScanState &S, const Params &P, int64_t first, in
   }
   if (!generic.empty()) {
     int maxtw = 0;
-    for (int32_t k : generic) maxtw = std::max(maxtw, S.task(k).tw);
+    for (int32_t k : generic) maxtw = std::max(maxtw, S.task(k + S.ns).tw);
     const int64_t per = 3 * ((int64_t)maxtw + 2);
     C.d_idx.ensure(C, sizeof(int32_t) * generic.size());
     C.d_scratch.ensure(C, sizeof(int32_t) * per * generic.size());
@@ -300,10 +329,10 @@ void run_scan_round(Context &C, ScanState &S, const Params &P, int64_t first, in
                         P, C.d_keys.as<unsigned long long>(), C.d_scratch.as<int32_t>(), per, C.st);
     C.stats.kernel_launches += 1;
   }
-  launch_reverse(C.d_tasks.as<ScanTask>(), (int)first, (int)n, C.d_keys.as<unsigned long long>(), C.seqbase_dev,
+  launch_reverse(C.d_tasks.as<ScanTask>(), (int)d0, (int)n, C.d_keys.as<unsigned long long>(), C.seqbase_dev,
                  nullptr, C.arena, P, C.st);
   C.stats.kernel_launches += 1;
-  d2h(C, host_dst, C.d_tasks, (size_t)n, (size_t)first);
+  d2h(C, S.tasks.data() + first, C.d_tasks, (size_t)n, (size_t)d0);
   sync(C);
   C.stats.ms_scan_xfer += ms_since(tx);
   if (ntiles > 0) {
@@ -313,182 +342,49 @@ void run_scan_round(Context &C, ScanState &S, const Params &P, int64_t first, in
   }
 }
 
-// Level 0: every window of every pair against its whole reference.  Tasks and tiles are written in parallel straight
-// into pinned buffers; pairs are laid out by decreasing reference length so the persistent scan kernel's work queue
-// hands out the longest tiles first.
-void scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, const Params &P, bool one_gap) {
-  auto t0 = Clock::now();
-  const int64_t np = (int64_t)pairs.size();
-  S.wstart.assign(np, 0);
-  S.nwin.assign(np, 0);
-  auto count_windows = [&](int32_t n2) {
-    // window starts 0, step, ... as in :462-480 (1-gap stops once past the query end) / :376-390 (2-gap)
-    int32_t k = 0, s = 0;
-    while (true) {
-      ++k;
-      s += P.step;
-      if (one_gap && s > n2) break;
-      if (s + P.window > n2) {
-        ++k;
-        break;
-      }
-    }
-    return k;
-  };
-  int64_t n0 = 0;
-  for (int64_t p = 0; p < np; ++p) {
-    S.wstart[p] = n0;
-    S.nwin[p] = count_windows(pairs[p].n2);
-    n0 += S.nwin[p];
-  }
-  S.n0 = n0;
-  S.first_new = n0;
-  C.h_tasks.ensure(sizeof(ScanTask) * std::max<int64_t>(n0, 1));
-  S.base = C.h_tasks.as<ScanTask>();
-  const bool fast = fast_scan_ok(P);
-  // windows with tw > 0 pair up two per tile; tw <= 0 windows (a short tail can be empty) are never scanned
-  std::vector<int32_t> nfast(np, 0);
-  int64_t total_rows = 0, nduo = 0;
-  for (int64_t p = 0; p < np; ++p) {
-    int32_t cnt = 0;
-    for (int32_t k = 0; k < S.nwin[p]; ++k) {
-      const int32_t s2 = k * P.step;
-      const int32_t tw = (s2 + P.window) > pairs[p].n2 ? (pairs[p].n2 - s2) : P.window;
-      if (tw > 0 && pairs[p].n1 > 0) ++cnt;
-    }
-    nfast[p] = fast ? cnt : 0;
-    nduo += (nfast[p] + 1) / 2;
-    total_rows += (int64_t)((nfast[p] + 1) / 2) * pairs[p].n1;
-  }
-  const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * 128;
-  const int K = warmup_rows(P, kScanW);
-  int64_t chunk = INT64_MAX;
-  if (nduo < 8 * resident && K != INT_MAX && total_rows > 0)
-    chunk = std::max<int64_t>(4 * (int64_t)K, (total_rows + 8 * resident - 1) / (8 * resident));
-  std::vector<int64_t> order(np), tile_off(np + 1, 0);
-  for (int64_t p = 0; p < np; ++p) order[p] = p;
-  std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
-    return pairs[a].n1 != pairs[b].n1 ? pairs[a].n1 > pairs[b].n1 : a < b;
-  });
-  auto nchunks = [&](int32_t n1) -> int64_t { return chunk == INT64_MAX ? 1 : (n1 + chunk - 1) / chunk; };
-  std::vector<int64_t> toff(np, 0);
-  int64_t ntiles = 0;
-  for (int64_t q = 0; q < np; ++q) {
-    const int64_t p = order[q];
-    toff[p] = ntiles;
-    ntiles += (int64_t)((nfast[p] + 1) / 2) * nchunks(pairs[p].n1);
-  }
-  C.h_tiles.ensure(sizeof(ScanTile) * std::max<int64_t>(ntiles, 1));
-  ScanTile *tiles = C.h_tiles.as<ScanTile>();
-  std::vector<std::vector<int32_t>> gen(np);
-  parallel_for(np, [&](int64_t p) {
-    const int32_t n1 = pairs[p].n1, n2 = pairs[p].n2;
-    ScanTask *T = S.base + S.wstart[p];
-    int32_t pending = -1;
-    int64_t to = toff[p];
-    auto emit = [&](int32_t a, int32_t b) {
-      ScanTile tl{};
-      tl.ref_base = C.seq_base[2 * p];
-      tl.qry_base = C.seq_base[2 * p + 1];
-      for (int h = 0; h < 2; ++h) {
-        const int32_t id = h == 0 ? a : b;
-        if (id >= 0) {
-          const ScanTask &x = S.base[id];
-          tl.s2[h] = x.s2, tl.tw[h] = x.tw, tl.lo[h] = 0, tl.hi[h] = n1, tl.task[h] = id;
-        } else {
-          tl.s2[h] = 0, tl.tw[h] = 0, tl.lo[h] = 0, tl.hi[h] = n1, tl.task[h] = -1;
-        }
-      }
-      for (int64_t c0 = 0; c0 < n1; c0 += chunk) {
-        ScanTile t = tl;
-        t.cnt_begin = (int32_t)c0;
-        t.row_end = (int32_t)std::min<int64_t>(n1, c0 + chunk);
-        t.row_begin = (int32_t)std::max<int64_t>(0, c0 - (c0 == 0 ? 0 : K));
-        tiles[to++] = t;
-        if (chunk == INT64_MAX) break;
-      }
-    };
-    for (int32_t k = 0; k < S.nwin[p]; ++k) {
-      ScanTask x{};
-      x.pair = (int32_t)p;
-      x.s2 = k * P.step;
-      x.tw = (x.s2 + P.window) > n2 ? (n2 - x.s2) : P.window;
-      x.lo = 0;
-      x.hi = n1;
-      x.striped = striped_for_host(n1, x.tw, P.open1, P.ext1, P.match) ? 1 : 0;
-      T[k] = x;
-      const int32_t id = (int32_t)(S.wstart[p] + k);
-      if (x.tw <= 0 || n1 <= 0) continue;
-      if (!fast) {
-        gen[p].push_back(id);
-        continue;
-      }
-      if (pending < 0) {
-        pending = id;
-      } else {
-        emit(pending, id);
-        pending = -1;
-      }
-    }
-    if (pending >= 0) emit(pending, -1);
-  });
-  std::vector<int32_t> generic;
-  for (auto &g : gen) generic.insert(generic.end(), g.begin(), g.end());
-  S.left.assign(n0, -1);
-  S.right.assign(n0, -1);
-  C.stats.ms_scan_prep += ms_since(t0);
-  C.d_tasks.ensure(C, sizeof(ScanTask) * std::max<int64_t>(n0, 1));
-  auto tx = Clock::now();
-  h2d(C, C.d_tasks, S.base, (size_t)n0);
-  C.stats.ms_scan_xfer += ms_since(tx);
-  run_scan_round(C, S, P, 0, n0, tiles, ntiles, generic, S.base);
-  C.stats.ms_scan += ms_since(t0);
-}
-
-// Recursion rounds: tasks [S.first_new, size) (all in `more`).  Fast tasks of one pair with similar row ranges are
-// paired into int16x2 tiles; the rest go to the generic kernel.
+// Recursion rounds (and the generic level 0): tasks [S.first_new, size).  Fast tasks of one pair with similar row
+// ranges are paired into int16x2 tiles; the rest go to the generic kernel.
 void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
   const int64_t first = S.first_new, n = S.size() - first;
   if (n <= 0) return;
   S.first_new = S.size();
   auto t0 = Clock::now();
   const bool fast_ok = fast_scan_ok(P);
-  std::vector<int32_t> fast, generic;
+  std::vector<int32_t> fast, generic;  // device slots
   for (int64_t k = first; k < first + n; ++k) {
     ScanTask &T = S.task(k);
     T.striped = striped_for_host(T.hi - T.lo, T.tw, P.open1, P.ext1, P.match) ? 1 : 0;
     if (T.tw <= 0 || T.hi <= T.lo) continue;  // nothing to scan: key stays 0
     if (fast_ok && T.striped && T.tw <= kScanW)
-      fast.push_back((int32_t)k);
+      fast.push_back((int32_t)(k - S.ns));
     else
-      generic.push_back((int32_t)k);
+      generic.push_back((int32_t)(k - S.ns));
   }
-  std::sort(fast.begin(), fast.end(), [&](int32_t a, int32_t b) {
-    const ScanTask &x = S.task(a), &y = S.task(b);
-    if (x.pair != y.pair) return x.pair < y.pair;
-    if (x.lo != y.lo) return x.lo < y.lo;
-    if (x.hi != y.hi) return x.hi < y.hi;
-    return x.s2 < y.s2;
+  auto tk = [&](int32_t d) -> const ScanTask & { return S.task(d + S.ns); };
+  // Recursion tasks arrive grouped by pair (the replay requests them pair by pair); within a pair, order by row
+  // range so that the two halves of a tile cover similar rows.  Pairs' groups are sorted independently.
+  std::vector<size_t> gb{0};
+  for (size_t i = 1; i <= fast.size(); ++i)
+    if (i == fast.size() || tk(fast[i]).pair != tk(fast[i - 1]).pair) gb.push_back(i);
+  parallel_for((int64_t)gb.size() - 1, [&](int64_t g) {
+    std::sort(fast.begin() + gb[g], fast.begin() + gb[g + 1], [&](int32_t a, int32_t b) {
+      const ScanTask &x = tk(a), &y = tk(b);
+      if (x.lo != y.lo) return x.lo < y.lo;
+      if (x.hi != y.hi) return x.hi < y.hi;
+      return x.s2 < y.s2;
+    });
   });
   struct Half2 {
     int32_t a, b;
   };
   std::vector<Half2> duo;
-  for (size_t i = 0; i < fast.size();) {
-    const int32_t a = fast[i];
-    if (i + 1 < fast.size() && S.task(fast[i + 1]).pair == S.task(a).pair) {
-      duo.push_back({a, fast[i + 1]});
-      i += 2;
-    } else {
-      duo.push_back({a, -1});
-      i += 1;
-    }
-  }
+  for (size_t g = 0; g + 1 < gb.size(); ++g)
+    for (size_t i = gb[g]; i < gb[g + 1]; i += 2) duo.push_back({fast[i], i + 1 < gb[g + 1] ? fast[i + 1] : -1});
   int64_t total_rows = 0;
   for (const Half2 &d : duo) {
-    const ScanTask &A = S.task(d.a);
+    const ScanTask &A = tk(d.a);
     int lo = A.lo, hi = A.hi;
-    if (d.b >= 0) lo = std::min(lo, S.task(d.b).lo), hi = std::max(hi, S.task(d.b).hi);
+    if (d.b >= 0) lo = std::min(lo, tk(d.b).lo), hi = std::max(hi, tk(d.b).hi);
     total_rows += hi - lo;
   }
   const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * 128;
@@ -501,13 +397,13 @@ void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
   tiles.reserve(duo.size() + 16);
   for (const Half2 &d : duo) {
     ScanTile tl{};
-    const ScanTask &A = S.task(d.a);
+    const ScanTask &A = tk(d.a);
     tl.ref_base = C.seq_base[2 * A.pair];
     tl.qry_base = C.seq_base[2 * A.pair + 1];
     int lo = A.lo, hi = A.hi;
     tl.s2[0] = A.s2, tl.tw[0] = A.tw, tl.lo[0] = A.lo, tl.hi[0] = A.hi, tl.task[0] = d.a;
     if (d.b >= 0) {
-      const ScanTask &B = S.task(d.b);
+      const ScanTask &B = tk(d.b);
       tl.s2[1] = B.s2, tl.tw[1] = B.tw, tl.lo[1] = B.lo, tl.hi[1] = B.hi, tl.task[1] = d.b;
       lo = std::min(lo, B.lo);
       hi = std::max(hi, B.hi);
@@ -524,17 +420,200 @@ void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
       if (chunk == INT64_MAX) break;
     }
   }
-  std::sort(tiles.begin(), tiles.end(), [](const ScanTile &a, const ScanTile &b) {
-    return (a.row_end - a.row_begin) > (b.row_end - b.row_begin);
-  });
+  // longest tiles first for the work queue: a bucket order by log-length (linear time)
+  {
+    std::vector<std::vector<ScanTile>> bucket(64);
+    for (const ScanTile &t : tiles) {
+      const int len = std::max(1, t.row_end - t.row_begin);
+      const int b = std::min(63, (int)(4.0 * std::log2((double)len)));
+      bucket[63 - b].push_back(t);
+    }
+    tiles.clear();
+    for (auto &bk : bucket) tiles.insert(tiles.end(), bk.begin(), bk.end());
+  }
   C.stats.ms_scan_prep += ms_since(t0);
-  C.d_tasks.ensure(C, sizeof(ScanTask) * S.size());
-  // tasks [first, first+n) are all recursion tasks: contiguous in `more`
-  h2d(C, C.d_tasks, S.more.data() + (first - S.n0), (size_t)n, (size_t)first);
-  run_scan_round(C, S, P, first, n, tiles.data(), (int64_t)tiles.size(), generic, S.more.data() + (first - S.n0));
+  C.d_tasks.ensure(C, sizeof(ScanTask) * (S.size() - S.ns));
+  h2d(C, C.d_tasks, S.tasks.data() + first, (size_t)n, (size_t)(first - S.ns));
+  run_scan_round(C, S, P, first, n, tiles.data(), (int64_t)tiles.size(), generic);
   C.stats.ms_scan += ms_since(t0);
   S.left.resize(S.size(), -1);
   S.right.resize(S.size(), -1);
+}
+
+// Number of windows of the drivers' loops (:462-480 for 1-gap, which stops once past the query end; :376-390 for
+// 2-gap): start 0 always, then i*step while i*step + window <= n2, then the first i* with i*step + window > n2 unless
+// the 1-gap loop already stopped at i*step > n2.
+int32_t window_count(int32_t n2, const Params &P, bool one_gap) {
+  const int32_t istar = (n2 - P.window < 0) ? 1 : (n2 - P.window) / P.step + 1;
+  const bool pushed = !(one_gap && (int64_t)istar * P.step > n2);
+  return istar + (pushed ? 1 : 0);
+}
+
+inline int32_t window_tw(int32_t n2, int32_t s2, const Params &P) { return (s2 + P.window) > n2 ? (n2 - s2) : P.window; }
+
+// Level 0: every window of every pair against its whole reference.  On the fast path the device derives each tile
+// from a per-pair table and compacts the windows whose maximum reached min_score (with their reverse re-scans);
+// only those records reach the host.  Returns the level-0 algorithmic cells (every window is scanned).
+int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, const Params &P, bool one_gap) {
+  auto t0 = Clock::now();
+  const int64_t np = (int64_t)pairs.size();
+  std::vector<int64_t> wstart(np + 1, 0);
+  std::vector<int32_t> nwin(np), nfast(np);
+  int64_t cells = 0;
+  for (int64_t p = 0; p < np; ++p) {
+    const int32_t n1 = pairs[p].n1, n2 = pairs[p].n2;
+    nwin[p] = window_count(n2, P, one_gap);
+    wstart[p + 1] = wstart[p] + nwin[p];
+    // windows with tw > 0 are the prefix w * step < n2
+    nfast[p] = n1 > 0 ? std::min<int32_t>(nwin[p], (n2 + P.step - 1) / P.step) : 0;
+    // scan cells: n1 * sum of tw over scanned windows (full windows, then the short tail)
+    const int32_t nfull = std::min<int32_t>(nfast[p], n2 >= P.window ? (n2 - P.window) / P.step + 1 : 0);
+    int64_t tws = (int64_t)nfull * P.window;
+    for (int32_t w = nfull; w < nfast[p]; ++w) tws += std::max(0, window_tw(n2, w * P.step, P));
+    cells += (int64_t)n1 * tws;
+  }
+  const int64_t n0 = wstart[np];
+  S.tasks.clear();
+  S.pbeg.assign(np + 1, 0);
+  if (!fast_scan_ok(P)) {
+    // generic level 0: every window is a task the replay walks (those below min_score are skipped there)
+    S.tasks.reserve(n0);
+    for (int64_t p = 0; p < np; ++p) {
+      S.pbeg[p] = (int64_t)S.tasks.size();
+      for (int32_t k = 0; k < nwin[p]; ++k) {
+        ScanTask x{};
+        x.pair = (int32_t)p;
+        x.s2 = k * P.step;
+        x.tw = window_tw(pairs[p].n2, x.s2, P);
+        x.lo = 0;
+        x.hi = pairs[p].n1;
+        S.tasks.push_back(x);
+      }
+    }
+    S.pbeg[np] = (int64_t)S.tasks.size();
+    S.ns = 0;
+    S.first_new = 0;
+    C.stats.ms_scan_prep += ms_since(t0);
+    compute_scan_tasks(C, S, P);
+    S.ns = S.size();
+    S.first_new = S.ns;
+    S.left.assign(S.size(), -1);
+    S.right.assign(S.size(), -1);
+    return cells;
+  }
+  int64_t total_rows = 0, nduo = 0;
+  for (int64_t p = 0; p < np; ++p) {
+    nduo += (nfast[p] + 1) / 2;
+    total_rows += (int64_t)((nfast[p] + 1) / 2) * pairs[p].n1;
+  }
+  const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * 128;
+  const int K = warmup_rows(P, kScanW);
+  int64_t chunk = INT32_MAX;
+  if (nduo < 8 * resident && K != INT_MAX && total_rows > 0)
+    chunk = std::min<int64_t>(INT32_MAX, std::max<int64_t>(4 * (int64_t)K, (total_rows + 8 * resident - 1) / (8 * resident)));
+  std::vector<int64_t> order(np);
+  for (int64_t p = 0; p < np; ++p) order[p] = p;
+  std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+    return pairs[a].n1 != pairs[b].n1 ? pairs[a].n1 > pairs[b].n1 : a < b;
+  });
+  C.h_misc.ensure(sizeof(L0Pair) * np + sizeof(int64_t) * (np + 1) + sizeof(int2) * np + 64);
+  L0Pair *tab = C.h_misc.as<L0Pair>();
+  int64_t ntiles = 0;
+  for (int64_t q = 0; q < np; ++q) {
+    const int64_t p = order[q];
+    L0Pair &e = tab[q];
+    e.ref_base = C.seq_base[2 * p];
+    e.qry_base = C.seq_base[2 * p + 1];
+    e.tile_begin = ntiles;
+    e.wstart = wstart[p];
+    e.n1 = pairs[p].n1;
+    e.n2 = pairs[p].n2;
+    e.nfast = nfast[p];
+    e.nch = chunk >= INT32_MAX ? 1 : (int32_t)std::max<int64_t>(1, (pairs[p].n1 + chunk - 1) / chunk);
+    ntiles += (int64_t)((nfast[p] + 1) / 2) * e.nch;
+  }
+  int64_t *wst = reinterpret_cast<int64_t *>(tab + np);
+  int2 *plen = reinterpret_cast<int2 *>(wst + np + 1);
+  for (int64_t p = 0; p <= np; ++p) wst[p] = wstart[p];
+  for (int64_t p = 0; p < np; ++p) plen[p] = int2{pairs[p].n1, pairs[p].n2};
+  C.stats.ms_scan_prep += ms_since(t0);
+  auto tx = Clock::now();
+  C.d_tiles.ensure(C, sizeof(L0Pair) * np + 64);
+  C.d_scratch.ensure(C, sizeof(int64_t) * (np + 1) + sizeof(int2) * np + sizeof(int) * ((n0 + 255) / 256 + 8) + 64);
+  C.d_keys.ensure(C, sizeof(unsigned long long) * std::max<int64_t>(n0, 1));
+  C.d_counter.ensure(C, 64);
+  C.d_tasks.ensure(C, sizeof(L0Rec) * std::max<int64_t>(n0, 1));
+  int64_t *d_wst = C.d_scratch.as<int64_t>();
+  int2 *d_plen = reinterpret_cast<int2 *>(d_wst + np + 1);
+  int *d_blk = reinterpret_cast<int *>(d_plen + np);
+  int *d_count = C.d_counter.as<int>() + 1;
+  h2d(C, C.d_tiles, tab, (size_t)np);
+  DCNS_CK(cudaMemcpyAsync(d_wst, wst, sizeof(int64_t) * (np + 1), cudaMemcpyHostToDevice, C.st));
+  DCNS_CK(cudaMemcpyAsync(d_plen, plen, sizeof(int2) * np, cudaMemcpyHostToDevice, C.st));
+  DCNS_CK(cudaMemsetAsync(C.d_keys.p, 0, sizeof(unsigned long long) * n0, C.st));
+  DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int) * 2, C.st));
+  L0Desc D{C.d_tiles.as<L0Pair>(), (int32_t)np, P.step, P.window, (int32_t)chunk, K, 0};
+  const int grid = (int)std::min<int64_t>((int64_t)C.nsm * C.scan_blocks_per_sm, (ntiles + 127) / 128);
+  DCNS_CK(cudaEventRecord(C.ev0, C.st));
+  launch_scan_l0(D, ntiles, C.arena, P, C.d_keys.as<unsigned long long>(), C.d_counter.as<int>(), std::max(grid, 1),
+                 C.st);
+  DCNS_CK(cudaEventRecord(C.ev1, C.st));
+  C.stats.scan_launches += 1;
+  C.stats.kernel_launches += 1;
+  launch_l0_select(C.d_keys.as<unsigned long long>(), n0, d_wst, d_plen, (int)np, C.seqbase_dev, C.arena, P, d_blk,
+                   d_count, C.d_tasks.as<L0Rec>(), C.st);
+  C.stats.kernel_launches += 3;
+  int nsel = 0;
+  DCNS_CK(cudaMemcpyAsync(&nsel, d_count, sizeof(int), cudaMemcpyDeviceToHost, C.st));
+  sync(C);
+  C.h_tasks.ensure(sizeof(L0Rec) * std::max(nsel, 1));
+  L0Rec *rec = C.h_tasks.as<L0Rec>();
+  d2h(C, rec, C.d_tasks, (size_t)nsel);
+  sync(C);
+  {
+    float ms = 0;
+    DCNS_CK(cudaEventElapsedTime(&ms, C.ev0, C.ev1));
+    C.stats.ms_scan_kernel += ms;
+  }
+  C.stats.ms_scan_xfer += ms_since(tx);
+  auto tb = Clock::now();
+  S.tasks.resize(nsel);
+  // records are in task order: pair p's records start at the first record with task >= wstart[p]
+  for (int64_t p = 0; p <= np; ++p) {
+    int64_t lo = 0, hi = nsel;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      if (rec[mid].task < wstart[p])
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    S.pbeg[p] = lo;
+  }
+  parallel_for(np, [&](int64_t p) {
+    for (int64_t k = S.pbeg[p]; k < S.pbeg[p + 1]; ++k) {
+      const L0Rec &r = rec[k];
+      ScanTask x{};
+      x.pair = (int32_t)p;
+      x.s2 = (int32_t)(r.task - wstart[p]) * P.step;
+      x.tw = window_tw(pairs[p].n2, x.s2, P);
+      x.lo = 0;
+      x.hi = pairs[p].n1;
+      x.score = r.score;
+      x.end1 = r.end1;
+      x.end2 = r.end2;
+      x.start1 = r.start1;
+      x.start2 = r.start2;
+      S.tasks[k] = x;
+    }
+  });
+  S.ns = nsel;
+  S.first_new = nsel;
+  S.left.assign(nsel, -1);
+  S.right.assign(nsel, -1);
+  C.stats.ms_scan_prep += ms_since(tb);
+  C.stats.ms_scan += ms_since(t0);
+  return cells;
 }
 
 inline Seed4 seed_of(const ScanTask &T) { return Seed4{T.start1, T.end1, T.start2, T.end2}; }
@@ -558,38 +637,27 @@ bool subtree(ReplayCtx &R, int32_t t, SeedSet &out) {
   R.cells_rev += (int64_t)std::min(T.end1 - T.lo + 1, lim) * std::min(T.end2 - T.s2 + 1, lim);
   out.insert(seed_of(T));
   bool ok = true;
-  if (T.start1 - T.lo >= R.mini) {
-    const int32_t c = R.S.left[t];
+  for (int side = 0; side < 2; ++side) {
+    const bool cond = side == 0 ? (T.start1 - T.lo >= R.mini) : (T.hi - T.end1 - 1 >= R.mini);
+    if (!cond) continue;
+    const int32_t c = side == 0 ? R.S.left[t] : R.S.right[t];
     if (c < 0) {
-      R.req.push_back({t, 0});
+      R.req.push_back({t, side});
       ok = false;
-    } else {
-      SeedSet sub;
-      ok &= subtree(R, c, sub);
-      for (const Seed4 &s : sub) out.insert(s);
+      continue;
     }
-  }
-  if (T.hi - T.end1 - 1 >= R.mini) {
-    const int32_t c = R.S.right[t];
-    if (c < 0) {
-      R.req.push_back({t, 1});
-      ok = false;
-    } else {
-      SeedSet sub;
-      ok &= subtree(R, c, sub);
-      for (const Seed4 &s : sub) out.insert(s);
-    }
+    SeedSet sub;
+    ok &= subtree(R, c, sub);
+    for (const Seed4 &s : sub) out.insert(s);
   }
   return ok;
 }
 
-// The set-gated window loop (:131-201 per window, :462-480 over windows).
+// The set-gated window loop (:131-201 per window, :462-480 over windows) over the pair's level-0 windows with a seed.
 bool replay_pair(ReplayCtx &R, int64_t p, SeedSet &global) {
   bool ok = true;
-  for (int64_t t = R.S.wstart[p]; t < R.S.wstart[p] + R.S.nwin[p]; ++t) {
+  for (int64_t t = R.S.pbeg[p]; t < R.S.pbeg[p + 1]; ++t) {
     const ScanTask &T = R.S.task(t);
-    R.visited++;
-    R.cells += (int64_t)(T.hi - T.lo) * std::max(T.tw, 0);
     if (T.score < R.P.min_score) continue;
     const int lim = T.tw + R.P.window;
     R.cells_rev += (int64_t)std::min(T.end1 - T.lo + 1, lim) * std::min(T.end2 - T.s2 + 1, lim);
@@ -601,7 +669,7 @@ bool replay_pair(ReplayCtx &R, int64_t p, SeedSet &global) {
       if (!cond) continue;
       const int32_t c = side == 0 ? R.S.left[t] : R.S.right[t];
       if (c < 0) {
-        R.req.push_back({t, side});
+        R.req.push_back({(int32_t)t, side});
         ok = false;
         continue;
       }
@@ -655,35 +723,21 @@ void link_seeds(SeedSet &seeds) {  // :288-344
   for (const Seed4 &s : cur) seeds.insert(s);
 }
 
-// Window starts of the 1-gap driver (:462-480, stops once past the query end) and of getAllExtendSeed (:376-390).
-void window_starts(int32_t n2, const Params &P, bool stop_past_end, std::vector<int32_t> &st) {
-  st.clear();
-  int32_t s = 0;
-  while (true) {
-    st.push_back(s);
-    s += P.step;
-    if (stop_past_end && s > n2) break;
-    if (s + P.window > n2) {
-      st.push_back(s);
-      break;
-    }
-  }
-}
-
 // Seed scan + replay + linking for every pair; returns the linked seed list of each pair in set order.
 void scan_and_link(Context &C, const std::vector<PairIn> &pairs, const Params &P, bool one_gap,
                    std::vector<std::vector<Seed4>> &linked) {
   const int64_t np = (int64_t)pairs.size();
   ScanState S;
-  scan_level0(C, S, pairs, P, one_gap);
+  int64_t cells = scan_level0(C, S, pairs, P, one_gap);
+  int64_t level0_tasks = 0;
+  for (int64_t p = 0; p < np; ++p) level0_tasks += window_count(pairs[p].n2, P, one_gap);
   const int mini = P.min_score / P.match;
   std::vector<SeedSet> sets(np);
   std::vector<uint8_t> done(np, 0);
-  int64_t cells = 0, cells_rev = 0, visited_final = 0;
+  int64_t cells_rev = 0, visited_final = 0;
   for (int round = 0;; ++round) {
     if (round > 0) compute_scan_tasks(C, S, P);
     auto t0 = Clock::now();
-    std::vector<ReplayCtx> rc;
     std::vector<std::vector<std::pair<int32_t, int32_t>>> reqs(np);
     std::vector<int64_t> pc(np, 0), pr(np, 0), pv(np, 0);
     std::vector<int64_t> todo;
@@ -711,8 +765,7 @@ void scan_and_link(Context &C, const std::vector<PairIn> &pairs, const Params &P
       visited_final += pv[p];
       for (auto &rq : reqs[p]) {
         const int32_t t = rq.first;
-        int32_t &slot = rq.second == 0 ? S.left[t] : S.right[t];
-        if (slot >= 0) continue;
+        if ((rq.second == 0 ? S.left[t] : S.right[t]) >= 0) continue;
         const ScanTask P0 = S.task(t);
         ScanTask ch{};
         ch.pair = P0.pair;
@@ -725,21 +778,21 @@ void scan_and_link(Context &C, const std::vector<PairIn> &pairs, const Params &P
           ch.lo = P0.end1 + 1;
           ch.hi = P0.hi;
         }
-        slot = (int32_t)S.size();
-        S.more.push_back(ch);
+        (rq.second == 0 ? S.left[t] : S.right[t]) = (int32_t)S.size();
+        S.tasks.push_back(ch);
         ++nreq;
       }
+      S.left.resize(S.size(), -1);
+      S.right.resize(S.size(), -1);
     }
-    S.left.resize(S.size(), -1);
-    S.right.resize(S.size(), -1);
     C.stats.ms_replay += ms_since(t0);
     if (nreq == 0) break;
     if (round > 100000) throw Error(DCNS_ERR_DEVICE, "seed recursion did not converge");
   }
   C.stats.cells_scan += cells;
   C.stats.cells_scan_reverse += cells_rev;
-  C.stats.tasks_scan += visited_final;
-  C.stats.tasks_scan_speculative += S.size() - visited_final;
+  C.stats.tasks_scan += level0_tasks + visited_final;
+  C.stats.tasks_scan_speculative += (S.size() - S.ns) - visited_final;
   auto t0 = Clock::now();
   linked.assign(np, {});
   parallel_for(np, [&](int64_t p) {
@@ -774,8 +827,9 @@ int wpr_of(int w) { return (2 * w + 1 + 7) / 8; }
 
 // Runs the given x-drop passes to completion (band restarts, traceback-slot growth), then their tracebacks when
 // want_codes.  X lives on the host between launches.
-void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_codes,
-               std::vector<std::vector<uint32_t>> *cigars) {
+// With want_codes, every pass's CIGAR is appended to *flat and hoff[k] is its offset there (X[k].ncig words).
+void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_codes, std::vector<uint32_t> *flat,
+               std::vector<int64_t> *hoff) {
   if (X.empty()) return;
   auto t0 = Clock::now();
   const int64_t n = (int64_t)X.size();
@@ -787,7 +841,8 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
     X[k].iii = X[k].jjj = X[k].ncig = 0;
     rows_cap[k] = std::min<int64_t>(X[k].n1, 1024);
   }
-  if (cigars) cigars->assign(n, {});
+  if (flat) flat->clear();
+  if (hoff) hoff->assign(n, -1);
   std::vector<int32_t> pend(n);
   for (int64_t k = 0; k < n; ++k) pend[k] = (int32_t)k;
   C.d_x.ensure(C, sizeof(XTask) * n);
@@ -876,7 +931,8 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
         const int32_t k = pend[q];
         X[k] = Xc[q];
         if (X[k].status == 3) throw Error(DCNS_ERR_DEVICE, "x-drop traceback exceeded its CIGAR slot");
-        (*cigars)[k].assign(hc + X[k].cig_off, hc + X[k].cig_off + X[k].ncig);
+        (*hoff)[k] = (int64_t)flat->size();
+        flat->insert(flat->end(), hc + X[k].cig_off, hc + X[k].cig_off + X[k].ncig);
       }
     }
     pend.swap(next);
@@ -893,14 +949,15 @@ inline void evalue(const Params &P, double L1, double L2, int32_t score, double 
 struct XSeedOut {
   bool ok;
   int32_t start1, end1, start2, end2, score;
-  std::vector<uint32_t> cigar;
+  int64_t cig_off;  // into the stage's flat CIGAR buffer
+  int32_t cig_len;
 };
 
 // x_extend_seed (:205-285) for every linked seed of every pair: forward pass, reverse pass (with codes when
 // want_cigar), then the coordinate bookkeeping of the reference.
 void extend_seeds(Context &C, const std::vector<PairIn> &pairs, const Params &P,
                   const std::vector<std::vector<Seed4>> &linked, bool want_cigar,
-                  std::vector<std::vector<XSeedOut>> &res) {
+                  std::vector<std::vector<XSeedOut>> &res, std::vector<uint32_t> &cig_flat) {
   const int64_t np = (int64_t)pairs.size();
   res.assign(np, {});
   std::vector<XTask> F;
@@ -923,7 +980,7 @@ void extend_seeds(Context &C, const std::vector<PairIn> &pairs, const Params &P,
     }
   }
   C.stats.seeds += (int64_t)F.size();
-  run_xdrop(C, F, P, false, nullptr);
+  run_xdrop(C, F, P, false, nullptr, nullptr);
   std::vector<XTask> R;
   std::vector<int32_t> rmap;
   for (size_t k = 0; k < F.size(); ++k) {
@@ -931,6 +988,8 @@ void extend_seeds(Context &C, const std::vector<PairIn> &pairs, const Params &P,
     XSeedOut &o = res[owner[k].first][owner[k].second];
     o.ok = false;
     o.score = f.score;
+    o.cig_off = 0;
+    o.cig_len = 0;
     if (f.end1 - 1 < 0 || f.end2 - 1 < 0) continue;  // p = 100
     const int32_t b1 = f.a1 + f.end1 - 1, b2 = f.a2 + f.end2 - 1;
     XTask r{};
@@ -945,14 +1004,14 @@ void extend_seeds(Context &C, const std::vector<PairIn> &pairs, const Params &P,
     R.push_back(r);
     rmap.push_back((int32_t)k);
   }
-  std::vector<std::vector<uint32_t>> cg;
-  run_xdrop(C, R, P, want_cigar, want_cigar ? &cg : nullptr);
+  std::vector<int64_t> hoff;
+  run_xdrop(C, R, P, want_cigar, want_cigar ? &cig_flat : nullptr, want_cigar ? &hoff : nullptr);
   for (size_t q = 0; q < R.size(); ++q) {
     const XTask &r = R[q];
     const XTask &f = F[rmap[q]];
     XSeedOut &o = res[owner[rmap[q]].first][owner[rmap[q]].second];
     o.score = r.score;
-    if (want_cigar) o.cigar.swap(cg[q]);
+    if (want_cigar) o.cig_off = hoff[q], o.cig_len = r.ncig;
     if (r.end1 - 1 < 0 || r.end2 - 1 < 0) continue;
     const int32_t b1 = f.a1 + f.end1 - 1, b2 = f.a2 + f.end2 - 1;
     o.ok = true;
@@ -1135,6 +1194,8 @@ void two_gap_stage(Context &C, const std::vector<PairIn> &pairs, const Params &P
 // ------------------------------------------------------------------ entry points
 void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
                 std::vector<std::vector<FragOut>> &out);
+void align_single(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
+                  std::vector<std::vector<FragOut>> &out);
 
 void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
                  std::vector<std::vector<FragOut>> &out) {
@@ -1178,14 +1239,100 @@ void align_batch(Context &C, Batch &B, const Params &P, int mode, std::vector<st
   C.stats.ms_total = ms_since(t0);
 }
 
+void add_stats(dcns_stats &a, const dcns_stats &b) {
+  a.cells_scan += b.cells_scan, a.cells_scan_reverse += b.cells_scan_reverse, a.cells_xdrop += b.cells_xdrop;
+  a.cells_semiglobal += b.cells_semiglobal, a.tasks_scan += b.tasks_scan;
+  a.tasks_scan_speculative += b.tasks_scan_speculative, a.seeds += b.seeds, a.xdrop_passes += b.xdrop_passes;
+  a.semiglobal_dps += b.semiglobal_dps, a.ms_upload += b.ms_upload, a.ms_scan += b.ms_scan;
+  a.ms_replay += b.ms_replay, a.ms_xdrop += b.ms_xdrop, a.ms_semiglobal += b.ms_semiglobal;
+  a.ms_download += b.ms_download, a.ms_scan_kernel += b.ms_scan_kernel, a.ms_scan_prep += b.ms_scan_prep;
+  a.ms_scan_xfer += b.ms_scan_xfer, a.ms_link += b.ms_link, a.scan_launches += b.scan_launches;
+  a.kernel_launches += b.kernel_launches;
+}
+
+// Batches large enough to fill the GPU several times over are split into bins of similar work (pairs dealt
+// round-robin in decreasing n1*n2), and the bins are run by two lanes: while one lane's host threads replay seed sets
+// and link, the other lane's kernels run.  Results and stats are the per-pair results of the single-lane path.
 void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
                 std::vector<std::vector<FragOut>> &out) {
+  const int64_t np = (int64_t)pairs.size();
+  const int nl = C.is_lane ? 1 : C.max_lanes;
+  const int kBins = std::max(C.bins, nl);
+  if (nl < 2 || np < 4096) {
+    align_single(C, pairs, P, mode, out);
+    return;
+  }
+  DCNS_CK(cudaStreamSynchronize(C.st));  // the arena (packed on this context's stream) is complete
+  while ((int)C.lanes.size() < nl) {
+    auto L = std::make_unique<Context>();
+    const size_t room = C.budget > C.used ? C.budget - C.used : 0;
+    init_context(*L, C.device, std::max<size_t>(room / (2 * nl), (size_t)1 << 30));
+    L->is_lane = true;
+    C.lanes.push_back(std::move(L));
+  }
+  std::vector<int64_t> order(np);
+  for (int64_t p = 0; p < np; ++p) order[p] = p;
+  std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+    const int64_t wa = (int64_t)pairs[a].n1 * pairs[a].n2, wb = (int64_t)pairs[b].n1 * pairs[b].n2;
+    return wa != wb ? wa > wb : a < b;
+  });
+  std::vector<std::vector<int64_t>> bins(kBins);
+  for (int64_t q = 0; q < np; ++q) bins[q % kBins].push_back(order[q]);
+  for (auto &b : bins) std::sort(b.begin(), b.end());  // each bin keeps the caller's pair order
+  std::atomic<int> next(0);
+  std::vector<std::string> errs(nl);
+  std::vector<int> codes(nl, 0);
+  std::vector<dcns_stats> st(nl, dcns_stats{});
+  auto worker = [&](int l) {
+    Context &L = *C.lanes[l];
+    try {
+      DCNS_CK(cudaSetDevice(C.device));
+      for (int b; (b = next.fetch_add(1)) < kBins;) {
+        const std::vector<int64_t> &ids = bins[b];
+        std::vector<PairIn> sub(ids.size());
+        L.seq_base.resize(2 * ids.size());
+        for (size_t k = 0; k < ids.size(); ++k) {
+          sub[k] = pairs[ids[k]];
+          L.seq_base[2 * k] = C.seq_base[2 * ids[k]];
+          L.seq_base[2 * k + 1] = C.seq_base[2 * ids[k] + 1];
+        }
+        L.arena = C.arena;
+        L.d_seqbase.ensure(L, sizeof(int64_t) * L.seq_base.size() + 8);
+        DCNS_CK(cudaMemcpyAsync(L.d_seqbase.p, L.seq_base.data(), sizeof(int64_t) * L.seq_base.size(),
+                                cudaMemcpyHostToDevice, L.st));
+        L.seqbase_dev = L.d_seqbase.as<int64_t>();
+        L.stats = dcns_stats{};
+        std::vector<std::vector<FragOut>> so(ids.size());
+        align_single(L, sub, P, mode, so);
+        for (size_t k = 0; k < ids.size(); ++k) out[ids[k]] = std::move(so[k]);
+        add_stats(st[l], L.stats);
+      }
+    } catch (const Error &e) {
+      errs[l] = e.what();
+      codes[l] = e.code;
+    } catch (const std::exception &e) {
+      errs[l] = e.what();
+      codes[l] = DCNS_ERR_DEVICE;
+    }
+  };
+  std::vector<std::thread> th;
+  for (int l = 1; l < nl; ++l) th.emplace_back(worker, l);
+  worker(0);
+  for (auto &t : th) t.join();
+  for (int l = 0; l < nl; ++l)
+    if (codes[l]) throw Error(codes[l], errs[l]);
+  for (int l = 0; l < nl; ++l) add_stats(C.stats, st[l]);
+}
+
+void align_single(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
+                  std::vector<std::vector<FragOut>> &out) {
   const int64_t np = (int64_t)pairs.size();
   const bool one_gap = mode == DCNS_MODE_ONE_GAP;
   std::vector<std::vector<Seed4>> linked;
   scan_and_link(C, pairs, P, one_gap, linked);
   std::vector<std::vector<XSeedOut>> xr;
-  extend_seeds(C, pairs, P, linked, one_gap, xr);
+  std::vector<uint32_t> cig_flat;
+  extend_seeds(C, pairs, P, linked, one_gap, xr, cig_flat);
   if (one_gap) {
     parallel_for(np, [&](int64_t p) {
       const double L1 = double(pairs[p].n1), L2 = double(pairs[p].n2);
@@ -1196,7 +1343,9 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
         evalue(P, L1, L2, x.score, ev, pv);
         if (!(pv < P.pvalue)) continue;
         FragOut f{(int64_t)x.start1 + 1, (int64_t)x.end1 + 1, (int64_t)x.start2 + 1, (int64_t)x.end2 + 1,
-                  (int64_t)(uint32_t)x.score, std::move(x.cigar), pv, ev};
+                  (int64_t)(uint32_t)x.score,
+                  std::vector<uint32_t>(cig_flat.begin() + x.cig_off, cig_flat.begin() + x.cig_off + x.cig_len), pv,
+                  ev};
         bool fresh = true;
         for (FragOut &g : fr) {  // :503-517: compares 0-based new ends with stored 1-based ones
           if (g.s1 == f.s1 && g.s2 == f.s2) {
@@ -1253,7 +1402,7 @@ void smith_waterman_batch(Context &C, const std::vector<PairIn> &tasks, const Pa
     T.tw = tasks[k].n2;
     T.lo = 0;
     T.hi = tasks[k].n1;
-    S.more.push_back(T);
+    S.tasks.push_back(T);
   }
   Params Q = P;
   Q.min_score = INT_MAX;  // maxima and positions only: no reverse scans
@@ -1285,7 +1434,11 @@ void xextend_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P
     x.w = P.w;
     X[k] = x;
   }
-  run_xdrop(C, X, P, want_cigar, want_cigar ? &cigars : nullptr);
+  std::vector<uint32_t> flat;
+  std::vector<int64_t> hoff;
+  run_xdrop(C, X, P, want_cigar, want_cigar ? &flat : nullptr, want_cigar ? &hoff : nullptr);
+  if (want_cigar)
+    for (int64_t k = 0; k < n; ++k) cigars[k].assign(flat.begin() + hoff[k], flat.begin() + hoff[k] + X[k].ncig);
   for (int64_t k = 0; k < n; ++k) {
     out[6 * k + 0] = X[k].score;
     out[6 * k + 1] = X[k].end1 - 1;
@@ -1353,7 +1506,7 @@ void sliding_window(Context &C, const int8_t *const *seqs, const int32_t *lens, 
       T.tw = tw_of[k];
       T.lo = 0;
       T.hi = lens[i];
-      S.more.push_back(T);
+      S.tasks.push_back(T);
     }
   Params Q = P;
   Q.min_score = INT_MAX;

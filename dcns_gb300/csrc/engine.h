@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <set>
 #include <stdexcept>
 #include <string>
@@ -102,8 +103,18 @@ struct Context {
   Arena arena{};
   const int64_t *seqbase_dev = nullptr;
 
+  // Large batches are split into bins run on `lanes` (each its own stream and buffers, sharing the arena), so one
+  // bin's host-side replay and linking overlap another bin's kernels.
+  std::vector<std::unique_ptr<Context>> lanes;
+  // DCNS_LANES / DCNS_BINS in the environment override the defaults at context creation.
+  bool is_lane = false;
+  int max_lanes = 2;
+  int bins = 4;
+
   ~Context();
 };
+
+void init_context(Context &C, int device, size_t budget);
 
 Params to_params(const dcns_params *p);
 void validate(const Params &P);

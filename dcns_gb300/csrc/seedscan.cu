@@ -85,9 +85,46 @@ __device__ __forceinline__ int min_above(int cur, int a, int b, int c, int d, in
   return m;
 }
 
-template <int W>
-__global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ tiles, int ntiles, Arena ar, int open,
-                                                   int ext, int match, int mismatch,
+// Level-0 tile t, derived from the per-pair table (no tile array in memory).
+__device__ __forceinline__ ScanTile l0_tile(const L0Desc &D, int64_t t) {
+  int lo = 0, hi = D.npairs - 1;
+  while (lo < hi) {  // last pair with tile_begin <= t
+    const int mid = (lo + hi + 1) >> 1;
+    if (D.pairs[mid].tile_begin <= t)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const L0Pair P = D.pairs[lo];
+  const int64_t lt = t - P.tile_begin;
+  const int duo = (int)(lt / P.nch), ch = (int)(lt % P.nch);
+  ScanTile tl;
+  tl.ref_base = P.ref_base;
+  tl.qry_base = P.qry_base;
+  for (int h = 0; h < 2; ++h) {
+    const int w = 2 * duo + h;
+    const bool on = w < P.nfast;
+    const int s2 = w * D.step;
+    tl.s2[h] = on ? s2 : 0;
+    tl.tw[h] = on ? min(D.window, P.n2 - s2) : 0;
+    tl.lo[h] = 0;
+    tl.hi[h] = P.n1;
+    tl.task[h] = on ? (int32_t)(P.wstart + w) : -1;
+  }
+  if (P.nch == 1) {
+    tl.row_begin = 0, tl.cnt_begin = 0, tl.row_end = P.n1;
+  } else {
+    const int c0 = ch * D.chunk;
+    tl.cnt_begin = c0;
+    tl.row_end = min(P.n1, c0 + D.chunk);
+    tl.row_begin = c0 == 0 ? 0 : max(0, c0 - D.warm);
+  }
+  return tl;
+}
+
+template <int W, bool L0>
+__global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ tiles, L0Desc l0, int64_t ntiles,
+                                                   Arena ar, int open, int ext, int match, int mismatch,
                                                    unsigned long long *__restrict__ keys, int *__restrict__ counter) {
   // Score table per reference symbol (index = 2-bit code | N << 2): bytes 0..4 = s(ref, read code 0..4) - open,
   // byte 5 = 0xC0 and byte 6 = 0x00, which the padding selector (6, 5) turns into the lane value -16384.
@@ -114,7 +151,7 @@ __global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ 
   for (;;) {
     const int t = atomicAdd(counter, 1);
     if (t >= ntiles) break;
-    const ScanTile tl = tiles[t];
+    const ScanTile tl = L0 ? l0_tile(l0, t) : tiles[t];
 
     // Registers hold G = H + open (not H): then the diagonal term H + s is G + (s - open) from the table, the
     // horizontal candidate H + open is G itself, and H + open = max(F + open, Hpre + open) is one fused op.
@@ -231,8 +268,15 @@ __global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ 
 void launch_scan(const ScanTile *tiles, int ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
                  int grid, cudaStream_t st) {
   if (ntiles <= 0) return;
-  scan_kernel<kScanW><<<grid, 128, 0, st>>>(tiles, ntiles, ar, p.open1, p.ext1, p.match, p.mismatch, keys,
-                                            work_counter);
+  scan_kernel<kScanW, false><<<grid, 128, 0, st>>>(tiles, L0Desc{}, ntiles, ar, p.open1, p.ext1, p.match, p.mismatch,
+                                                   keys, work_counter);
+}
+
+void launch_scan_l0(L0Desc d, int64_t ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
+                    int grid, cudaStream_t st) {
+  if (ntiles <= 0) return;
+  scan_kernel<kScanW, true><<<grid, 128, 0, st>>>(nullptr, d, ntiles, ar, p.open1, p.ext1, p.match, p.mismatch, keys,
+                                                  work_counter);
 }
 
 // ------------------------------------------------------------------ generic int32 Smith-Waterman (one thread)
@@ -360,6 +404,106 @@ __global__ void reverse_kernel(ScanTask *__restrict__ tasks, int first, int n,
   T.start2 = end2 - bj;
 }
 
+// ------------------------------------------------------------------ level-0 selection
+// count -> scan -> emit: the windows whose maximum reached min_score, compacted in task order, each with its reverse
+// re-scan.  Only these records travel to the host.
+constexpr int kSelBlock = 256;
+
+__global__ void l0_count_kernel(const unsigned long long *__restrict__ keys, int64_t n0, int min_score,
+                                int *__restrict__ block_cnt) {
+  const int64_t t = (int64_t)blockIdx.x * kSelBlock + threadIdx.x;
+  int f = 0;
+  if (t < n0) f = (int)(keys[t] >> 40) >= min_score;
+  const int c = __syncthreads_count(f);
+  if (threadIdx.x == 0) block_cnt[blockIdx.x] = c;
+}
+
+// Exclusive scan of the block counts in place (one block); the total goes to *count.
+__global__ void l0_scan_kernel(int *__restrict__ block_cnt, int nb, int *__restrict__ count) {
+  __shared__ int warp_sums[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const int v = i < nb ? block_cnt[i] : 0;
+    int x = v;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int ws = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+      for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, ws, d);
+        if (lane >= d) ws += y;
+      }
+      warp_sums[lane] = ws;
+    }
+    __syncthreads();
+    const int incl = x + (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
+    if (i < nb) block_cnt[i] = incl - v;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *count = carry;
+}
+
+__global__ void l0_emit_kernel(const unsigned long long *__restrict__ keys, int64_t n0,
+                               const int *__restrict__ block_off, const int64_t *__restrict__ wstart,
+                               const int2 *__restrict__ plen, int np, const int64_t *__restrict__ seq_base, Arena ar,
+                               Params P, L0Rec *__restrict__ out) {
+  __shared__ int warp_cnt[kSelBlock / 32];
+  const int64_t t = (int64_t)blockIdx.x * kSelBlock + threadIdx.x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned long long key = 0;
+  int score = 0, row = -1, col = -1;
+  if (t < n0) key = keys[t];
+  if (key) scan_unkey(key, score, row, col);
+  const bool f = t < n0 && score >= P.min_score;
+  const unsigned m = __ballot_sync(0xFFFFFFFFu, f);
+  if (lane == 0) warp_cnt[wid] = __popc(m);
+  __syncthreads();
+  if (!f) return;
+  int pos = block_off[blockIdx.x] + __popc(m & ((1u << lane) - 1));
+  for (int k = 0; k < wid; ++k) pos += warp_cnt[k];
+  int lo = 0, hi = np - 1;  // the pair owning task t: last wstart <= t
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (wstart[mid] <= t)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const int p = lo;
+  const int s2 = (int)(t - wstart[p]) * P.step;
+  const int tw = min(P.window, plen[p].y - s2);
+  const int lim = tw + P.window;
+  const int e1 = min(row + 1, lim), e2 = min(col + 1, lim);
+  const int64_t b1 = seq_base[2 * p], b2 = seq_base[2 * p + 1];
+  const int end1 = row, end2 = s2 + col;
+  int32_t H[kRevMax + 1], Hp[kRevMax + 1], E[kRevMax + 1];
+  int best, bi, bj;
+  sw_one([&](int i) { return 4 - base_code(ar, b1 + end1 - i); }, e1,
+         [&](int q) { return 4 - base_code(ar, b2 + end2 - q); }, e2, P.open1, P.ext1, P.match, P.mismatch,
+         striped_for(e1, e2, P.open1, P.ext1, P.match), H, Hp, E, best, bi, bj);
+  out[pos] = L0Rec{(int32_t)t, score, end1, end2, end1 - bi, end2 - bj};
+}
+
+void launch_l0_select(const unsigned long long *keys, int64_t n0, const int64_t *wstart, const int2 *plen, int np,
+                      const int64_t *seq_base, Arena ar, Params p, int *scratch, int *count, L0Rec *out,
+                      cudaStream_t st) {
+  if (n0 <= 0) return;
+  const int nb = (int)((n0 + kSelBlock - 1) / kSelBlock);
+  l0_count_kernel<<<nb, kSelBlock, 0, st>>>(keys, n0, p.min_score, scratch);
+  l0_scan_kernel<<<1, 1024, 0, st>>>(scratch, nb, count);
+  l0_emit_kernel<<<nb, kSelBlock, 0, st>>>(keys, n0, scratch, wstart, plen, np, seq_base, ar, p, out);
+}
+
 void launch_reverse(ScanTask *tasks, int first, int n, const unsigned long long *keys, const int64_t *pair_base,
                     const int32_t *pair_len, Arena ar, Params p, cudaStream_t st) {
   (void)pair_len;
@@ -373,7 +517,7 @@ namespace dcns {
 // Resident blocks per SM of the fast scan kernel at 128 threads (sizes the persistent grid).
 int scan_occupancy_impl() {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, scan_kernel<kScanW>, 128, 0) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, scan_kernel<kScanW, true>, 128, 0) != cudaSuccess) {
     (void)cudaGetLastError();
     nb = 1;
   }

@@ -39,6 +39,19 @@ __device__ void xdrop_pass(XTask &T, const Arena &ar, const Params &P, uint32_t 
   const int wpr = xd_words_per_row(w);
   int score = 0, e1 = 0, e2 = 0, rows = 0;
   T.status = 0;
+  // Register path: the query codes under the band, 4 bits per band cell k (column j = i - w + k), shifted one cell
+  // per row, so each row loads one new code instead of one per cell.
+  constexpr int NQ = WC > 0 ? (2 * WC + 1 + 15) / 16 : 1;
+  uint64_t qw[NQ];
+  if constexpr (WC > 0) {
+#pragma unroll
+    for (int u = 0; u < NQ; ++u) qw[u] = 0;
+#pragma unroll
+    for (int k = 0; k < 2 * WC + 1; ++k) {
+      const int j = 1 - w + k;
+      if (k < nk && j >= 1 && j <= n2) qw[k >> 4] |= (uint64_t)s2.at(ar, j - 1) << (4 * (k & 15));
+    }
+  }
   for (int i = 1; i <= n1; ++i) {
     const int c0 = max(i - w, 1), c1 = min(i + w, n2);
     if (T.want_codes && (int64_t)i * wpr > T.tb_cap) {
@@ -51,13 +64,13 @@ __device__ void xdrop_pass(XTask &T, const Arena &ar, const Params &P, uint32_t 
     uint32_t cw = 0;
     int kw = 0;
     uint32_t *row_codes = tb + T.tb_off + (int64_t)(i - 1) * wpr;
-    auto cell = [&](int32_t *Mv, int32_t *Fv, int k) {
+    auto cell = [&](int32_t *Mv, int32_t *Fv, int k, int cj) {
       const int j = i - w + k;
       uint32_t nib = 0xFu;
       if (j >= c0 && j <= c1) {
         const int32_t diag = (j == 1) ? (i == 1 ? 0 : kOut) : Mv[k];
         const int32_t fin = (j == c1) ? kOut : Fv[k + 1];
-        int32_t v = score_of(ci, s2.at(ar, j - 1), P.match, P.mismatch) + diag;
+        int32_t v = score_of(ci, cj, P.match, P.mismatch) + diag;
         uint32_t d = v > fin ? 0u : 1u;
         if (!(v > fin)) v = fin;
         if (!(v > e)) {
@@ -89,9 +102,22 @@ __device__ void xdrop_pass(XTask &T, const Arena &ar, const Params &P, uint32_t 
     if constexpr (WC > 0) {
 #pragma unroll
       for (int k = 0; k < 2 * WC + 1; ++k)
-        if (k < nk) cell(Mr, Fr, k);
+        if (k < nk) cell(Mr, Fr, k, (int)((qw[k >> 4] >> (4 * (k & 15))) & 15u));
+      // next row's band starts one column to the right: drop cell 0, append column (i + 1) + w
+#pragma unroll
+      for (int u = 0; u < NQ; ++u) qw[u] = (qw[u] >> 4) | (u + 1 < NQ ? qw[u + 1] << 60 : 0ull);
+      const int jn = i + 1 + w;
+      if (jn <= n2) {
+        const int kl = nk - 1;
+#pragma unroll
+        for (int u = 0; u < NQ; ++u)
+          if (u == (kl >> 4)) qw[u] |= (uint64_t)s2.at(ar, jn - 1) << (4 * (kl & 15));
+      }
     } else {
-      for (int k = 0; k < nk; ++k) cell(M, F, k);
+      for (int k = 0; k < nk; ++k) {
+        const int j = i - w + k;
+        cell(M, F, k, (j >= 1 && j <= n2) ? s2.at(ar, j - 1) : 0);
+      }
     }
     rows = i;
     if (bestj != n2 && bestj != 1 && (bestj == c0 || bestj == c1)) {

@@ -275,3 +275,18 @@ def test_semiglobal_multiwarp_vs_oracle(eng, oracle):
                 exp = oracle.semiglobal(a, b, cigar=cig, bandwidth=bw, zdrop=zd, open2=o2, ext2=e2)
                 assert tuple(int(v) for v in out[k, :3]) == (exp["score"], exp["end1"], exp["end2"]), (k, bw, zd)
                 assert cigars[k] == exp["cigar"], (k, bw, zd, cig)
+
+
+def test_binned_two_lane_batch_vs_oracle(eng, oracle):
+    # 4200 pairs take the path that splits a batch into bins run on two lanes (batches of at least 4096 pairs)
+    rng = np.random.default_rng(4096)
+    pairs = []
+    for _ in range(4200):
+        a, b = W.planted_pair(rng, int(rng.integers(150, 700)), int(rng.integers(150, 700)), int(rng.integers(0, 4)),
+                              30, 120, 0.7, 0.95, 0.01, 0.1)
+        pairs.append((W.prepare(a), W.prepare(b)))
+    exp = _oracle_many(oracle, pairs, False)
+    got = eng.align_pairs(pairs, 1)
+    assert len(got) == len(pairs)
+    for i in range(len(pairs)):
+        assert_same_fragments(got[i], exp[i], i)
