@@ -105,7 +105,8 @@ class Stats(C.Structure):
                [(n, C.c_double) for n in ("ms_upload", "ms_scan", "ms_replay", "ms_xdrop", "ms_semiglobal",
                                           "ms_download", "ms_total", "ms_scan_kernel", "ms_scan_prep",
                                           "ms_scan_xfer", "ms_link")] + \
-               [("scan_launches", C.c_int32), ("kernel_launches", C.c_int32)]
+               [("scan_launches", C.c_int32), ("kernel_launches", C.c_int32), ("scan_rounds", C.c_int32),
+                ("xdrop_rounds", C.c_int32), ("ms_xdrop_kernel", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -199,15 +200,39 @@ def _codes(a):
     return a
 
 
+_PAIR_DT = np.dtype({"names": ["seq1", "len1", "seq2", "len2"], "formats": ["<u8", "<i4", "<u8", "<i4"],
+                     "offsets": [Pair.seq1.offset, Pair.len1.offset, Pair.seq2.offset, Pair.len2.offset],
+                     "itemsize": C.sizeof(Pair)})
+
+
 def _pairs(pairs):
-    keep = [(_codes(a), _codes(b)) for a, b in pairs]
-    arr = (Pair * max(1, len(keep)))()
-    for k, (a, b) in enumerate(keep):
-        arr[k].seq1 = a.ctypes.data_as(_I8P)
-        arr[k].len1 = len(a)
-        arr[k].seq2 = b.ctypes.data_as(_I8P)
-        arr[k].len2 = len(b)
-    return arr, keep
+    """dcns_pair array pointing at the callers' sequences (contiguous int8 views; copies only where a sequence is not
+    already one).  Returns (array, keep-alive object whose len() is the number of pairs)."""
+    n = len(pairs)
+    if n == 0:
+        return (Pair * 1)(), _Keep(0, ())
+    seqs = [_codes(x).reshape(-1) for ab in pairs for x in ab]
+    if len(seqs) != 2 * n:
+        raise ValueError("every pair must hold exactly two sequences")
+    ptr = np.fromiter((x.ctypes.data for x in seqs), np.uint64, 2 * n)
+    lens = np.fromiter((x.shape[0] for x in seqs), np.int64, 2 * n)
+    sa = np.zeros(n, _PAIR_DT)
+    sa["seq1"], sa["seq2"] = ptr[0::2], ptr[1::2]
+    sa["len1"], sa["len2"] = lens[0::2], lens[1::2]
+    arr = (Pair * n).from_buffer(sa)
+    return arr, _Keep(n, (seqs, sa))
+
+
+class _Keep(tuple):
+    """Keeps the concatenated sequences alive; len() is the number of pairs."""
+
+    def __new__(cls, n, objs):
+        t = super().__new__(cls, objs)
+        t.n = n
+        return t
+
+    def __len__(self):
+        return self.n
 
 
 class FragmentList:
@@ -306,6 +331,22 @@ class Engine:
         finally:
             self.lib.dcns_results_free(res)
 
+    def prepare(self, pairs):
+        """The dcns_pair table of a batch of host sequences (pointers to them, no copy), for align_prepared: the
+        form a C or C++ caller already holds, so timing align_prepared times the C call itself."""
+        return _pairs(pairs)
+
+    def align_prepared(self, prepared, mode=MODE_ONE_GAP, **kw):
+        """align_pairs on a prepare()d table: the sequences are read from host memory by dcns_align_pairs."""
+        arr, keep = prepared
+        p = params(**kw)
+        res = C.POINTER(Results)()
+        self._check(self.lib.dcns_align_pairs(self.h, arr, len(keep), C.byref(p), mode, C.byref(res)))
+        try:
+            return _unpack(res)
+        finally:
+            self.lib.dcns_results_free(res)
+
     def upload(self, pairs):
         """Pack pairs into device memory once; returns a handle for align_resident."""
         arr, keep = _pairs(pairs)
@@ -349,7 +390,7 @@ class Engine:
         arr, keep = _pairs(tasks)
         n = len(keep)
         out = np.zeros((max(1, n), width), np.int32)
-        cap = sum(len(a) + len(b) + 4 for a, b in keep) + 4
+        cap = (int(keep[1]["len1"].sum()) + int(keep[1]["len2"].sum()) + 4 * n + 4) if n else 4
         cig = np.zeros(cap, np.uint32)
         off = np.zeros(n + 1, np.int64)
         self._check(fn(self.h, arr, n, C.byref(params(**kw)), int(want_cigar), out.ctypes.data_as(_I32P),

@@ -48,6 +48,21 @@ struct L0Desc {
   const L0Pair *pairs;
   int32_t npairs, step, window, chunk, warm, pad;
 };
+// A round of tasks (recursion levels, the generic-entry batches), described per duo: two tasks of one pair that share
+// a tile (b = -1 when alone).  Tile t belongs to the duo with tile_begin <= t < next tile_begin and covers row chunk
+// t - tile_begin of the union of the two tasks' row ranges.  Task records are read from the device task array.
+struct RecDuo {
+  int64_t tile_begin;
+  int32_t a, b;
+};
+struct ScanTask;
+struct RecDesc {
+  const RecDuo *duos;
+  const ScanTask *tasks;
+  const int64_t *seqbase;
+  int32_t nduo, chunk, warm, pad;  // chunk = INT32_MAX: one tile per duo
+};
+
 // A level-0 window whose maximum reached min_score, compacted in task order.
 struct L0Rec {
   int32_t task, score, end1, end2, start1, start2;
@@ -108,8 +123,8 @@ struct SgTask {
 // ---- kernel launchers (defined in the .cu files)
 void launch_pack(const int8_t *codes, const int64_t *src_off, const int64_t *dst_base, const int32_t *len, int nseq,
                  uint32_t *pk, uint32_t *nm, cudaStream_t st);
-void launch_scan(const ScanTile *tiles, int ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
-                 int grid, cudaStream_t st);
+void launch_scan(RecDesc d, int64_t ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter, int grid,
+                 cudaStream_t st);
 void launch_scan_l0(L0Desc d, int64_t ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
                     int grid, cudaStream_t st);
 // Compacts the level-0 tasks whose maximum reached min_score (in task order) and runs their reverse scans.

@@ -26,6 +26,9 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <deque>
+#include <condition_variable>
 #include <functional>
 #include <thread>
 
@@ -123,6 +126,7 @@ void init_context(Context &C, int device, size_t budget) {
   C.budget = budget;
   if (const char *e = std::getenv("DCNS_LANES")) C.max_lanes = std::max(1, std::min(8, std::atoi(e)));
   if (const char *e = std::getenv("DCNS_BINS")) C.bins = std::max(1, std::min(64, std::atoi(e)));
+  if (const char *e = std::getenv("DCNS_TRACE")) C.trace = std::atoi(e) != 0;
 }
 
 Params to_params(const dcns_params *p) {
@@ -166,20 +170,114 @@ namespace {
 using Clock = std::chrono::steady_clock;
 double ms_since(Clock::time_point t) { return std::chrono::duration<double, std::milli>(Clock::now() - t).count(); }
 
+// Adds the time since t to phase `name` when tracing; returns now.
+Clock::time_point phase(Context &C, const char *name, Clock::time_point t) {
+  const Clock::time_point now = Clock::now();
+  if (C.trace) {
+    const double ms = std::chrono::duration<double, std::milli>(now - t).count();
+    for (auto &e : C.phases)
+      if (std::strcmp(e.first, name) == 0) {
+        e.second += ms;
+        return now;
+      }
+    C.phases.push_back({name, ms});
+  }
+  return now;
+}
+
+void print_phases(Context &C, const char *what) {
+  if (!C.trace) return;
+  std::string s = std::string("[dcns trace] ") + what;
+  char buf[96];
+  for (auto &e : C.phases) {
+    std::snprintf(buf, sizeof buf, " %s=%.2f", e.first, e.second);
+    s += buf;
+  }
+  std::fprintf(stderr, "%s\n", s.c_str());
+  C.phases.clear();
+}
+
+// Host worker pool for parallel_for: created on first use, shared by every context and lane.  Jobs are served in
+// arrival order; the calling thread works on its own job too, so concurrent callers (two lanes) always progress.
+class HostPool {
+ public:
+  struct Job {
+    const std::function<void(int64_t)> *f;
+    int64_t n;
+    std::atomic<int64_t> next{0}, done{0};
+    std::mutex m;
+    std::condition_variable cv;
+  };
+  static HostPool &get() {
+    static HostPool *pool = new HostPool();  // never destroyed: workers may outlive static destructors
+    return *pool;
+  }
+  int size() const { return (int)th_.size() + 1; }
+  void run(int64_t n, const std::function<void(int64_t)> &f) {
+    auto J = std::make_shared<Job>();
+    J->f = &f;
+    J->n = n;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      q_.push_back(J);
+    }
+    cv_.notify_all();
+    work(*J);
+    {
+      std::unique_lock<std::mutex> lk(J->m);
+      J->cv.wait(lk, [&] { return J->done.load() >= n; });
+    }
+    std::lock_guard<std::mutex> lk(mu_);
+    for (auto it = q_.begin(); it != q_.end(); ++it)
+      if (it->get() == J.get()) {
+        q_.erase(it);
+        break;
+      }
+  }
+  static thread_local bool in_worker;
+
+ private:
+  HostPool() {
+    const int nt = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), 32u);
+    for (int t = 1; t < nt; ++t) th_.emplace_back([this] { loop(); });
+    for (auto &t : th_) t.detach();
+  }
+  static void work(Job &J) {
+    for (int64_t i; (i = J.next.fetch_add(1)) < J.n;) {
+      (*J.f)(i);
+      if (J.done.fetch_add(1) + 1 == J.n) {
+        std::lock_guard<std::mutex> lk(J.m);
+        J.cv.notify_all();
+      }
+    }
+  }
+  void loop() {
+    in_worker = true;
+    for (;;) {
+      std::shared_ptr<Job> J;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return !q_.empty(); });
+        while (!q_.empty() && q_.front()->next.load() >= q_.front()->n) q_.pop_front();
+        if (q_.empty()) continue;
+        J = q_.front();
+      }
+      work(*J);
+    }
+  }
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::deque<std::shared_ptr<Job>> q_;
+  std::vector<std::thread> th_;
+};
+thread_local bool HostPool::in_worker = false;
+
 void parallel_for(int64_t n, const std::function<void(int64_t)> &f) {
-  int nt = (int)std::min<int64_t>(std::max(1u, std::thread::hardware_concurrency()), 32);
-  if (n < 64 || nt <= 1) {
+  if (n < 64 || HostPool::in_worker || std::thread::hardware_concurrency() <= 1) {
     for (int64_t i = 0; i < n; ++i) f(i);
     return;
   }
-  std::atomic<int64_t> next(0);
-  auto work = [&]() {
-    for (int64_t i; (i = next.fetch_add(1)) < n;) f(i);
-  };
-  std::vector<std::thread> pool;
-  for (int t = 1; t < nt; ++t) pool.emplace_back(work);
-  work();
-  for (auto &th : pool) th.join();
+  HostPool::get().run(n, f);
 }
 
 template <class T>
@@ -227,11 +325,19 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
   total_dst += 128;  // lets every kernel read one 64-base block past any sequence end
   C.h_codes.ensure((size_t)std::max<int64_t>(total_src, 1));
   int8_t *stage = C.h_codes.as<int8_t>();
+  // staged copy; the reference indexes its 5x5 score table with the codes, so anything outside 0..4 is rejected
+  std::atomic<bool> badcode(false);
   parallel_for(ns, [&](int64_t s) {
     const PairIn &p = pairs[s / 2];
     const int8_t *src = (s & 1) ? p.s2 : p.s1;
-    if (len[s]) std::memcpy(stage + src_off[s], src, (size_t)len[s]);
+    if (!len[s]) return;
+    int8_t *dst = stage + src_off[s];
+    std::memcpy(dst, src, (size_t)len[s]);
+    uint8_t bad = 0;
+    for (int32_t i = 0; i < len[s]; ++i) bad |= (uint8_t)((uint8_t)dst[i] > 4);
+    if (bad) badcode = true;
   });
+  if (badcode) throw Error(DCNS_ERR_INVALID, "sequence codes must be dCNS codes 0..4 (A C N G T)");
   C.d_codes.ensure(C, (size_t)std::max<int64_t>(total_src, 1));
   C.d_srcoff.ensure(C, sizeof(int64_t) * ns + 8);
   C.d_dstbase.ensure(C, sizeof(int64_t) * ns + 8);
@@ -252,17 +358,6 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
   C.stats.kernel_launches += 1;
   arena.pk = d_pk.as<uint32_t>();
   arena.nm = d_nm.as<uint32_t>();
-  // the reference indexes its 5x5 score table with the codes: anything outside 0..4 is rejected up front
-  std::atomic<bool> badcode(false);
-  parallel_for((total_src + (1 << 20) - 1) >> 20, [&](int64_t b) {
-    const int64_t lo = b << 20, hi = std::min<int64_t>(total_src, lo + (1 << 20));
-    for (int64_t i = lo; i < hi; ++i)
-      if ((uint8_t)stage[i] > 4) {
-        badcode = true;
-        break;
-      }
-  });
-  if (badcode) throw Error(DCNS_ERR_INVALID, "sequence codes must be dCNS codes 0..4 (A C N G T)");
 }
 
 // Uploads into the context's own buffers and makes them the current arena.
@@ -299,21 +394,22 @@ int warmup_rows(const Params &P, int tw) {
 
 // Launches the scan over `tiles` plus the generic kernel over `generic` (device slots), then the reverse scans for
 // recursion tasks [first, first+n) (device slots first - ns ...); downloads those tasks.
-void run_scan_round(Context &C, ScanState &S, const Params &P, int64_t first, int64_t n, const ScanTile *tiles,
-                    int64_t ntiles, const std::vector<int32_t> &generic) {
+void run_scan_round(Context &C, ScanState &S, const Params &P, int64_t first, int64_t n, const RecDuo *duos,
+                    int64_t nduo, int64_t ntiles, int32_t chunk, int warm, const std::vector<int32_t> &generic) {
   auto tx = Clock::now();
   const int64_t d0 = first - S.ns;  // device slot of the first task
   C.d_keys.ensure(C, sizeof(unsigned long long) * (S.size() - S.ns));
   DCNS_CK(cudaMemsetAsync(C.d_keys.as<unsigned long long>() + d0, 0, sizeof(unsigned long long) * n, C.st));
   if (ntiles > 0) {
-    C.d_tiles.ensure(C, sizeof(ScanTile) * ntiles);
+    C.d_tiles.ensure(C, sizeof(RecDuo) * nduo);
     C.d_counter.ensure(C, 64);
-    h2d(C, C.d_tiles, tiles, (size_t)ntiles);
+    h2d(C, C.d_tiles, duos, (size_t)nduo);
     DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int), C.st));
     const int grid = (int)std::min<int64_t>((int64_t)C.nsm * C.scan_blocks_per_sm, (ntiles + 127) / 128);
+    const RecDesc D{C.d_tiles.as<RecDuo>(), C.d_tasks.as<ScanTask>(), C.seqbase_dev, (int32_t)nduo, chunk, warm, 0};
     DCNS_CK(cudaEventRecord(C.ev0, C.st));
-    launch_scan(C.d_tiles.as<ScanTile>(), (int)ntiles, C.arena, P, C.d_keys.as<unsigned long long>(),
-                C.d_counter.as<int>(), grid, C.st);
+    launch_scan(D, ntiles, C.arena, P, C.d_keys.as<unsigned long long>(), C.d_counter.as<int>(), std::max(grid, 1),
+                C.st);
     DCNS_CK(cudaEventRecord(C.ev1, C.st));
     C.stats.scan_launches += 1;
     C.stats.kernel_launches += 1;
@@ -334,6 +430,7 @@ void run_scan_round(Context &C, ScanState &S, const Params &P, int64_t first, in
   C.stats.kernel_launches += 1;
   d2h(C, S.tasks.data() + first, C.d_tasks, (size_t)n, (size_t)d0);
   sync(C);
+  C.stats.scan_rounds += 1;
   C.stats.ms_scan_xfer += ms_since(tx);
   if (ntiles > 0) {
     float ms = 0;
@@ -349,6 +446,7 @@ void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
   if (n <= 0) return;
   S.first_new = S.size();
   auto t0 = Clock::now();
+  auto tp = t0;
   const bool fast_ok = fast_scan_ok(P);
   std::vector<int32_t> fast, generic;  // device slots
   for (int64_t k = first; k < first + n; ++k) {
@@ -360,6 +458,7 @@ void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
     else
       generic.push_back((int32_t)(k - S.ns));
   }
+  tp = phase(C, "sc_classify", tp);
   auto tk = [&](int32_t d) -> const ScanTask & { return S.task(d + S.ns); };
   // Recursion tasks arrive grouped by pair (the replay requests them pair by pair); within a pair, order by row
   // range so that the two halves of a tile cover similar rows.  Pairs' groups are sorted independently.
@@ -374,67 +473,60 @@ void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
       return x.s2 < y.s2;
     });
   });
-  struct Half2 {
-    int32_t a, b;
-  };
-  std::vector<Half2> duo;
+  tp = phase(C, "sc_sort", tp);
+  std::vector<RecDuo> duo;
   for (size_t g = 0; g + 1 < gb.size(); ++g)
-    for (size_t i = gb[g]; i < gb[g + 1]; i += 2) duo.push_back({fast[i], i + 1 < gb[g + 1] ? fast[i + 1] : -1});
+    for (size_t i = gb[g]; i < gb[g + 1]; i += 2)
+      duo.push_back(RecDuo{0, fast[i], i + 1 < gb[g + 1] ? fast[i + 1] : -1});
+  const int64_t nd = (int64_t)duo.size();
+  std::vector<int32_t> drows(nd);
   int64_t total_rows = 0;
-  for (const Half2 &d : duo) {
-    const ScanTask &A = tk(d.a);
+  for (int64_t d = 0; d < nd; ++d) {
+    const ScanTask &A = tk(duo[d].a);
     int lo = A.lo, hi = A.hi;
-    if (d.b >= 0) lo = std::min(lo, tk(d.b).lo), hi = std::max(hi, tk(d.b).hi);
+    if (duo[d].b >= 0) lo = std::min(lo, tk(duo[d].b).lo), hi = std::max(hi, tk(duo[d].b).hi);
+    drows[d] = hi - lo;
     total_rows += hi - lo;
   }
   const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * 128;
   const int64_t want_tiles = 8 * resident;
   const int K = warmup_rows(P, kScanW);
-  int64_t chunk = INT64_MAX;
-  if ((int64_t)duo.size() < want_tiles && K != INT_MAX && total_rows > 0)
-    chunk = std::max<int64_t>(4 * (int64_t)K, (total_rows + want_tiles - 1) / want_tiles);
-  std::vector<ScanTile> tiles;
-  tiles.reserve(duo.size() + 16);
-  for (const Half2 &d : duo) {
-    ScanTile tl{};
-    const ScanTask &A = tk(d.a);
-    tl.ref_base = C.seq_base[2 * A.pair];
-    tl.qry_base = C.seq_base[2 * A.pair + 1];
-    int lo = A.lo, hi = A.hi;
-    tl.s2[0] = A.s2, tl.tw[0] = A.tw, tl.lo[0] = A.lo, tl.hi[0] = A.hi, tl.task[0] = d.a;
-    if (d.b >= 0) {
-      const ScanTask &B = tk(d.b);
-      tl.s2[1] = B.s2, tl.tw[1] = B.tw, tl.lo[1] = B.lo, tl.hi[1] = B.hi, tl.task[1] = d.b;
-      lo = std::min(lo, B.lo);
-      hi = std::max(hi, B.hi);
-    } else {
-      tl.s2[1] = 0, tl.tw[1] = 0, tl.lo[1] = A.lo, tl.hi[1] = A.hi, tl.task[1] = -1;
-    }
-    for (int64_t c0 = lo; c0 < hi; c0 += chunk) {
-      const int64_t c1 = std::min<int64_t>(hi, c0 + chunk);
-      ScanTile t = tl;
-      t.cnt_begin = (int32_t)c0;
-      t.row_end = (int32_t)c1;
-      t.row_begin = (int32_t)std::max<int64_t>(lo, c0 - (c0 == lo ? 0 : K));
-      tiles.push_back(t);
-      if (chunk == INT64_MAX) break;
-    }
-  }
-  // longest tiles first for the work queue: a bucket order by log-length (linear time)
+  int64_t chunk = INT32_MAX;
+  if (nd < want_tiles && K != INT_MAX && total_rows > 0)
+    chunk = std::min<int64_t>(INT32_MAX, std::max<int64_t>(4 * (int64_t)K, (total_rows + want_tiles - 1) / want_tiles));
+  // longest duos first for the work queue: a counting sort by log-length (linear time); tile_begin follows that order
+  std::vector<RecDuo> ord(nd);
   {
-    std::vector<std::vector<ScanTile>> bucket(64);
-    for (const ScanTile &t : tiles) {
-      const int len = std::max(1, t.row_end - t.row_begin);
-      const int b = std::min(63, (int)(4.0 * std::log2((double)len)));
-      bucket[63 - b].push_back(t);
+    std::vector<uint8_t> bk(nd);
+    int64_t cnt[65] = {0};
+    for (int64_t d = 0; d < nd; ++d) {
+      const int b = std::min(63, (int)(4.0 * std::log2((double)std::max(1, drows[d]))));
+      bk[d] = (uint8_t)(63 - b);
+      cnt[bk[d] + 1]++;
     }
-    tiles.clear();
-    for (auto &bk : bucket) tiles.insert(tiles.end(), bk.begin(), bk.end());
+    for (int b = 0; b < 64; ++b) cnt[b + 1] += cnt[b];
+    std::vector<int32_t> rows_of(nd);
+    for (int64_t d = 0; d < nd; ++d) {
+      const int64_t at = cnt[bk[d]]++;
+      ord[at] = duo[d];
+      rows_of[at] = drows[d];
+    }
+    int64_t tb = 0;
+    for (int64_t d = 0; d < nd; ++d) {
+      ord[d].tile_begin = tb;
+      tb += chunk >= INT32_MAX ? 1 : std::max<int64_t>(1, (rows_of[d] + chunk - 1) / chunk);
+    }
+    duo.swap(ord);
+    duo.push_back(RecDuo{tb, -1, -1});  // sentinel: total tile count
   }
+  const int64_t ntiles = duo.back().tile_begin;
+  duo.pop_back();
+  tp = phase(C, "sc_tiles", tp);
   C.stats.ms_scan_prep += ms_since(t0);
   C.d_tasks.ensure(C, sizeof(ScanTask) * (S.size() - S.ns));
   h2d(C, C.d_tasks, S.tasks.data() + first, (size_t)n, (size_t)(first - S.ns));
-  run_scan_round(C, S, P, first, n, tiles.data(), (int64_t)tiles.size(), generic);
+  run_scan_round(C, S, P, first, n, duo.data(), nd, ntiles, (int32_t)chunk, K, generic);
+  tp = phase(C, "sc_round", tp);
   C.stats.ms_scan += ms_since(t0);
   S.left.resize(S.size(), -1);
   S.right.resize(S.size(), -1);
@@ -532,6 +624,7 @@ int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, 
     e.nch = chunk >= INT32_MAX ? 1 : (int32_t)std::max<int64_t>(1, (pairs[p].n1 + chunk - 1) / chunk);
     ntiles += (int64_t)((nfast[p] + 1) / 2) * e.nch;
   }
+  auto tp = phase(C, "l0_table", t0);
   int64_t *wst = reinterpret_cast<int64_t *>(tab + np);
   int2 *plen = reinterpret_cast<int2 *>(wst + np + 1);
   for (int64_t p = 0; p <= np; ++p) wst[p] = wstart[p];
@@ -559,13 +652,16 @@ int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, 
                  C.st);
   DCNS_CK(cudaEventRecord(C.ev1, C.st));
   C.stats.scan_launches += 1;
+  C.stats.scan_rounds += 1;
   C.stats.kernel_launches += 1;
   launch_l0_select(C.d_keys.as<unsigned long long>(), n0, d_wst, d_plen, (int)np, C.seqbase_dev, C.arena, P, d_blk,
                    d_count, C.d_tasks.as<L0Rec>(), C.st);
   C.stats.kernel_launches += 3;
   int nsel = 0;
   DCNS_CK(cudaMemcpyAsync(&nsel, d_count, sizeof(int), cudaMemcpyDeviceToHost, C.st));
+  tp = phase(C, "l0_launch", tp);
   sync(C);
+  tp = phase(C, "l0_sync", tp);
   C.h_tasks.ensure(sizeof(L0Rec) * std::max(nsel, 1));
   L0Rec *rec = C.h_tasks.as<L0Rec>();
   d2h(C, rec, C.d_tasks, (size_t)nsel);
@@ -576,6 +672,7 @@ int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, 
     C.stats.ms_scan_kernel += ms;
   }
   C.stats.ms_scan_xfer += ms_since(tx);
+  tp = phase(C, "l0_d2h", tp);
   auto tb = Clock::now();
   S.tasks.resize(nsel);
   // records are in task order: pair p's records start at the first record with task >= wstart[p]
@@ -611,6 +708,7 @@ int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, 
   S.first_new = nsel;
   S.left.assign(nsel, -1);
   S.right.assign(nsel, -1);
+  phase(C, "l0_records", tp);
   C.stats.ms_scan_prep += ms_since(tb);
   C.stats.ms_scan += ms_since(t0);
   return cells;
@@ -786,6 +884,7 @@ void scan_and_link(Context &C, const std::vector<PairIn> &pairs, const Params &P
       S.right.resize(S.size(), -1);
     }
     C.stats.ms_replay += ms_since(t0);
+    phase(C, "replay", t0);
     if (nreq == 0) break;
     if (round > 100000) throw Error(DCNS_ERR_DEVICE, "seed recursion did not converge");
   }
@@ -857,9 +956,12 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
         words += X[k].tb_cap;
       }
     if (want_codes) C.d_tb.ensure(C, sizeof(uint32_t) * std::max<int64_t>(words, 1));
+    auto tp = phase(C, "xd_prep0", Clock::now());
     C.h_misc.ensure(sizeof(XTask) * m);
     XTask *Xc = C.h_misc.as<XTask>();
-    for (int64_t q = 0; q < m; ++q) Xc[q] = X[pend[q]];
+    parallel_for((m + 4095) / 4096, [&](int64_t b) {
+      for (int64_t q = b * 4096, e = std::min(m, q + 4096); q < e; ++q) Xc[q] = X[pend[q]];
+    });
     h2d(C, C.d_x, Xc, (size_t)m);
     std::vector<int32_t> g10, g20, gw;
     int maxw = 0;
@@ -890,15 +992,27 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
       C.stats.xdrop_passes += (int64_t)g.size();
       off += g.size();
     };
+    tp = phase(C, "xd_prep", tp);
+    DCNS_CK(cudaEventRecord(C.ev0, C.st));
     launch_group(g10, 10);
     launch_group(g20, 20);
     launch_group(gw, 0);
+    DCNS_CK(cudaEventRecord(C.ev1, C.st));
     d2h(C, Xc, C.d_x, (size_t)m);
     sync(C);
+    {
+      float ms = 0;
+      DCNS_CK(cudaEventElapsedTime(&ms, C.ev0, C.ev1));
+      C.stats.ms_xdrop_kernel += ms;
+      C.stats.xdrop_rounds += 1;
+    }
+    tp = phase(C, "xd_launch_sync", tp);
     std::vector<int32_t> next, fin_c;  // fin_c: compact indices of finished passes
+    parallel_for((m + 4095) / 4096, [&](int64_t b) {
+      for (int64_t q = b * 4096, e = std::min(m, q + 4096); q < e; ++q) X[pend[q]] = Xc[q];
+    });
     for (int64_t q = 0; q < m; ++q) {
       const int32_t k = pend[q];
-      X[k] = Xc[q];
       if (Xc[q].status == 1) {
         X[k].w *= 2;  // the reference restarts the whole pass with twice the band (:1272-1276)
         next.push_back(k);
@@ -909,6 +1023,7 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
         fin_c.push_back((int32_t)q);
       }
     }
+    tp = phase(C, "xd_collect", tp);
     if (want_codes && !fin_c.empty()) {
       int64_t cw = 0;
       for (int32_t q : fin_c) {
@@ -926,14 +1041,26 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
       d2h(C, Xc, C.d_x, (size_t)m);
       d2h(C, C.h_out.as<uint32_t>(), C.d_cig, (size_t)cw);
       sync(C);
+      tp = phase(C, "xd_tb_sync", tp);
       const uint32_t *hc = C.h_out.as<uint32_t>();
+      int64_t total = (int64_t)flat->size();
       for (int32_t q : fin_c) {
         const int32_t k = pend[q];
-        X[k] = Xc[q];
-        if (X[k].status == 3) throw Error(DCNS_ERR_DEVICE, "x-drop traceback exceeded its CIGAR slot");
-        (*hoff)[k] = (int64_t)flat->size();
-        flat->insert(flat->end(), hc + X[k].cig_off, hc + X[k].cig_off + X[k].ncig);
+        if (Xc[q].status == 3) throw Error(DCNS_ERR_DEVICE, "x-drop traceback exceeded its CIGAR slot");
+        (*hoff)[k] = total;
+        total += Xc[q].ncig;
       }
+      flat->resize(total);
+      uint32_t *fo = flat->data();
+      const int64_t nf = (int64_t)fin_c.size();
+      parallel_for((nf + 1023) / 1024, [&](int64_t b) {
+        for (int64_t i = b * 1024, e = std::min(nf, i + 1024); i < e; ++i) {
+          const int32_t q = fin_c[i], k = pend[q];
+          X[k] = Xc[q];
+          std::memcpy(fo + (*hoff)[k], hc + Xc[q].cig_off, sizeof(uint32_t) * Xc[q].ncig);
+        }
+      });
+      tp = phase(C, "xd_tb_host", tp);
     }
     pend.swap(next);
   }
@@ -980,7 +1107,9 @@ void extend_seeds(Context &C, const std::vector<PairIn> &pairs, const Params &P,
     }
   }
   C.stats.seeds += (int64_t)F.size();
+  auto tp = phase(C, "xs_build_fwd", Clock::now());
   run_xdrop(C, F, P, false, nullptr, nullptr);
+  tp = phase(C, "xs_run_fwd", tp);
   std::vector<XTask> R;
   std::vector<int32_t> rmap;
   for (size_t k = 0; k < F.size(); ++k) {
@@ -1005,7 +1134,9 @@ void extend_seeds(Context &C, const std::vector<PairIn> &pairs, const Params &P,
     rmap.push_back((int32_t)k);
   }
   std::vector<int64_t> hoff;
+  tp = phase(C, "xs_build_rev", tp);
   run_xdrop(C, R, P, want_cigar, want_cigar ? &cig_flat : nullptr, want_cigar ? &hoff : nullptr);
+  tp = phase(C, "xs_run_rev", tp);
   for (size_t q = 0; q < R.size(); ++q) {
     const XTask &r = R[q];
     const XTask &f = F[rmap[q]];
@@ -1247,7 +1378,8 @@ void add_stats(dcns_stats &a, const dcns_stats &b) {
   a.ms_replay += b.ms_replay, a.ms_xdrop += b.ms_xdrop, a.ms_semiglobal += b.ms_semiglobal;
   a.ms_download += b.ms_download, a.ms_scan_kernel += b.ms_scan_kernel, a.ms_scan_prep += b.ms_scan_prep;
   a.ms_scan_xfer += b.ms_scan_xfer, a.ms_link += b.ms_link, a.scan_launches += b.scan_launches;
-  a.kernel_launches += b.kernel_launches;
+  a.kernel_launches += b.kernel_launches, a.scan_rounds += b.scan_rounds, a.xdrop_rounds += b.xdrop_rounds;
+  a.ms_xdrop_kernel += b.ms_xdrop_kernel;
 }
 
 // Batches large enough to fill the GPU several times over are split into bins of similar work (pairs dealt
@@ -1329,10 +1461,21 @@ void align_single(Context &C, const std::vector<PairIn> &pairs, const Params &P,
   const int64_t np = (int64_t)pairs.size();
   const bool one_gap = mode == DCNS_MODE_ONE_GAP;
   std::vector<std::vector<Seed4>> linked;
+  auto tp = Clock::now();
   scan_and_link(C, pairs, P, one_gap, linked);
+  tp = phase(C, "scan_and_link", tp);
   std::vector<std::vector<XSeedOut>> xr;
   std::vector<uint32_t> cig_flat;
   extend_seeds(C, pairs, P, linked, one_gap, xr, cig_flat);
+  tp = phase(C, "extend_seeds", tp);
+  struct Done {
+    Context &C;
+    Clock::time_point t;
+    ~Done() {
+      phase(C, "fragments", t);
+      print_phases(C, C.is_lane ? "lane" : "call");
+    }
+  } done{C, tp};
   if (one_gap) {
     parallel_for(np, [&](int64_t p) {
       const double L1 = double(pairs[p].n1), L2 = double(pairs[p].n2);

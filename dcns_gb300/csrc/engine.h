@@ -108,6 +108,8 @@ struct Context {
   std::vector<std::unique_ptr<Context>> lanes;
   // DCNS_LANES / DCNS_BINS in the environment override the defaults at context creation.
   bool is_lane = false;
+  bool trace = false;  // DCNS_TRACE=1: per-phase host timings of each align call on stderr
+  std::vector<std::pair<const char *, double>> phases;
   int max_lanes = 2;
   int bins = 4;
 

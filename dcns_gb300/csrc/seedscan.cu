@@ -122,8 +122,42 @@ __device__ __forceinline__ ScanTile l0_tile(const L0Desc &D, int64_t t) {
   return tl;
 }
 
-template <int W, bool L0>
-__global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ tiles, L0Desc l0, int64_t ntiles,
+// Tile t of a duo-described round (RecDesc).
+__device__ __forceinline__ ScanTile rec_tile(const RecDesc &D, int64_t t) {
+  int lo = 0, hi = D.nduo - 1;
+  while (lo < hi) {  // last duo with tile_begin <= t
+    const int mid = (lo + hi + 1) >> 1;
+    if (D.duos[mid].tile_begin <= t)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const RecDuo u = D.duos[lo];
+  const ScanTask A = D.tasks[u.a];
+  ScanTile tl;
+  tl.ref_base = D.seqbase[2 * A.pair];
+  tl.qry_base = D.seqbase[2 * A.pair + 1];
+  tl.s2[0] = A.s2, tl.tw[0] = A.tw, tl.lo[0] = A.lo, tl.hi[0] = A.hi, tl.task[0] = u.a;
+  int r0 = A.lo, r1 = A.hi;
+  if (u.b >= 0) {
+    const ScanTask B = D.tasks[u.b];
+    tl.s2[1] = B.s2, tl.tw[1] = B.tw, tl.lo[1] = B.lo, tl.hi[1] = B.hi, tl.task[1] = u.b;
+    r0 = min(r0, B.lo);
+    r1 = max(r1, B.hi);
+  } else {
+    tl.s2[1] = 0, tl.tw[1] = 0, tl.lo[1] = A.lo, tl.hi[1] = A.hi, tl.task[1] = -1;
+  }
+  const int64_t c = t - u.tile_begin;
+  const int64_t c0 = (int64_t)r0 + c * D.chunk;
+  tl.cnt_begin = (int32_t)c0;
+  tl.row_end = (int32_t)min((int64_t)r1, c0 + D.chunk);
+  tl.row_begin = c == 0 ? r0 : (int32_t)max((int64_t)r0, c0 - D.warm);
+  return tl;
+}
+
+// MODE 1: level-0 tiles from the per-pair table; MODE 2: round tiles from the duo table.
+template <int W, int MODE>
+__global__ void __launch_bounds__(128) scan_kernel(RecDesc rec, L0Desc l0, int64_t ntiles,
                                                    Arena ar, int open, int ext, int match, int mismatch,
                                                    unsigned long long *__restrict__ keys, int *__restrict__ counter) {
   // Score table per reference symbol (index = 2-bit code | N << 2): bytes 0..4 = s(ref, read code 0..4) - open,
@@ -151,7 +185,7 @@ __global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ 
   for (;;) {
     const int t = atomicAdd(counter, 1);
     if (t >= ntiles) break;
-    const ScanTile tl = L0 ? l0_tile(l0, t) : tiles[t];
+    const ScanTile tl = MODE == 1 ? l0_tile(l0, t) : rec_tile(rec, t);
 
     // Registers hold G = H + open (not H): then the diagonal term H + s is G + (s - open) from the table, the
     // horizontal candidate H + open is G itself, and H + open = max(F + open, Hpre + open) is one fused op.
@@ -265,18 +299,18 @@ __global__ void __launch_bounds__(128) scan_kernel(const ScanTile *__restrict__ 
   }
 }
 
-void launch_scan(const ScanTile *tiles, int ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
-                 int grid, cudaStream_t st) {
+void launch_scan(RecDesc d, int64_t ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter, int grid,
+                 cudaStream_t st) {
   if (ntiles <= 0) return;
-  scan_kernel<kScanW, false><<<grid, 128, 0, st>>>(tiles, L0Desc{}, ntiles, ar, p.open1, p.ext1, p.match, p.mismatch,
-                                                   keys, work_counter);
+  scan_kernel<kScanW, 2><<<grid, 128, 0, st>>>(d, L0Desc{}, ntiles, ar, p.open1, p.ext1, p.match, p.mismatch, keys,
+                                               work_counter);
 }
 
 void launch_scan_l0(L0Desc d, int64_t ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
                     int grid, cudaStream_t st) {
   if (ntiles <= 0) return;
-  scan_kernel<kScanW, true><<<grid, 128, 0, st>>>(nullptr, d, ntiles, ar, p.open1, p.ext1, p.match, p.mismatch, keys,
-                                                  work_counter);
+  scan_kernel<kScanW, 1><<<grid, 128, 0, st>>>(RecDesc{}, d, ntiles, ar, p.open1, p.ext1, p.match, p.mismatch, keys,
+                                               work_counter);
 }
 
 // ------------------------------------------------------------------ generic int32 Smith-Waterman (one thread)
@@ -517,7 +551,7 @@ namespace dcns {
 // Resident blocks per SM of the fast scan kernel at 128 threads (sizes the persistent grid).
 int scan_occupancy_impl() {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, scan_kernel<kScanW, true>, 128, 0) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, scan_kernel<kScanW, 1>, 128, 0) != cudaSuccess) {
     (void)cudaGetLastError();
     nb = 1;
   }

@@ -79,6 +79,9 @@ typedef struct {
   double ms_scan_xfer;    /* task/tile/result transfers and the synchronising wait of the scan rounds */
   double ms_link;         /* host: link_seeds */
   int32_t scan_launches, kernel_launches;
+  int32_t scan_rounds;     /* seed-scan launches rounds (level 0 + recursion levels), summed over lanes */
+  int32_t xdrop_rounds;    /* x-drop launch rounds (band restarts), summed over lanes */
+  double ms_xdrop_kernel;  /* device: x-drop pass kernels, CUDA events */
 } dcns_stats;
 
 /* Results of one dcns_align_pairs call; owned by the library until dcns_results_free. */
