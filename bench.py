@@ -295,7 +295,8 @@ def main():
         "stages_ms": {k: round(last_stats[k], 2) for k in ("ms_scan_kernel", "ms_scan_prep", "ms_scan_xfer",
                                                             "ms_replay", "ms_link", "ms_xdrop", "ms_xdrop_kernel",
                                                             "ms_semiglobal", "ms_total")},
-        "rounds": {k: last_stats[k] for k in ("scan_rounds", "xdrop_rounds", "kernel_launches")},
+        "rounds": {k: last_stats[k] for k in ("scan_rounds", "xdrop_rounds", "kernel_launches", "seeds",
+                                              "xdrop_passes", "tasks_scan")},
     }
     line.update(extras)
     print(json.dumps(line), flush=True)

@@ -1383,8 +1383,8 @@ void add_stats(dcns_stats &a, const dcns_stats &b) {
 }
 
 // Batches large enough to fill the GPU several times over are split into bins of similar work (pairs dealt
-// round-robin in decreasing n1*n2), and the bins are run by two lanes: while one lane's host threads replay seed sets
-// and link, the other lane's kernels run.  Results and stats are the per-pair results of the single-lane path.
+// round-robin in decreasing n1*n2), and the bins are run by several lanes: while one lane's host threads replay seed
+// sets and link, the other lanes' kernels run.  Results and stats are the per-pair results of the single-lane path.
 void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
                 std::vector<std::vector<FragOut>> &out) {
   const int64_t np = (int64_t)pairs.size();
