@@ -155,6 +155,7 @@ def _bind(lib):
     lib.dcns_align_pairs.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(Params), C.c_int, P(P(Results))]
     lib.dcns_results_free.argtypes = [P(Results)]
     lib.dcns_last_stats.argtypes = [C.c_void_p, P(Stats)]
+    lib.dcns_ctx_set_lanes.argtypes = [C.c_void_p, C.c_int, C.c_int]
     lib.dcns_smith_waterman_batch.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(Params), _I32P]
     lib.dcns_xextend_batch.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(Params), C.c_int, _I32P, _U32P, C.c_int64,
                                        _I64P]
@@ -313,6 +314,10 @@ class Engine:
     @property
     def stream(self) -> int:
         return int(self.lib.dcns_ctx_stream(self.h) or 0)
+
+    def set_lanes(self, lanes: int, bins: int):
+        """Concurrent lanes and work bins for batches of at least 4096 pairs (results do not depend on them)."""
+        self._check(self.lib.dcns_ctx_set_lanes(self.h, int(lanes), int(bins)))
 
     def last_stats(self) -> dict:
         s = Stats()

@@ -280,6 +280,13 @@ int dcns_measure_scan_roofline(dcns_ctx *ctx, double *gcups) {
   });
 }
 
+int dcns_ctx_set_lanes(dcns_ctx *ctx, int lanes, int bins) {
+  if (!ctx || lanes < 1 || lanes > 8 || bins < 1 || bins > 64) return DCNS_ERR_INVALID;
+  ctx->C.max_lanes = lanes;
+  ctx->C.bins = bins;
+  return DCNS_OK;
+}
+
 int dcns_last_stats(const dcns_ctx *ctx, dcns_stats *out) {
   if (!ctx || !out) return DCNS_ERR_INVALID;
   *out = ctx->C.stats;

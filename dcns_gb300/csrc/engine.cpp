@@ -115,6 +115,7 @@ void init_context(Context &C, int device, size_t budget) {
   C.device = device;
   C.nsm = prop.multiProcessorCount;
   C.scan_blocks_per_sm = scan_occupancy();
+  if (C.scan_blocks_per_sm <= 0) throw Error(DCNS_ERR_DEVICE, "the seed-scan kernel could not be configured");
   DCNS_CK(cudaStreamCreateWithFlags(&C.st, cudaStreamNonBlocking));
   DCNS_CK(cudaEventCreate(&C.ev0));
   DCNS_CK(cudaEventCreate(&C.ev1));

@@ -156,13 +156,22 @@ __device__ __forceinline__ ScanTile rec_tile(const RecDesc &D, int64_t t) {
 }
 
 // MODE 1: level-0 tiles from the per-pair table; MODE 2: round tiles from the duo table.
+constexpr int kScanThreads = 128;
+constexpr int kProfGroups = (kScanW + 3) / 4;  // query columns in groups of four (one 128-bit shared load)
+constexpr int kProfSyms = 5;                   // reference symbols A, C, G, T (2-bit codes 0..3) and N
+constexpr size_t kProfBytes = sizeof(uint4) * kProfSyms * kProfGroups * kScanThreads;
+
 template <int W, int MODE>
-__global__ void __launch_bounds__(128) scan_kernel(RecDesc rec, L0Desc l0, int64_t ntiles,
+__global__ void __launch_bounds__(kScanThreads) scan_kernel(RecDesc rec, L0Desc l0, int64_t ntiles,
                                                    Arena ar, int open, int ext, int match, int mismatch,
                                                    unsigned long long *__restrict__ keys, int *__restrict__ counter) {
   // Score table per reference symbol (index = 2-bit code | N << 2): bytes 0..4 = s(ref, read code 0..4) - open,
   // byte 5 = 0xC0 and byte 6 = 0x00, which the padding selector (6, 5) turns into the lane value -16384.
   __shared__ uint32_t tab[16];
+  // Per-thread query profile of the current tile: prof[(sym * kProfGroups + g) * kScanThreads + thread] holds the
+  // int16x2 score words (s - open, both halves) of columns 4g..4g+3 against reference symbol sym.  Each thread reads
+  // and writes only its own entries.
+  extern __shared__ uint4 prof[];
   if (threadIdx.x < 8) {
     const int idx = threadIdx.x;
     const int c = (idx & 4) ? 2 : ((idx & 3) + ((idx & 3) >> 1));
@@ -179,7 +188,7 @@ __global__ void __launch_bounds__(128) scan_kernel(RecDesc rec, L0Desc l0, int64
     tab[2 * idx + 1] = hi;
   }
   __syncthreads();
-  const uint32_t open2 = pack2(open), ext2 = pack2(ext);
+  const uint32_t open2 = pack2(open), ext2 = pack2(ext), fext2 = pack2(max(ext, open));
   const uint32_t open_lo = open2 & 0xFFFFu, open_hi = open2 & 0xFFFF0000u;
 
   for (;;) {
@@ -189,15 +198,32 @@ __global__ void __launch_bounds__(128) scan_kernel(RecDesc rec, L0Desc l0, int64
 
     // Registers hold G = H + open (not H): then the diagonal term H + s is G + (s - open) from the table, the
     // horizontal candidate H + open is G itself, and H + open = max(F + open, Hpre + open) is one fused op.
-    uint32_t sel[W], G[W], E[W];
+    // Two banks of G alternate between rows (row r reads Ga and writes Gb, row r+1 the reverse), so the previous
+    // row's values stay in place while the new row is written: no register copies in the column loop.
+    uint32_t Ga[W], Gb[W], E[W];
+    {
+      uint32_t sel[4 * kProfGroups];
+#pragma unroll
+      for (int p = 0; p < 4 * kProfGroups; ++p) {
+        const uint32_t ra = p < tl.tw[0] ? (uint32_t)base_code(ar, tl.qry_base + tl.s2[0] + p) : 0u;
+        const uint32_t rb = p < tl.tw[1] ? (uint32_t)base_code(ar, tl.qry_base + tl.s2[1] + p) : 0u;
+        const uint32_t sa = p < tl.tw[0] ? (ra | ((ra | 8u) << 4)) : 0x56u;  // padding column: -16384
+        const uint32_t sb = p < tl.tw[1] ? (rb | ((rb | 8u) << 4)) : 0x56u;
+        sel[p] = sa | (sb << 8);
+      }
+#pragma unroll
+      for (int sym = 0; sym < kProfSyms; ++sym) {
+        const uint32_t T0 = tab[2 * sym], T1 = tab[2 * sym + 1];  // table index sym: 2-bit code, 4 = N
+#pragma unroll
+        for (int g = 0; g < kProfGroups; ++g)
+          prof[(sym * kProfGroups + g) * kScanThreads + threadIdx.x] =
+              make_uint4(prmt(T0, T1, sel[4 * g]), prmt(T0, T1, sel[4 * g + 1]), prmt(T0, T1, sel[4 * g + 2]),
+                         prmt(T0, T1, sel[4 * g + 3]));
+      }
+    }
 #pragma unroll
     for (int p = 0; p < W; ++p) {
-      const uint32_t ra = p < tl.tw[0] ? (uint32_t)base_code(ar, tl.qry_base + tl.s2[0] + p) : 0u;
-      const uint32_t rb = p < tl.tw[1] ? (uint32_t)base_code(ar, tl.qry_base + tl.s2[1] + p) : 0u;
-      const uint32_t sa = p < tl.tw[0] ? (ra | ((ra | 8u) << 4)) : 0x56u;  // padding column: -16384
-      const uint32_t sb = p < tl.tw[1] ? (rb | ((rb | 8u) << 4)) : 0x56u;
-      sel[p] = sa | (sb << 8);
-      G[p] = open2;
+      Ga[p] = open2;
       E[p] = 0;
     }
 
@@ -219,19 +245,20 @@ __global__ void __launch_bounds__(128) scan_kernel(RecDesc rec, L0Desc l0, int64
     uint32_t wcur = __ldg(ar.pk + (rk >> 4)) >> (2u * (uint32_t)(rk & 15));
     uint32_t ncur = __ldg(ar.nm + (rk >> 5)) >> (uint32_t)(rk & 31);
 
-    for (; r < tl.row_end; ++r) {
+    // One reference row: Gi holds row r-1, Go receives row r.
+    auto row = [&](uint32_t(&Gi)[W], uint32_t(&Go)[W]) {
       if (r == nev) {
         if (zr0 == r) {
 #pragma unroll
           for (int p = 0; p < W; ++p) {
-            G[p] = (G[p] & 0xFFFF0000u) | open_lo;
+            Gi[p] = (Gi[p] & 0xFFFF0000u) | open_lo;
             E[p] &= 0xFFFF0000u;
           }
         }
         if (zr1 == r) {
 #pragma unroll
           for (int p = 0; p < W; ++p) {
-            G[p] = (G[p] & 0x0000FFFFu) | open_hi;
+            Gi[p] = (Gi[p] & 0x0000FFFFu) | open_hi;
             E[p] &= 0x0000FFFFu;
           }
         }
@@ -241,26 +268,30 @@ __global__ void __launch_bounds__(128) scan_kernel(RecDesc rec, L0Desc l0, int64
         if (ce1 == r) cmpb = (cmpb & 0x0000FFFFu) | 0x7FFF0000u;
         nev = min_above(r, zr0, zr1, cs0, ce0, cs1, ce1);
       }
-      const int idx = (int)((wcur & 3u) | ((ncur & 1u) << 2));
-      const uint32_t T0 = tab[2 * idx], T1 = tab[2 * idx + 1];
+      const int sym = (ncur & 1u) ? 4 : (int)(wcur & 3u);
+      const uint4 *pr = prof + sym * (kProfGroups * kScanThreads) + threadIdx.x;
       ++rk;
       wcur >>= 2;
       ncur >>= 1;
       if ((rk & 15) == 0) wcur = __ldg(ar.pk + (rk >> 4));
       if ((rk & 31) == 0) ncur = __ldg(ar.nm + (rk >> 5));
 
-      uint32_t gd = open2, F = 0, gl = open2, rmax = open2, gprev = open2;
+      // F of column p is max(F[p-1] + ext, H[p-1] + open) with H[p-1] = max(F[p-1], Hpre[p-1]) (H merged with F
+      // before it feeds the next column), i.e. F[p] = max(F[p-1] + max(ext, open), Hpre[p-1] + open): one add-max
+      // per column on the serial chain, and F[0] = max(ext, open) from the zero boundary.
+      uint32_t gd = open2, F = fext2, rmax = open2, gprev = open2;
+      uint4 q4 = make_uint4(0, 0, 0, 0);
 #pragma unroll
       for (int p = 0; p < W; ++p) {
-        const uint32_t s = prmt(T0, T1, sel[p]);
+        if ((p & 3) == 0) q4 = pr[(p >> 2) * kScanThreads];
+        const uint32_t s = (p & 3) == 0 ? q4.x : (p & 3) == 1 ? q4.y : (p & 3) == 2 ? q4.z : q4.w;
         const uint32_t hp = __viaddmax_s16x2_relu(gd, s, E[p]);  // max(H[i-1][p-1] + s, E, 0)
-        gd = G[p];
+        gd = Gi[p];
         const uint32_t tv = __vadd2(hp, open2);
-        E[p] = __viaddmax_s16x2(E[p], ext2, tv);  // max(E + ext, Hpre + open)
-        F = __viaddmax_s16x2(F, ext2, gl);        // max(F + ext, H[i][p-1] + open)
+        E[p] = __viaddmax_s16x2(E[p], ext2, tv);            // max(E + ext, Hpre + open)
         const uint32_t g = __viaddmax_s16x2(F, open2, tv);  // max(F, Hpre) + open
-        G[p] = g;
-        gl = g;
+        F = __viaddmax_s16x2(F, fext2, tv);                 // F of the next column
+        Go[p] = g;
         if (p & 1)
           rmax = __vimax3_s16x2(rmax, gprev, g);
         else if (p == W - 1)
@@ -275,7 +306,7 @@ __global__ void __launch_bounds__(128) scan_kernel(RecDesc rec, L0Desc l0, int64
           int col = W - 1;
 #pragma unroll
           for (int p = W - 1; p >= 0; --p)
-            if (half_s16(G[p], 0) == v) col = p;
+            if (half_s16(Go[p], 0) == v) col = p;
           best0 = v - open;
           brow0 = r;
           bcol0 = col;
@@ -286,13 +317,19 @@ __global__ void __launch_bounds__(128) scan_kernel(RecDesc rec, L0Desc l0, int64
           int col = W - 1;
 #pragma unroll
           for (int p = W - 1; p >= 0; --p)
-            if (half_s16(G[p], 1) == v) col = p;
+            if (half_s16(Go[p], 1) == v) col = p;
           best1 = v - open;
           brow1 = r;
           bcol1 = col;
           cmpb = (cmpb & 0x0000FFFFu) | ((uint32_t)(uint16_t)v << 16);
         }
       }
+      ++r;
+    };
+    while (r < tl.row_end) {
+      row(Ga, Gb);
+      if (r >= tl.row_end) break;
+      row(Gb, Ga);
     }
     if (tl.task[0] >= 0 && best0 > 0) atomicMax(keys + tl.task[0], scan_key(best0, brow0, bcol0));
     if (tl.task[1] >= 0 && best1 > 0) atomicMax(keys + tl.task[1], scan_key(best1, brow1, bcol1));
@@ -302,15 +339,15 @@ __global__ void __launch_bounds__(128) scan_kernel(RecDesc rec, L0Desc l0, int64
 void launch_scan(RecDesc d, int64_t ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter, int grid,
                  cudaStream_t st) {
   if (ntiles <= 0) return;
-  scan_kernel<kScanW, 2><<<grid, 128, 0, st>>>(d, L0Desc{}, ntiles, ar, p.open1, p.ext1, p.match, p.mismatch, keys,
-                                               work_counter);
+  scan_kernel<kScanW, 2><<<grid, kScanThreads, kProfBytes, st>>>(d, L0Desc{}, ntiles, ar, p.open1, p.ext1, p.match,
+                                                                 p.mismatch, keys, work_counter);
 }
 
 void launch_scan_l0(L0Desc d, int64_t ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
                     int grid, cudaStream_t st) {
   if (ntiles <= 0) return;
-  scan_kernel<kScanW, 1><<<grid, 128, 0, st>>>(RecDesc{}, d, ntiles, ar, p.open1, p.ext1, p.match, p.mismatch, keys,
-                                               work_counter);
+  scan_kernel<kScanW, 1><<<grid, kScanThreads, kProfBytes, st>>>(RecDesc{}, d, ntiles, ar, p.open1, p.ext1, p.match,
+                                                                 p.mismatch, keys, work_counter);
 }
 
 // ------------------------------------------------------------------ generic int32 Smith-Waterman (one thread)
@@ -549,9 +586,19 @@ void launch_reverse(ScanTask *tasks, int first, int n, const unsigned long long 
 
 namespace dcns {
 // Resident blocks per SM of the fast scan kernel at 128 threads (sizes the persistent grid).
+// Opts both scan kernels in to their dynamic shared memory (above the 48 KB default) and returns the resident blocks
+// per SM.  Called once per context before any scan launch.
 int scan_occupancy_impl() {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, scan_kernel<kScanW, 1>, 128, 0) != cudaSuccess) {
+  if (cudaFuncSetAttribute(scan_kernel<kScanW, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kProfBytes) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(scan_kernel<kScanW, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kProfBytes) !=
+          cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, scan_kernel<kScanW, 1>, kScanThreads, kProfBytes) !=
+      cudaSuccess) {
     (void)cudaGetLastError();
     nb = 1;
   }
@@ -561,28 +608,32 @@ int scan_occupancy_impl() {
 
 namespace dcns {
 // ------------------------------------------------------------------ integer-issue roofline probe
-// Runs the scan kernel's per-cell instruction sequence (prmt lookup, fused add-max-relu, E and F updates, fused
-// H merge, row maximum every second column) on 8 independent chains per thread at full occupancy, so the only limit is
-// instruction issue.  Each chain step is one int16x2 cell pair of the scan; the result is an upper bound for the
-// scan's cells per second with exactly its instruction mix.
+// Runs the scan kernel's per-cell instruction sequence (score word from a 128-bit shared-memory profile load per four
+// columns, fused add-max-relu, H + open, E and F updates, fused H merge, row maximum every second column) on 8
+// independent chains per thread at full occupancy, so the only limit is instruction issue.  Each chain step is one
+// int16x2 cell pair of the scan; the result is an upper bound for the scan's cells per second with exactly its
+// instruction mix.
 __global__ void __launch_bounds__(256) issue_probe_kernel(uint32_t *out, int iters, uint32_t seed) {
   constexpr int NC = 8;
-  uint32_t d[NC], e[NC], f[NC], u[NC], rm[NC];
-  const uint32_t T0 = 0xFDFD02FDu ^ seed, T1 = 0x0000FDFDu, open2 = pack2(-4), ext2 = pack2(-2);
-  uint32_t sel = 0x00009810u + (threadIdx.x & 3);
+  __shared__ uint4 pf[4 * 256];
+  for (int g = 0; g < 4; ++g)
+    pf[g * 256 + threadIdx.x] = make_uint4(0xFFFDFFFDu ^ seed, 0x00020002u, 0xFFFDFFFDu, 0xC000C000u ^ (g << 1));
+  uint32_t d[NC], e[NC], f[NC], rm[NC];
+  const uint32_t open2 = pack2(-4), ext2 = pack2(-2);
 #pragma unroll
-  for (int c = 0; c < NC; ++c) d[c] = seed * (c + 1), e[c] = 0, f[c] = 0, u[c] = open2, rm[c] = 0;
+  for (int c = 0; c < NC; ++c) d[c] = seed * (c + 1), e[c] = 0, f[c] = 0, rm[c] = 0;
   for (int it = 0; it < iters; ++it) {
+    uint4 q4 = make_uint4(0, 0, 0, 0);
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-      const uint32_t s = prmt(T0, T1, sel + c);
+      if ((c & 3) == 0) q4 = pf[((it + (c >> 2)) & 3) * 256 + threadIdx.x];
+      const uint32_t s = (c & 3) == 0 ? q4.x : (c & 3) == 1 ? q4.y : (c & 3) == 2 ? q4.z : q4.w;
       const uint32_t hp = __viaddmax_s16x2_relu(d[c], s, e[c]);
       const uint32_t tv = __vadd2(hp, open2);
       e[c] = __viaddmax_s16x2(e[c], ext2, tv);
-      f[c] = __viaddmax_s16x2(f[c], ext2, u[c]);
       const uint32_t g = __viaddmax_s16x2(f[c], open2, tv);
+      f[c] = __viaddmax_s16x2(f[c], ext2, tv);
       if (c & 1) rm[c] = __vimax3_s16x2(rm[c], d[c], g);
-      u[c] = g;
       d[c] = g;
     }
   }

@@ -121,6 +121,12 @@ void dcns_batch_free(dcns_ctx *ctx, dcns_batch *batch);
  * the GCUPS ceiling for that instruction mix at the clock the GPU ran during the probe. */
 int dcns_measure_scan_roofline(dcns_ctx *ctx, double *gcups);
 
+/* Tuning (no counterpart in the reference): batches of at least 4096 pairs are split into `bins` bins of similar
+ * work run by `lanes` concurrent lanes, each with its own stream and buffers, so host-side seed replay of one bin
+ * overlaps kernels of another.  lanes = 1 runs every batch as one piece.  Defaults 4 and 4; the environment variables
+ * DCNS_LANES and DCNS_BINS override them when a context is created.  Results do not depend on either value. */
+int dcns_ctx_set_lanes(dcns_ctx *ctx, int lanes, int bins);
+
 /* Stats of the context's last dcns_align_pairs call. */
 int dcns_last_stats(const dcns_ctx *ctx, dcns_stats *out);
 
