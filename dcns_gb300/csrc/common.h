@@ -126,7 +126,7 @@ void launch_pack(const int8_t *codes, const int64_t *src_off, const int64_t *dst
 void launch_scan(RecDesc d, int64_t ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter, int grid,
                  cudaStream_t st);
 void launch_scan_l0(L0Desc d, int64_t ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
-                    int grid, cudaStream_t st);
+                    int64_t grid, cudaStream_t st);
 // Compacts the level-0 tasks whose maximum reached min_score (in task order) and runs their reverse scans.
 // scratch: >= (n0 / 256 + 2) ints.  Returns nothing; the count is written to *count (device).
 void launch_l0_select(const unsigned long long *keys, int64_t n0, const int64_t *wstart, const int2 *plen, int np,

@@ -97,6 +97,8 @@ Context::~Context() {
   h_tiles.release();
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
+  if (ev_bulk) cudaEventDestroy(ev_bulk);
+  if (st_bulk) cudaStreamDestroy(st_bulk);
   if (st) cudaStreamDestroy(st);
 }
 
@@ -116,7 +118,11 @@ void init_context(Context &C, int device, size_t budget) {
   C.nsm = prop.multiProcessorCount;
   C.scan_blocks_per_sm = scan_occupancy();
   if (C.scan_blocks_per_sm <= 0) throw Error(DCNS_ERR_DEVICE, "the seed-scan kernel could not be configured");
-  DCNS_CK(cudaStreamCreateWithFlags(&C.st, cudaStreamNonBlocking));
+  int prio_lo = 0, prio_hi = 0;
+  DCNS_CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+  DCNS_CK(cudaStreamCreateWithPriority(&C.st, cudaStreamNonBlocking, prio_hi));
+  DCNS_CK(cudaStreamCreateWithPriority(&C.st_bulk, cudaStreamNonBlocking, prio_lo));
+  DCNS_CK(cudaEventCreateWithFlags(&C.ev_bulk, cudaEventDisableTiming));
   DCNS_CK(cudaEventCreate(&C.ev0));
   DCNS_CK(cudaEventCreate(&C.ev1));
   if (budget == 0) {
@@ -127,7 +133,8 @@ void init_context(Context &C, int device, size_t budget) {
   C.budget = budget;
   if (const char *e = std::getenv("DCNS_LANES")) C.max_lanes = std::max(1, std::min(8, std::atoi(e)));
   if (const char *e = std::getenv("DCNS_BINS")) C.bins = std::max(1, std::min(64, std::atoi(e)));
-  if (const char *e = std::getenv("DCNS_TRACE")) C.trace = std::atoi(e) != 0;
+  if (const char *e = std::getenv("DCNS_TRACE")) C.trace = std::atoi(e);
+  if (const char *e = std::getenv("DCNS_BIN_RATIO")) C.bin_ratio = std::max(0.1, std::min(1.0, std::atof(e)));
 }
 
 Params to_params(const dcns_params *p) {
@@ -176,6 +183,10 @@ Clock::time_point phase(Context &C, const char *name, Clock::time_point t) {
   const Clock::time_point now = Clock::now();
   if (C.trace) {
     const double ms = std::chrono::duration<double, std::milli>(now - t).count();
+    if (C.trace >= 2)
+      std::fprintf(stderr, "[dcns tl] lane %d %s %.2f %.2f\n", C.lane_id,
+                   name, std::chrono::duration<double, std::milli>(t - C.call_t0).count(),
+                   std::chrono::duration<double, std::milli>(now - C.call_t0).count());
     for (auto &e : C.phases)
       if (std::strcmp(e.first, name) == 0) {
         e.second += ms;
@@ -569,6 +580,11 @@ int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, 
   S.tasks.clear();
   S.pbeg.assign(np + 1, 0);
   if (!fast_scan_ok(P)) {
+    if (C.l0_turn) {  // no level-0 kernel to order: let the later bins go
+      std::lock_guard<std::mutex> lk(C.l0_turn->mu);
+      C.l0_turn->next = std::max(C.l0_turn->next, C.bin + 1);
+      C.l0_turn->cv.notify_all();
+    }
     // generic level 0: every window is a task the replay walks (those below min_score are skipped there)
     S.tasks.reserve(n0);
     for (int64_t p = 0; p < np; ++p) {
@@ -604,6 +620,7 @@ int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, 
   int64_t chunk = INT32_MAX;
   if (nduo < 8 * resident && K != INT_MAX && total_rows > 0)
     chunk = std::min<int64_t>(INT32_MAX, std::max<int64_t>(4 * (int64_t)K, (total_rows + 8 * resident - 1) / (8 * resident)));
+
   std::vector<int64_t> order(np);
   for (int64_t p = 0; p < np; ++p) order[p] = p;
   std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
@@ -647,11 +664,27 @@ int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, 
   DCNS_CK(cudaMemsetAsync(C.d_keys.p, 0, sizeof(unsigned long long) * n0, C.st));
   DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int) * 2, C.st));
   L0Desc D{C.d_tiles.as<L0Pair>(), (int32_t)np, P.step, P.window, (int32_t)chunk, K, 0};
-  const int grid = (int)std::min<int64_t>((int64_t)C.nsm * C.scan_blocks_per_sm, (ntiles + 127) / 128);
-  DCNS_CK(cudaEventRecord(C.ev0, C.st));
-  launch_scan_l0(D, ntiles, C.arena, P, C.d_keys.as<unsigned long long>(), C.d_counter.as<int>(), std::max(grid, 1),
-                 C.st);
-  DCNS_CK(cudaEventRecord(C.ev1, C.st));
+  // One thread per tile (not a persistent grid): blocks retire as they finish, so the short kernels of other lanes,
+  // on higher-priority streams, are scheduled in between instead of waiting for the whole level-0 scan.
+  const int64_t grid = std::max<int64_t>(1, (ntiles + 127) / 128);
+  cudaStream_t bulk = C.st_bulk;
+  if (C.l0_turn) {  // a bin of a binned call: wait for the earlier bins' level-0 scans to be enqueued
+    std::unique_lock<std::mutex> lk(C.l0_turn->mu);
+    C.l0_turn->cv.wait(lk, [&] { return C.l0_turn->next >= C.bin || C.l0_turn->abort; });
+    if (C.l0_turn->abort) throw Error(DCNS_ERR_DEVICE, "another bin of this call failed");
+    bulk = C.bulk_shared;
+  }
+  DCNS_CK(cudaEventRecord(C.ev_bulk, C.st));
+  DCNS_CK(cudaStreamWaitEvent(bulk, C.ev_bulk, 0));
+  DCNS_CK(cudaEventRecord(C.ev0, bulk));
+  launch_scan_l0(D, ntiles, C.arena, P, C.d_keys.as<unsigned long long>(), C.d_counter.as<int>(), grid, bulk);
+  DCNS_CK(cudaEventRecord(C.ev1, bulk));
+  DCNS_CK(cudaStreamWaitEvent(C.st, C.ev1, 0));
+  if (C.l0_turn) {
+    std::lock_guard<std::mutex> lk(C.l0_turn->mu);
+    C.l0_turn->next = std::max(C.l0_turn->next, C.bin + 1);
+    C.l0_turn->cv.notify_all();
+  }
   C.stats.scan_launches += 1;
   C.stats.scan_rounds += 1;
   C.stats.kernel_launches += 1;
@@ -1338,6 +1371,7 @@ void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, 
     if (p.n1 >= (1 << 24) - 2 || p.n2 >= (1 << 24) - 2) throw Error(DCNS_ERR_INVALID, "sequences must be < 16M bases");
   }
   auto t0 = Clock::now();
+  C.call_t0 = t0;
   C.stats = dcns_stats{};
   out.assign(pairs.size(), {});
   if (pairs.empty()) return;
@@ -1361,6 +1395,7 @@ void align_batch(Context &C, Batch &B, const Params &P, int mode, std::vector<st
   validate(P);
   if (mode != DCNS_MODE_ONE_GAP && mode != DCNS_MODE_TWO_GAP) throw Error(DCNS_ERR_INVALID, "mode must be 1 or 2");
   auto t0 = Clock::now();
+  C.call_t0 = t0;
   C.stats = dcns_stats{};
   out.assign(B.lens.size(), {});
   if (B.lens.empty()) return;
@@ -1390,6 +1425,7 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
                 std::vector<std::vector<FragOut>> &out) {
   const int64_t np = (int64_t)pairs.size();
   const int nl = C.is_lane ? 1 : C.max_lanes;
+  if (C.trace >= 2) std::fprintf(stderr, "[dcns tl] call_start %lld pairs\n", (long long)np);
   const int kBins = std::max(C.bins, nl);
   if (nl < 2 || np < 4096) {
     align_single(C, pairs, P, mode, out);
@@ -1409,10 +1445,33 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
     const int64_t wa = (int64_t)pairs[a].n1 * pairs[a].n2, wb = (int64_t)pairs[b].n1 * pairs[b].n2;
     return wa != wb ? wa > wb : a < b;
   });
+  // bin b's share of the work is proportional to bin_ratio^b: the last bins to finish their level-0 scan have the
+  // least host work left; pairs are dealt in decreasing work to the bin furthest below its share
+  std::vector<double> target(kBins);
+  {
+    double tot = 0, wsum = 0, f = 1;
+    for (int64_t p = 0; p < np; ++p) tot += (double)pairs[p].n1 * pairs[p].n2 + 1;
+    for (int b = 0; b < kBins; ++b, f *= C.bin_ratio) target[b] = f, wsum += f;
+    for (int b = 0; b < kBins; ++b) target[b] *= tot / wsum;
+  }
   std::vector<std::vector<int64_t>> bins(kBins);
-  for (int64_t q = 0; q < np; ++q) bins[q % kBins].push_back(order[q]);
+  for (int64_t q = 0; q < np; ++q) {
+    const int64_t p = order[q];
+    int bb = 0;
+    for (int b = 1; b < kBins; ++b)
+      if (target[b] > target[bb]) bb = b;
+    bins[bb].push_back(p);
+    target[bb] -= (double)pairs[p].n1 * pairs[p].n2 + 1;
+  }
   for (auto &b : bins) std::sort(b.begin(), b.end());  // each bin keeps the caller's pair order
   std::atomic<int> next(0);
+  Context::Turnstile turn;
+  auto pass_turn = [&](int b, bool failed) {
+    std::lock_guard<std::mutex> lk(turn.mu);
+    turn.next = std::max(turn.next, b + 1);
+    if (failed) turn.abort = true;
+    turn.cv.notify_all();
+  };
   std::vector<std::string> errs(nl);
   std::vector<int> codes(nl, 0);
   std::vector<dcns_stats> st(nl, dcns_stats{});
@@ -1421,6 +1480,12 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
     try {
       DCNS_CK(cudaSetDevice(C.device));
       for (int b; (b = next.fetch_add(1)) < kBins;) {
+        struct Pass {  // every bin passes the turnstile, whether or not it reached its level-0 scan
+          decltype(pass_turn) &fn;
+          int b;
+          bool failed = true;
+          ~Pass() { fn(b, failed); }
+        } pass{pass_turn, b};
         const std::vector<int64_t> &ids = bins[b];
         std::vector<PairIn> sub(ids.size());
         L.seq_base.resize(2 * ids.size());
@@ -1435,8 +1500,16 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
                                 cudaMemcpyHostToDevice, L.st));
         L.seqbase_dev = L.d_seqbase.as<int64_t>();
         L.stats = dcns_stats{};
+        L.call_t0 = C.call_t0;
+        L.lane_id = l;
+        L.trace = C.trace;
+        L.l0_turn = &turn;
+        L.bin = b;
+        L.bulk_shared = C.st_bulk;
+        phase(L, "bin_start", Clock::now());
         std::vector<std::vector<FragOut>> so(ids.size());
         align_single(L, sub, P, mode, so);
+        pass.failed = false;
         for (size_t k = 0; k < ids.size(); ++k) out[ids[k]] = std::move(so[k]);
         add_stats(st[l], L.stats);
       }
@@ -1452,6 +1525,7 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
   for (int l = 1; l < nl; ++l) th.emplace_back(worker, l);
   worker(0);
   for (auto &t : th) t.join();
+  for (int l = 0; l < nl; ++l) C.lanes[l]->l0_turn = nullptr;
   for (int l = 0; l < nl; ++l)
     if (codes[l]) throw Error(codes[l], errs[l]);
   for (int l = 0; l < nl; ++l) add_stats(C.stats, st[l]);

@@ -2,7 +2,10 @@
 // C ABI (capi.cpp) exposes.
 #pragma once
 
+#include <chrono>
 #include <cstdint>
+#include <condition_variable>
+#include <mutex>
 #include <memory>
 #include <set>
 #include <stdexcept>
@@ -84,7 +87,9 @@ using SeedSet = std::set<Seed4, SeedLess>;
 
 struct Context {
   int device = 0;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;       // every launch and copy of the context (high priority)
+  cudaStream_t st_bulk = nullptr;  // the level-0 seed scan only (low priority): other lanes' short kernels overtake it
+  cudaEvent_t ev_bulk = nullptr;
   size_t budget = 0, used = 0;
   int nsm = 0, scan_blocks_per_sm = 1;
   std::string err;
@@ -109,7 +114,21 @@ struct Context {
   std::vector<std::unique_ptr<Context>> lanes;
   // DCNS_LANES / DCNS_BINS in the environment override the defaults at context creation.
   bool is_lane = false;
-  bool trace = false;  // DCNS_TRACE=1: per-phase host timings of each align call on stderr
+  double bin_ratio = 0.6;  // bin b holds a share of the work proportional to bin_ratio^b (later bins smaller)
+  // Level-0 turnstile of one binned call: the bins enqueue their level-0 scans on the parent's bulk stream in bin
+  // order, so the scans run one after another and the first bins' host work overlaps the later bins' scans.
+  struct Turnstile {
+    std::mutex mu;
+    std::condition_variable cv;
+    int next = 0;
+    bool abort = false;
+  };
+  Turnstile *l0_turn = nullptr;
+  int bin = -1;
+  cudaStream_t bulk_shared = nullptr;
+  int trace = 0;  // DCNS_TRACE=1: per-phase host timings of each align call on stderr; 2: also a per-lane timeline
+  int lane_id = -1;
+  std::chrono::steady_clock::time_point call_t0;
   std::vector<std::pair<const char *, double>> phases;
   int max_lanes = 4;
   int bins = 4;

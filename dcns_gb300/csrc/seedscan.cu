@@ -344,9 +344,9 @@ void launch_scan(RecDesc d, int64_t ntiles, Arena ar, Params p, unsigned long lo
 }
 
 void launch_scan_l0(L0Desc d, int64_t ntiles, Arena ar, Params p, unsigned long long *keys, int *work_counter,
-                    int grid, cudaStream_t st) {
+                    int64_t grid, cudaStream_t st) {
   if (ntiles <= 0) return;
-  scan_kernel<kScanW, 1><<<grid, kScanThreads, kProfBytes, st>>>(RecDesc{}, d, ntiles, ar, p.open1, p.ext1, p.match,
+  scan_kernel<kScanW, 1><<<(unsigned)grid, kScanThreads, kProfBytes, st>>>(RecDesc{}, d, ntiles, ar, p.open1, p.ext1, p.match,
                                                                  p.mismatch, keys, work_counter);
 }
 
