@@ -95,9 +95,10 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def workload(n_pairs, seed_offset=0):
+def workload(n_pairs, rank=0):
     from dcns_gb300 import workloads as W
-    return W.config2(n_pairs=n_pairs, seed=20261205 + seed_offset)
+    from dcns_gb300.ranks import shard_seed
+    return W.config2(n_pairs=n_pairs, seed=shard_seed(rank))
 
 
 def cells_of(st):
@@ -160,6 +161,7 @@ def main():
 
     import torch
     import dcns_gb300
+    from dcns_gb300 import ranks as R
 
     dist = None
     if world > 1:
@@ -170,7 +172,7 @@ def main():
     eng = dcns_gb300.Engine(local)
     stream = torch.cuda.ExternalStream(eng.stream)
     # each rank aligns its own shard of pairs (weak scaling: no data-path collective)
-    pairs = workload(args.pairs, seed_offset=rank)
+    pairs = workload(args.pairs, rank)
     n = len(pairs)
     h2d_bytes = int(sum(len(a) + len(b) for a, b in pairs))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -201,13 +203,11 @@ def main():
             launches += st["kernel_launches"]
             nfrag = sum(len(f) for f in res)
             last_stats = st
-    tot_ms = sum(ms)
-    if dist:
-        tt = torch.tensor([tot_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        tot_ms = float(tt.item())
-    gcups = world * cells / (tot_ms * 1e-3) / 1e9
-    pairs_s = world * n * args.steps / (tot_ms * 1e-3)
+    dev = "cuda" if dist is not None and dist.get_backend() == "nccl" else "cpu"
+    tot_ms = R.max_over_ranks(sum(ms), dist, dev)  # the slowest rank bounds the step
+    all_cells = R.sum_over_ranks(cells, dist, dev)
+    gcups = all_cells / (tot_ms * 1e-3) / 1e9
+    pairs_s = R.whole_job_rate(n * args.steps, world, tot_ms)
 
     # ---- the seed-scan kernel alone: the lanes of the timed steps run kernels concurrently, so its launch times are
     # taken from single-lane steps (same batch, CUDA events around every scan launch on the context's stream)
@@ -236,11 +236,8 @@ def main():
         e2e_ms.append(t)
         e2e_cells += cells_of(eng.last_stats())
         d2h = sum(len(f) for f in res) * (7 * 8 + 16) + sum(len(x.cigar) for f in res for x in f) * 4
-    e2e_tot = sum(e2e_ms)
-    if dist:
-        tt = torch.tensor([e2e_tot], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_tot = float(tt.item())
+    e2e_tot = R.max_over_ranks(sum(e2e_ms), dist, dev)
+    e2e_all_cells = R.sum_over_ranks(e2e_cells, dist, dev)
 
     if rank != 0:
         dist.barrier() if dist else None
@@ -301,8 +298,8 @@ def main():
         "config": {"workload": WORKLOAD, "pairs": n, "mode": args.mode, "parallelism": f"replicas x{world}",
                    "l2": "flushed (256 MB write) between timed steps"},
         "pairs_per_s": round(pairs_s, 2), "fragments": nfrag,
-        "e2e": {"value": round(world * e2e_cells / (e2e_tot * 1e-3) / 1e9, 3), "unit": "GCUPS",
-                "pairs_per_s": round(world * n * args.steps / (e2e_tot * 1e-3), 2),
+        "e2e": {"value": round(e2e_all_cells / (e2e_tot * 1e-3) / 1e9, 3), "unit": "GCUPS",
+                "pairs_per_s": round(R.whole_job_rate(n * args.steps, world, e2e_tot), 2),
                 "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h},
         "roofline": roofline, "cpu_baseline": cb, "gpu_launches": launches, "clocks": clk.summary(),
         "stages_ms": {k: round(last_stats[k], 2) for k in ("ms_scan_kernel", "ms_scan_prep", "ms_scan_xfer",
