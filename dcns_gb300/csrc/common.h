@@ -103,6 +103,7 @@ struct XTask {
   int32_t iii, jjj, ncig;              // traceback results
   int64_t cig_off;                     // CIGAR slot (uint32 entries) and its capacity
   int32_t cig_cap, pad;
+  int64_t cig_dense;                   // chained form: offset of the CIGAR in the batch's packed CIGAR array
 };
 
 // One 2-piece affine semi-global DP (SemiGlobal_no_avx, impl/sequenceAlignment3.cpp:681-928).
@@ -130,7 +131,7 @@ void launch_scan_l0(L0Desc d, int64_t ntiles, Arena ar, Params p, unsigned long 
 // Compacts the level-0 tasks whose maximum reached min_score (in task order) and runs their reverse scans.
 // scratch: >= (n0 / 256 + 2) ints.  Returns nothing; the count is written to *count (device).
 void launch_l0_select(const unsigned long long *keys, int64_t n0, const int64_t *wstart, const int2 *plen, int np,
-                      const int64_t *seq_base, Arena ar, Params p, int *scratch, int *count, L0Rec *out,
+                      const int64_t *seq_base, Arena ar, Params p, int *scratch, int *count, L0Rec *out, int nsm,
                       cudaStream_t st);
 void launch_scan_generic(const ScanTask *tasks, const int *idx, int n, const int64_t *seq_base, Arena ar, Params p,
                          unsigned long long *keys, int32_t *scratch, int64_t scratch_per_thread, cudaStream_t st);
@@ -139,6 +140,17 @@ void launch_reverse(ScanTask *tasks, int first, int n, const unsigned long long 
 void launch_xdrop(XTask *tasks, const int *idx, int n, Arena ar, Params p, uint32_t *tb, int wcap, int32_t *scratch,
                   int64_t scratch_per_thread, cudaStream_t st);
 void launch_xdrop_traceback(XTask *tasks, const int *idx, int n, const uint32_t *tb, uint32_t *cig, cudaStream_t st);
+// Chained x-drop levels (one launch per band width, work lists and counts in device memory).
+void launch_xdrop_iota(int *list, int n, int *count, cudaStream_t st);
+void launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
+                        int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, Arena ar,
+                        Params p, uint32_t *tb, int w, int n_bound, int nsm, int32_t *scratch, int64_t per_warp,
+                        int warps, cudaStream_t st);
+void launch_xdrop_traceback_all(XTask *tasks, int n, const uint32_t *tb, uint32_t *cig,
+                                unsigned long long *cig_cursor, cudaStream_t st);
+// Packs the CIGARs of every finished task in task order into dense (cig_dense offsets); *total = their words.
+void launch_xdrop_cigar_pack(XTask *tasks, int n, const uint32_t *cig, uint32_t *dense, unsigned long long *total,
+                             cudaStream_t st);
 void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p, uint8_t *tb, void *bnd,
                        int max_n2, int *work_counter, int grid, cudaStream_t st);
 int sg_ctas_per_sm();

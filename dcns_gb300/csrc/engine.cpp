@@ -689,8 +689,8 @@ int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, 
   C.stats.scan_rounds += 1;
   C.stats.kernel_launches += 1;
   launch_l0_select(C.d_keys.as<unsigned long long>(), n0, d_wst, d_plen, (int)np, C.seqbase_dev, C.arena, P, d_blk,
-                   d_count, C.d_tasks.as<L0Rec>(), C.st);
-  C.stats.kernel_launches += 3;
+                   d_count, C.d_tasks.as<L0Rec>(), C.nsm, C.st);
+  C.stats.kernel_launches += 4;
   int nsel = 0;
   DCNS_CK(cudaMemcpyAsync(&nsel, d_count, sizeof(int), cudaMemcpyDeviceToHost, C.st));
   tp = phase(C, "l0_launch", tp);
@@ -958,26 +958,23 @@ int64_t band_cells(int rows, int w, int n2) {
 
 int wpr_of(int w) { return (2 * w + 1 + 7) / 8; }
 
-// Runs the given x-drop passes to completion (band restarts, traceback-slot growth), then their tracebacks when
-// want_codes.  X lives on the host between launches.
-// With want_codes, every pass's CIGAR is appended to *flat and hoff[k] is its offset there (X[k].ncig words).
-void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_codes, std::vector<uint32_t> *flat,
-               std::vector<int64_t> *hoff) {
-  if (X.empty()) return;
-  auto t0 = Clock::now();
+// Runs the passes `subset` of X to completion in host-driven rounds (band restarts, traceback-slot growth), then
+// their tracebacks when want_codes; X lives on the host between launches.  Traceback slots start at the whole pass
+// (full_slots) or at min(n1, 1024) rows.  With want_codes, every finished pass's CIGAR is appended to *flat and
+// (*hoff)[k] is its offset there (X[k].ncig words).
+void run_xdrop_rounds(Context &C, std::vector<XTask> &X, const Params &P, bool want_codes, std::vector<uint32_t> *flat,
+                      std::vector<int64_t> *hoff, const std::vector<int32_t> &subset, bool full_slots) {
+  if (subset.empty()) return;
   const int64_t n = (int64_t)X.size();
   std::vector<int64_t> rows_cap(n, 0);
-  for (int64_t k = 0; k < n; ++k) {
+  for (int32_t k : subset) {
     X[k].want_codes = want_codes ? 1 : 0;
     X[k].status = 0;
     X[k].score = X[k].end1 = X[k].end2 = X[k].rows = 0;
     X[k].iii = X[k].jjj = X[k].ncig = 0;
-    rows_cap[k] = std::min<int64_t>(X[k].n1, 1024);
+    rows_cap[k] = full_slots ? (int64_t)X[k].n1 : std::min<int64_t>(X[k].n1, 1024);
   }
-  if (flat) flat->clear();
-  if (hoff) hoff->assign(n, -1);
-  std::vector<int32_t> pend(n);
-  for (int64_t k = 0; k < n; ++k) pend[k] = (int32_t)k;
+  std::vector<int32_t> pend(subset);
   C.d_x.ensure(C, sizeof(XTask) * n);
   while (!pend.empty()) {
     // Only the pending passes travel: gathered into a compact pinned array, indexed 0..m-1 on the device.
@@ -1098,6 +1095,132 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
     }
     pend.swap(next);
   }
+}
+
+// Runs every pass of X to completion and, with want_codes, its traceback.  All passes start with the same band w0;
+// the level kernels for bands w0, 2w0, 4w0, ... (up to a band that covers every pass, where no restart can occur)
+// are enqueued at once with their work lists in device memory, then one synchronisation.  Passes whose traceback
+// slot was too small (or the arena full) finish in host-driven rounds with whole-pass slots.  With want_codes,
+// every pass's CIGAR is in *flat at (*hoff)[k] (X[k].ncig words), in task order.
+void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_codes, std::vector<uint32_t> *flat,
+               std::vector<int64_t> *hoff) {
+  if (X.empty()) return;
+  auto t0 = Clock::now();
+  const int64_t n = (int64_t)X.size();
+  if (flat) flat->clear();
+  if (hoff) hoff->assign(n, -1);
+  const int w0 = X[0].w;
+  int64_t maxdim = 1, tb_words = 1 << 20, cig_words = 1;
+  bool uniform = w0 >= 1;
+  for (int64_t k = 0; k < n; ++k) {
+    XTask &T = X[k];
+    uniform &= T.w == w0;
+    T.want_codes = want_codes ? 1 : 0;
+    T.status = 0;
+    T.score = T.end1 = T.end2 = T.rows = 0;
+    T.iii = T.jjj = T.ncig = 0;
+    maxdim = std::max<int64_t>(maxdim, std::max(T.n1, T.n2));
+    if (want_codes) {
+      tb_words += 3 * std::min<int64_t>(T.n1, 1024) * wpr_of(w0);
+      cig_words += (int64_t)std::max(T.n1, 0) + std::max(T.n2, 0) + 2;
+    }
+  }
+  auto tp = phase(C, "xc_setup", t0);
+  if (!uniform || n >= INT32_MAX / 4) {
+    std::vector<int32_t> all(n);
+    for (int64_t k = 0; k < n; ++k) all[k] = (int32_t)k;
+    run_xdrop_rounds(C, X, P, want_codes, flat, hoff, all, false);
+  } else {
+    int nlev = 1;
+    while (((int64_t)w0 << (nlev - 1)) < maxdim) ++nlev;
+    // per level: warps of the wide-band kernel and their scratch (2 x (2w + 2) ints per warp, 512 MB at most)
+    std::vector<int> warps(nlev, 0);
+    std::vector<int64_t> per_warp(nlev, 0);
+    int64_t scratch_ints = 1;
+    for (int L = 0; L < nlev; ++L) {
+      const int64_t w = (int64_t)w0 << L;
+      if (w <= 20) continue;
+      per_warp[L] = 2 * (2 * w + 2);
+      const int64_t cap = std::max<int64_t>(32, ((int64_t)512 << 20) / (4 * per_warp[L]));
+      warps[L] = (int)(std::min<int64_t>({n, cap, (int64_t)C.nsm * 64}) + 3) / 4 * 4;  // whole blocks of 4 warps
+      scratch_ints = std::max(scratch_ints, warps[L] * per_warp[L]);
+    }
+    C.d_x.ensure(C, sizeof(XTask) * n);
+    C.d_idx.ensure(C, sizeof(int32_t) * (3 * n + 64));
+    C.d_counter.ensure(C, 64);
+    if (want_codes) {
+      C.d_tb.ensure(C, sizeof(uint32_t) * tb_words);
+      C.d_cig.ensure(C, sizeof(uint32_t) * 2 * cig_words);  // slots, then the packed CIGARs
+    }
+    if (scratch_ints > 1) C.d_scratch.ensure(C, sizeof(int32_t) * scratch_ints);
+    int *lists = C.d_idx.as<int>();
+    int *cnt = lists + 3 * n;  // [0], [1]: the two work-list counts, [2]: retry count
+    unsigned long long *cur = C.d_counter.as<unsigned long long>();  // [0]: traceback arena, [1]: CIGAR arena
+    h2d(C, C.d_x, X.data(), (size_t)n);
+    DCNS_CK(cudaMemsetAsync(cnt, 0, sizeof(int) * 4, C.st));
+    DCNS_CK(cudaMemsetAsync(cur, 0, sizeof(unsigned long long) * 2, C.st));
+    launch_xdrop_iota(lists, (int)n, cnt, C.st);
+    DCNS_CK(cudaEventRecord(C.ev0, C.st));
+    int in = 0;
+    for (int L = 0; L < nlev; ++L) {
+      const int out = 1 - in;
+      DCNS_CK(cudaMemsetAsync(cnt + out, 0, sizeof(int), C.st));
+      launch_xdrop_level(C.d_x.as<XTask>(), lists + in * n, cnt + in, lists + out * n, cnt + out, lists + 2 * n,
+                         cnt + 2, cur, want_codes ? tb_words : 0, C.arena, P, C.d_tb.as<uint32_t>(), w0 << L, (int)n,
+                         C.nsm, C.d_scratch.as<int32_t>(), per_warp[L], warps[L], C.st);
+      in = out;
+    }
+    DCNS_CK(cudaEventRecord(C.ev1, C.st));
+    if (want_codes) {
+      launch_xdrop_traceback_all(C.d_x.as<XTask>(), (int)n, C.d_tb.as<uint32_t>(), C.d_cig.as<uint32_t>(), cur + 1,
+                                 C.st);
+      launch_xdrop_cigar_pack(C.d_x.as<XTask>(), (int)n, C.d_cig.as<uint32_t>(), C.d_cig.as<uint32_t>() + cig_words,
+                              cur + 1, C.st);
+    }
+    C.stats.kernel_launches += nlev + 1 + (want_codes ? 3 : 0);
+    C.stats.xdrop_rounds += 1;
+    C.h_misc.ensure(sizeof(int32_t) * (n + 8) + 64);
+    int32_t *hret = C.h_misc.as<int32_t>();  // [0]: leftover count, [1]: retry count, [8..]: retry list
+    unsigned long long hcur[2] = {0, 0};
+    d2h(C, X.data(), C.d_x, (size_t)n);
+    DCNS_CK(cudaMemcpyAsync(hret, cnt + in, sizeof(int), cudaMemcpyDeviceToHost, C.st));
+    DCNS_CK(cudaMemcpyAsync(hret + 1, cnt + 2, sizeof(int), cudaMemcpyDeviceToHost, C.st));
+    DCNS_CK(cudaMemcpyAsync(hret + 8, lists + 2 * n, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, C.st));
+    DCNS_CK(cudaMemcpyAsync(hcur, cur, sizeof(hcur), cudaMemcpyDeviceToHost, C.st));
+    tp = phase(C, "xc_enqueue", tp);
+    sync(C);
+    tp = phase(C, "xc_sync", tp);
+    {
+      float ms = 0;
+      DCNS_CK(cudaEventElapsedTime(&ms, C.ev0, C.ev1));
+      C.stats.ms_xdrop_kernel += ms;
+    }
+    if (hret[0] != 0) throw Error(DCNS_ERR_DEVICE, "x-drop band restarts did not converge");
+    std::vector<int32_t> retry(hret + 8, hret + 8 + hret[1]);
+    std::sort(retry.begin(), retry.end());
+    if (want_codes) {
+      const int64_t cw = (int64_t)hcur[1];  // words of the packed CIGARs
+      flat->resize(cw);
+      if (cw > 0) {
+        DCNS_CK(cudaMemcpyAsync(flat->data(), C.d_cig.as<uint32_t>() + cig_words, sizeof(uint32_t) * cw,
+                                cudaMemcpyDeviceToHost, C.st));
+        sync(C);
+      }
+      for (int64_t k = 0; k < n; ++k) {
+        if (X[k].status == 3) throw Error(DCNS_ERR_DEVICE, "x-drop traceback exceeded its CIGAR slot");
+        if (X[k].status == 0) (*hoff)[k] = X[k].cig_dense;
+      }
+    }
+    for (int64_t k = 0; k < n; ++k) {
+      int lev = 0;
+      while ((w0 << lev) < X[k].w) ++lev;
+      C.stats.xdrop_passes += lev + 1;
+    }
+    tp = phase(C, "xc_cigars", tp);
+    if (C.trace) std::fprintf(stderr, "[dcns trace] x-drop chain: %lld passes, %d levels, %zu retries\n", (long long)n, nlev, retry.size());
+    run_xdrop_rounds(C, X, P, want_codes, flat, hoff, retry, true);
+    tp = phase(C, "xc_retry", tp);
+  }
   for (int64_t k = 0; k < n; ++k) C.stats.cells_xdrop += band_cells(X[k].rows, X[k].w, X[k].n2);
   C.stats.ms_xdrop += ms_since(t0);
 }
@@ -1144,29 +1267,40 @@ void extend_seeds(Context &C, const std::vector<PairIn> &pairs, const Params &P,
   auto tp = phase(C, "xs_build_fwd", Clock::now());
   run_xdrop(C, F, P, false, nullptr, nullptr);
   tp = phase(C, "xs_run_fwd", tp);
-  std::vector<XTask> R;
-  std::vector<int32_t> rmap;
-  for (size_t k = 0; k < F.size(); ++k) {
-    const XTask &f = F[k];
-    XSeedOut &o = res[owner[k].first][owner[k].second];
-    o.ok = false;
-    o.score = f.score;
-    o.cig_off = 0;
-    o.cig_len = 0;
-    if (f.end1 - 1 < 0 || f.end2 - 1 < 0) continue;  // p = 100
-    const int32_t b1 = f.a1 + f.end1 - 1, b2 = f.a2 + f.end2 - 1;
-    XTask r{};
-    r.base1 = f.base1;
-    r.base2 = f.base2;
-    r.a1 = b1;
-    r.a2 = b2;
-    r.n1 = b1 + 1;
-    r.n2 = b2 + 1;
-    r.dir = 1;
-    r.w = P.w;
-    R.push_back(r);
-    rmap.push_back((int32_t)k);
-  }
+  const int64_t nf = (int64_t)F.size();
+  std::vector<int32_t> rslot(nf + 1, 0);  // reverse task of forward pass k (exclusive prefix over kept passes)
+  parallel_for((nf + 4095) / 4096, [&](int64_t b) {
+    for (int64_t k = b * 4096, e = std::min(nf, k + 4096); k < e; ++k) {
+      const XTask &f = F[k];
+      XSeedOut &o = res[owner[k].first][owner[k].second];
+      o.ok = false;
+      o.score = f.score;
+      o.cig_off = 0;
+      o.cig_len = 0;
+      rslot[k + 1] = (f.end1 - 1 < 0 || f.end2 - 1 < 0) ? 0 : 1;  // p = 100 otherwise
+    }
+  });
+  for (int64_t k = 0; k < nf; ++k) rslot[k + 1] += rslot[k];
+  std::vector<XTask> R(rslot[nf]);
+  std::vector<int32_t> rmap(rslot[nf]);
+  parallel_for((nf + 4095) / 4096, [&](int64_t b) {
+    for (int64_t k = b * 4096, e = std::min(nf, k + 4096); k < e; ++k) {
+      if (rslot[k + 1] == rslot[k]) continue;
+      const XTask &f = F[k];
+      const int32_t b1 = f.a1 + f.end1 - 1, b2 = f.a2 + f.end2 - 1;
+      XTask r{};
+      r.base1 = f.base1;
+      r.base2 = f.base2;
+      r.a1 = b1;
+      r.a2 = b2;
+      r.n1 = b1 + 1;
+      r.n2 = b2 + 1;
+      r.dir = 1;
+      r.w = P.w;
+      R[rslot[k]] = r;
+      rmap[rslot[k]] = (int32_t)k;
+    }
+  });
   std::vector<int64_t> hoff;
   tp = phase(C, "xs_build_rev", tp);
   run_xdrop(C, R, P, want_cigar, want_cigar ? &cig_flat : nullptr, want_cigar ? &hoff : nullptr);

@@ -18,6 +18,8 @@
 // and the reported position is the first (i-major, p-minor) cell holding the maximum.
 #include <climits>
 
+#include <algorithm>
+
 #include "device_common.cuh"
 
 namespace dcns {
@@ -525,9 +527,7 @@ __global__ void l0_scan_kernel(int *__restrict__ block_cnt, int nb, int *__restr
 }
 
 __global__ void l0_emit_kernel(const unsigned long long *__restrict__ keys, int64_t n0,
-                               const int *__restrict__ block_off, const int64_t *__restrict__ wstart,
-                               const int2 *__restrict__ plen, int np, const int64_t *__restrict__ seq_base, Arena ar,
-                               Params P, L0Rec *__restrict__ out) {
+                               const int *__restrict__ block_off, int min_score, L0Rec *__restrict__ out) {
   __shared__ int warp_cnt[kSelBlock / 32];
   const int64_t t = (int64_t)blockIdx.x * kSelBlock + threadIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -535,44 +535,65 @@ __global__ void l0_emit_kernel(const unsigned long long *__restrict__ keys, int6
   int score = 0, row = -1, col = -1;
   if (t < n0) key = keys[t];
   if (key) scan_unkey(key, score, row, col);
-  const bool f = t < n0 && score >= P.min_score;
+  const bool f = t < n0 && score >= min_score;
   const unsigned m = __ballot_sync(0xFFFFFFFFu, f);
   if (lane == 0) warp_cnt[wid] = __popc(m);
   __syncthreads();
   if (!f) return;
   int pos = block_off[blockIdx.x] + __popc(m & ((1u << lane) - 1));
   for (int k = 0; k < wid; ++k) pos += warp_cnt[k];
-  int lo = 0, hi = np - 1;  // the pair owning task t: last wstart <= t
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (wstart[mid] <= t)
-      lo = mid;
-    else
-      hi = mid - 1;
+  out[pos] = L0Rec{(int32_t)t, score, row, col, 0, 0};  // end2 holds the window column until the reverse scan
+}
+
+// The reverse re-scan of every compacted level-0 window (one thread each, all busy): the window's start is the
+// argmax of Smith-Waterman on the reverse complements ending at the forward maximum, over at most tw + window
+// cells each way (findSimilarFragmentsForPairedSequence4.cpp:131-201).
+__global__ void __launch_bounds__(128) l0_reverse_kernel(L0Rec *__restrict__ recs, const int *__restrict__ count,
+                                                         const int64_t *__restrict__ wstart,
+                                                         const int2 *__restrict__ plen, int np,
+                                                         const int64_t *__restrict__ seq_base, Arena ar, Params P) {
+  const int n = *count;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    L0Rec r = recs[q];
+    const int64_t t = r.task;
+    int lo = 0, hi = np - 1;  // the pair owning task t: last wstart <= t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (wstart[mid] <= t)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int p = lo;
+    const int s2 = (int)(t - wstart[p]) * P.step;
+    const int tw = min(P.window, plen[p].y - s2);
+    const int lim = tw + P.window;
+    const int row = r.end1, col = r.end2;
+    const int e1 = min(row + 1, lim), e2 = min(col + 1, lim);
+    const int64_t b1 = seq_base[2 * p], b2 = seq_base[2 * p + 1];
+    const int end1 = row, end2 = s2 + col;
+    int32_t H[kRevMax + 1], Hp[kRevMax + 1], E[kRevMax + 1];
+    int best, bi, bj;
+    sw_one([&](int i) { return 4 - base_code(ar, b1 + end1 - i); }, e1,
+           [&](int k) { return 4 - base_code(ar, b2 + end2 - k); }, e2, P.open1, P.ext1, P.match, P.mismatch,
+           striped_for(e1, e2, P.open1, P.ext1, P.match), H, Hp, E, best, bi, bj);
+    r.end2 = end2;
+    r.start1 = end1 - bi;
+    r.start2 = end2 - bj;
+    recs[q] = r;
   }
-  const int p = lo;
-  const int s2 = (int)(t - wstart[p]) * P.step;
-  const int tw = min(P.window, plen[p].y - s2);
-  const int lim = tw + P.window;
-  const int e1 = min(row + 1, lim), e2 = min(col + 1, lim);
-  const int64_t b1 = seq_base[2 * p], b2 = seq_base[2 * p + 1];
-  const int end1 = row, end2 = s2 + col;
-  int32_t H[kRevMax + 1], Hp[kRevMax + 1], E[kRevMax + 1];
-  int best, bi, bj;
-  sw_one([&](int i) { return 4 - base_code(ar, b1 + end1 - i); }, e1,
-         [&](int q) { return 4 - base_code(ar, b2 + end2 - q); }, e2, P.open1, P.ext1, P.match, P.mismatch,
-         striped_for(e1, e2, P.open1, P.ext1, P.match), H, Hp, E, best, bi, bj);
-  out[pos] = L0Rec{(int32_t)t, score, end1, end2, end1 - bi, end2 - bj};
 }
 
 void launch_l0_select(const unsigned long long *keys, int64_t n0, const int64_t *wstart, const int2 *plen, int np,
-                      const int64_t *seq_base, Arena ar, Params p, int *scratch, int *count, L0Rec *out,
+                      const int64_t *seq_base, Arena ar, Params p, int *scratch, int *count, L0Rec *out, int nsm,
                       cudaStream_t st) {
   if (n0 <= 0) return;
   const int nb = (int)((n0 + kSelBlock - 1) / kSelBlock);
   l0_count_kernel<<<nb, kSelBlock, 0, st>>>(keys, n0, p.min_score, scratch);
   l0_scan_kernel<<<1, 1024, 0, st>>>(scratch, nb, count);
-  l0_emit_kernel<<<nb, kSelBlock, 0, st>>>(keys, n0, scratch, wstart, plen, np, seq_base, ar, p, out);
+  l0_emit_kernel<<<nb, kSelBlock, 0, st>>>(keys, n0, scratch, p.min_score, out);
+  const int rb = (int)std::min<int64_t>((n0 + 127) / 128, (int64_t)nsm * 16);
+  l0_reverse_kernel<<<rb, 128, 0, st>>>(out, count, wstart, plen, np, seq_base, ar, p);
 }
 
 void launch_reverse(ScanTask *tasks, int first, int n, const unsigned long long *keys, const int64_t *pair_base,

@@ -13,6 +13,8 @@
 // Direction codes (reverse pass) are 4-bit nibbles per band cell: bits 0-1 = winning state (0 diag, 1 vertical,
 // 2 horizontal), bit 2 = vertical gap extended, bit 3 = horizontal gap extended; state 3 marks cells the reference
 // never writes (its Matrix::reset value 255).  Eight nibbles per word, ceil((2w+1)/8) words per row.
+#include <algorithm>
+
 #include "device_common.cuh"
 
 namespace dcns {
@@ -179,18 +181,14 @@ __device__ __forceinline__ AffMax aff_then(AffMax f, AffMax g) {
   return r;
 }
 
-__global__ void __launch_bounds__(128) xdrop_warp_kernel(XTask *__restrict__ tasks, const int *__restrict__ idx,
-                                                         int n, Arena ar, Params P, uint32_t *__restrict__ tb,
-                                                         int32_t *__restrict__ scratch, int64_t per_warp) {
+// One pass of task T by the calling warp; M and F are the warp's scratch (2w + 2 ints each).  Lane 0 writes the
+// pass's results into T.
+__device__ void xdrop_warp_pass(XTask &T, const Arena &ar, const Params &P, uint32_t *__restrict__ tb,
+                                int32_t *__restrict__ M, int32_t *__restrict__ F) {
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (gw >= n) return;  // whole warp
-  XTask &T = tasks[idx[gw]];
   const int w = T.w, n1 = T.n1, n2 = T.n2, nk = 2 * w + 1;
   const int open = P.open1, ext = P.ext1, g = max(P.ext1, P.open1);
   const SeqView s1{T.base1, T.a1, T.dir}, s2{T.base2, T.a2, T.dir};
-  int32_t *M = scratch + per_warp * gw;
-  int32_t *F = M + (nk + 1);
   for (int k = lane; k <= nk; k += 32) M[k] = kOut, F[k] = kOut;
   __syncwarp();
   const int wpr = xd_words_per_row(w);
@@ -303,6 +301,101 @@ __global__ void __launch_bounds__(128) xdrop_warp_kernel(XTask *__restrict__ tas
   }
 }
 
+__global__ void __launch_bounds__(128) xdrop_warp_kernel(XTask *__restrict__ tasks, const int *__restrict__ idx,
+                                                         int n, Arena ar, Params P, uint32_t *__restrict__ tb,
+                                                         int32_t *__restrict__ scratch, int64_t per_warp) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (gw >= n) return;  // whole warp
+  XTask &T = tasks[idx[gw]];
+  int32_t *M = scratch + per_warp * gw;
+  xdrop_warp_pass(T, ar, P, tb, M, M + (2 * T.w + 2));
+}
+
+// ------------------------------------------------------------------ chained levels
+// All passes of a batch start with the same band w0; level L runs the passes that reached band w0 * 2^L.  Each level
+// kernel reads its work list and count from device memory, appends the passes that must restart (band edge touched;
+// band doubled here, as the reference does) to the next level's list, and the passes whose traceback slot did not fit
+// to the retry list; the host enqueues every level at once and synchronises once.  Traceback slots (reverse passes)
+// are taken from an arena by atomic add: min(n1, 1024) rows of the pass's band.
+struct XLevelArgs {
+  XTask *tasks;
+  const int *list_in;
+  const int *count_in;
+  int *list_out, *count_out;
+  int *retry, *retry_count;
+  unsigned long long *tb_cursor;
+  int64_t tb_words;
+};
+
+__device__ __forceinline__ bool xd_take_slot(XTask &T, const XLevelArgs &L) {
+  const int64_t rows = min(T.n1, 1024);
+  const int64_t words = max((int64_t)1, rows * xd_words_per_row(T.w));
+  const unsigned long long off = atomicAdd(L.tb_cursor, (unsigned long long)words);
+  if ((int64_t)off + words > L.tb_words) return false;
+  T.tb_off = (int64_t)off;
+  T.tb_cap = (int32_t)words;
+  return true;
+}
+
+__device__ __forceinline__ void xd_route(XTask &T, int id, const XLevelArgs &L) {
+  if (T.status == 1) {
+    T.w *= 2;
+    L.list_out[atomicAdd(L.count_out, 1)] = id;
+  } else if (T.status == 2) {
+    L.retry[atomicAdd(L.retry_count, 1)] = id;
+  }
+}
+
+template <int WC>
+__global__ void __launch_bounds__(128) xdrop_level_kernel(XLevelArgs L, Arena ar, Params P, uint32_t *__restrict__ tb) {
+  const int n = *L.count_in;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int id = L.list_in[q];
+    XTask &T = L.tasks[id];
+    if (T.want_codes && !xd_take_slot(T, L)) {
+      T.status = 2;
+      L.retry[atomicAdd(L.retry_count, 1)] = id;
+      continue;
+    }
+    xdrop_pass<WC>(T, ar, P, tb, nullptr, nullptr);
+    xd_route(T, id, L);
+  }
+}
+
+__global__ void __launch_bounds__(128) xdrop_level_warp_kernel(XLevelArgs L, Arena ar, Params P,
+                                                               uint32_t *__restrict__ tb, int32_t *__restrict__ scratch,
+                                                               int64_t per_warp) {
+  const int n = *L.count_in;
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  int32_t *M = scratch + per_warp * gw;
+  for (int q = gw; q < n; q += nw) {
+    const int id = L.list_in[q];
+    XTask &T = L.tasks[id];
+    int ok = 1;
+    if (lane == 0 && T.want_codes) ok = xd_take_slot(T, L) ? 1 : 0;
+    ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
+    __syncwarp();
+    if (!ok) {
+      if (lane == 0) {
+        T.status = 2;
+        L.retry[atomicAdd(L.retry_count, 1)] = id;
+      }
+      continue;
+    }
+    xdrop_warp_pass(T, ar, P, tb, M, M + (2 * T.w + 2));
+    __syncwarp();
+    if (lane == 0) xd_route(T, id, L);
+    __syncwarp();
+  }
+}
+
+__global__ void xdrop_iota_kernel(int *list, int n, int *count) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) list[k] = k;
+  if (k == 0) *count = n;
+}
+
 void launch_xdrop(XTask *tasks, const int *idx, int n, Arena ar, Params p, uint32_t *tb, int wcap, int32_t *scratch,
                   int64_t scratch_per_thread, cudaStream_t st) {
   if (n <= 0) return;
@@ -315,15 +408,30 @@ void launch_xdrop(XTask *tasks, const int *idx, int n, Arena ar, Params p, uint3
     xdrop_warp_kernel<<<(n + 3) / 4, 128, 0, st>>>(tasks, idx, n, ar, p, tb, scratch, scratch_per_thread);
 }
 
+void launch_xdrop_iota(int *list, int n, int *count, cudaStream_t st) {
+  xdrop_iota_kernel<<<(n + 255) / 256, 256, 0, st>>>(list, n, count);
+}
+
+void launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
+                        int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, Arena ar,
+                        Params p, uint32_t *tb, int w, int n_bound, int nsm, int32_t *scratch, int64_t per_warp,
+                        int warps, cudaStream_t st) {
+  if (n_bound <= 0) return;
+  const XLevelArgs L{tasks, list_in, count_in, list_out, count_out, retry, retry_count, tb_cursor, tb_words};
+  const int g = (int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * 16);
+  if (w <= 10)
+    xdrop_level_kernel<10><<<g, 128, 0, st>>>(L, ar, p, tb);
+  else if (w <= 20)
+    xdrop_level_kernel<20><<<g, 128, 0, st>>>(L, ar, p, tb);
+  else
+    xdrop_level_warp_kernel<<<(warps + 3) / 4, 128, 0, st>>>(L, ar, p, tb, scratch, per_warp);
+}
+
 // ------------------------------------------------------------------ traceback of the reverse pass
 // State machine of impl/sequenceAlignment3.cpp:1413-1438: start in the state that produced the cell; a gap state
 // persists while the cell's continuation bit is set; ops are appended as the walk goes (no final reverse, because
 // the walk over the reverse-complement pass already runs in forward order).  Unwritten cells read 255.
-__global__ void xdrop_traceback_kernel(XTask *__restrict__ tasks, const int *__restrict__ idx, int n,
-                                       const uint32_t *__restrict__ tb, uint32_t *__restrict__ cig) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  XTask &T = tasks[idx[t]];
+__device__ void xdrop_traceback_kernel_body(XTask &T, const uint32_t *__restrict__ tb, uint32_t *__restrict__ cig) {
   const int w = T.w, wpr = xd_words_per_row(w);
   int ii = T.end1, jj = T.end2, state = 0, nc = 0;
   uint32_t *out = cig + T.cig_off;
@@ -367,6 +475,77 @@ __global__ void xdrop_traceback_kernel(XTask *__restrict__ tasks, const int *__r
   T.iii = ii;
   T.jjj = jj;
   T.ncig = nc;
+}
+
+__global__ void xdrop_traceback_kernel(XTask *__restrict__ tasks, const int *__restrict__ idx, int n,
+                                       const uint32_t *__restrict__ tb, uint32_t *__restrict__ cig) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  xdrop_traceback_kernel_body(tasks[idx[t]], tb, cig);
+}
+
+// Chained form: every task of the batch that finished with codes takes a CIGAR slot of end1 + end2 + 2 words from an
+// arena sized for the bound n1 + n2 + 2 per task, then runs the state machine above.
+__global__ void xdrop_traceback_all_kernel(XTask *__restrict__ tasks, int n, const uint32_t *__restrict__ tb,
+                                           uint32_t *__restrict__ cig, unsigned long long *__restrict__ cig_cursor) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  XTask &T = tasks[t];
+  if (T.status != 0 || !T.want_codes) return;
+  T.cig_cap = max(T.end1, 0) + max(T.end2, 0) + 2;
+  T.cig_off = (int64_t)atomicAdd(cig_cursor, (unsigned long long)T.cig_cap);
+  xdrop_traceback_kernel_body(T, tb, cig);
+}
+
+void launch_xdrop_traceback_all(XTask *tasks, int n, const uint32_t *tb, uint32_t *cig,
+                                unsigned long long *cig_cursor, cudaStream_t st) {
+  if (n <= 0) return;
+  xdrop_traceback_all_kernel<<<(n + 127) / 128, 128, 0, st>>>(tasks, n, tb, cig, cig_cursor);
+}
+
+// Dense offsets of the finished tasks' CIGARs in task order: one block; each thread sums a contiguous run of tasks,
+// a block-wide exclusive scan of the run sums, then each thread assigns its run's offsets.
+__global__ void __launch_bounds__(1024) xdrop_cigar_scan_kernel(XTask *__restrict__ tasks, int n,
+                                                                unsigned long long *__restrict__ total) {
+  __shared__ long long part[1024];
+  const int t = threadIdx.x, per = (n + 1023) / 1024;
+  const int lo = min(n, t * per), hi = min(n, lo + per);
+  long long sum = 0;
+  for (int k = lo; k < hi; ++k)
+    if (tasks[k].status == 0 && tasks[k].want_codes) sum += tasks[k].ncig;
+  part[t] = sum;
+  __syncthreads();
+  for (int d = 1; d < 1024; d <<= 1) {  // inclusive Hillis-Steele scan
+    const long long v = t >= d ? part[t - d] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  long long off = part[t] - sum;
+  for (int k = lo; k < hi; ++k)
+    if (tasks[k].status == 0 && tasks[k].want_codes) {
+      tasks[k].cig_dense = off;
+      off += tasks[k].ncig;
+    } else {
+      tasks[k].cig_dense = -1;
+    }
+  if (t == 1023) *total = (unsigned long long)part[1023];
+}
+
+__global__ void xdrop_cigar_copy_kernel(const XTask *__restrict__ tasks, int n, const uint32_t *__restrict__ cig,
+                                        uint32_t *__restrict__ dense) {
+  const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (k >= n) return;
+  const XTask &T = tasks[k];
+  if (T.cig_dense < 0) return;
+  for (int q = lane; q < T.ncig; q += 32) dense[T.cig_dense + q] = cig[T.cig_off + q];
+}
+
+void launch_xdrop_cigar_pack(XTask *tasks, int n, const uint32_t *cig, uint32_t *dense, unsigned long long *total,
+                             cudaStream_t st) {
+  if (n <= 0) return;
+  xdrop_cigar_scan_kernel<<<1, 1024, 0, st>>>(tasks, n, total);
+  xdrop_cigar_copy_kernel<<<(n + 7) / 8, 256, 0, st>>>(tasks, n, cig, dense);
 }
 
 void launch_xdrop_traceback(XTask *tasks, const int *idx, int n, const uint32_t *tb, uint32_t *cig, cudaStream_t st) {
