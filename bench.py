@@ -101,6 +101,23 @@ def workload(n_pairs, rank=0):
     return W.config2(n_pairs=n_pairs, seed=shard_seed(rank))
 
 
+# DRAM bytes per algorithmic cell of the level-0 scan launch: ncu, 3,000 pairs of this workload, 18.15 MB read and 0
+# written for 161.25 G cells (profiles/scan_kernel_config2_3000pairs.md); traffic grows with the cells.
+SCAN_DRAM_BYTES_PER_CELL = 18.152192e6 / 161254407231
+
+
+def level0_cells(pairs, window=38, step=8):
+    """Algorithmic cells of the level-0 scan (every window of every pair against its whole reference)."""
+    tot = 0
+    for a, b in pairs:
+        n1, n2 = len(a), len(b)
+        istar = 1 if n2 - window < 0 else (n2 - window) // step + 1
+        nwin = istar + (0 if istar * step > n2 else 1)
+        nfast = min(nwin, (n2 + step - 1) // step) if n1 > 0 else 0
+        tot += n1 * sum(max(0, min(window, n2 - w * step)) for w in range(nfast))
+    return tot
+
+
 def cells_of(st):
     return st["cells_scan"] + st["cells_scan_reverse"] + st["cells_xdrop"] + st["cells_semiglobal"]
 
@@ -249,7 +266,9 @@ def main():
     roofline = {"bound": "int-issue", "kernel": "scan_kernel<38>", "achieved": round(achieved, 2) if achieved else None,
                 "peak": round(peak, 2), "unit": "GCUPS", "frac": round(achieved / peak, 4) if achieved else None,
                 "peak_kind": "measured live: the scan's per-cell int16x2 instruction mix at full occupancy",
-                "traffic": None, "scan_share_of_single_lane_step": round(scan_ms / single_ms, 4),
+                "traffic": round(SCAN_DRAM_BYTES_PER_CELL * level0_cells(pairs) / 1e9, 4) if args.mode == 1 else None,
+                "traffic_unit": "GB per level-0 launch (ncu bytes per cell x this batch's level-0 cells)",
+                "scan_share_of_single_lane_step": round(scan_ms / single_ms, 4),
                 "timing": "CUDA events around each scan launch, two single-lane steps after the timed region"}
 
     extras = {}
