@@ -147,6 +147,24 @@ def config3(n_pairs: int = 64, length: int = 200000, seed: int = 20261206):
     return out
 
 
+def config4(n_seeds: int = 1000000, seed: int = 20261207):
+    """Extension stress: per seed, a 38 bp core with 0-7 substitutions (SW score 41-76 at the default scoring) followed
+    by flanks of U(50, 2000) bp whose query copy has identity U(50, 98) % and 1-5 bp indels at rate U(0, 3) %.
+    Returns [(seq1 codes, seq2 codes)], each pair starting at the seed as x_extend_seed's forward pass sees it."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_seeds):
+        core = random_seq(rng, 38)
+        core2 = bytearray(core)
+        for pos in rng.choice(38, size=int(rng.integers(0, 8)), replace=False):
+            k = int(np.searchsorted(_BASES, core2[pos]))
+            core2[pos] = int(_BASES[(k + int(rng.integers(1, 4))) % 4])
+        flank = random_seq(rng, int(rng.integers(50, 2001)))
+        flank2 = mutate(rng, bytes(flank), float(rng.uniform(0.50, 0.98)), float(rng.uniform(0.0, 0.03)))
+        out.append((encode((core + flank).decode()), encode((core2 + flank2).decode())))
+    return out
+
+
 def random_pair(rng, n1, n2, alphabet=5):
     """Uniform codes over {0..alphabet-1} (alphabet=5 includes N=2) for exhaustive/edge tests."""
     return (rng.integers(0, alphabet, size=n1).astype(np.int8), rng.integers(0, alphabet, size=n2).astype(np.int8))

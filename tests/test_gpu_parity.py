@@ -290,3 +290,39 @@ def test_binned_two_lane_batch_vs_oracle(eng, oracle):
     assert len(got) == len(pairs)
     for i in range(len(pairs)):
         assert_same_fragments(got[i], exp[i], i)
+
+
+@pytest.mark.parametrize("cigar", [False, True])
+def test_xdrop_stress_config4_vs_oracle(eng, oracle, cigar):
+    """Extension-stress seeds (flanks 50-2000 bp, identity 50-98 %, indels 0-3 %): band restarts up to wide bands,
+    reverse passes longer than the first traceback slot, variable termination."""
+    tasks = W.config4(3000, seed=44)
+    out, cigars = eng.SemiGlobal_xextend(tasks, cigar=cigar)
+    for k, (a, b) in enumerate(tasks):
+        e = oracle.xextend(a, b, cigar=cigar)
+        assert tuple(int(v) for v in out[k, :5]) == (e["score"], e["end1"], e["end2"], e["iii"], e["jjj"]), k
+        if cigar:
+            assert cigars[k] == e["cigar"], k
+
+
+def test_long_pair_config3_subsets_vs_oracle(eng, oracle):
+    """Long-pair shapes of the 200 kb workload at sizes the oracle finishes quickly: a 200 kb reference against a 4 kb
+    query slice and a 4 kb reference slice against the 200 kb query (row chunking with warm-ups, many windows)."""
+    a, b = W.config3(n_pairs=1)[0]
+    pairs = [(a, b[100000:104000]), (a[50000:54000], b), (a[:30000], b[:30000])]
+    exp = _oracle_many(oracle, pairs, False)
+    got = eng.align_pairs(pairs, 1)
+    for i in range(len(pairs)):
+        assert_same_fragments(got[i], exp[i], i)
+
+
+def test_long_pair_config3_full_size_alone_equals_in_batch(eng):
+    """At full size (200 kb x 234 kb) the fragments of a pair do not depend on how its scan is tiled: alone (few
+    tiles, rows split into chunks with warm-ups) and inside a batch of other pairs (different chunking)."""
+    a, b = W.config3(n_pairs=1)[0]
+    alone = eng.align_pairs([(a, b)], 1)[0]
+    others = W.config2(n_pairs=300, seed=31)
+    mixed = eng.align_pairs(others[:150] + [(a, b)] + others[150:], 1)[150]
+    assert len(alone) > 50
+    assert frag_keys(alone) == frag_keys(mixed)
+    assert [f.cigar for f in alone] == [f.cigar for f in mixed]
