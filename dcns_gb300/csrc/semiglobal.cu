@@ -1,37 +1,44 @@
 // Two-piece affine semi-global DP with z-drop and band (SemiGlobal_no_avx, impl/sequenceAlignment3.cpp:681-928)
 // and its traceback.
 //
-// One CTA of 8 warps runs one DP.  Rows are processed in stripes of 32 (lane l owns row 32s+1+l), stripe s on warp
-// s mod 8, each as an anti-diagonal wavefront: at step t lane l computes column j = jstart + t - l, receiving the cell
-// above (M, both vertical-gap states, and the query code) from lane l-1 through __shfl_up_sync.  Lane 0 takes the row
-// above the stripe from the previous stripe, written to global scratch at least one CTA barrier earlier and staged
-// into shared memory 32-63 steps ahead of use, so consecutive stripes run concurrently on different warps.  The
-// horizontal gap states stay in registers of the lane that owns the row.
+// One CTA of 8 warps runs one DP.  Rows are processed in stripes of 128: lane l owns the four consecutive rows
+// 128s+1+4l .. 128s+4+4l, stripe s on warp s mod 8, each as an anti-diagonal wavefront: at step t lane l computes
+// column j = jstart + t - l for its four rows top to bottom, receiving the cell above its first row (M, both
+// vertical-gap states, and the query code) from lane l-1 through __shfl_up_sync; rows inside a lane pass the cell
+// above in registers.  Lane 0 takes the row above the stripe from the previous stripe, written to global scratch at
+// least one CTA barrier earlier and staged into shared memory (with the query codes) 32-63 steps ahead of use, so
+// consecutive stripes run concurrently on different warps.  The horizontal gap states stay in registers of the lane
+// that owns the row.  Each cell's priority chain (diag > F1 > E1 > F2 > E2, strict) and gap updates use the DPX
+// max-with-predicate instruction, which yields the maximum and the reference's comparison bit at once.
 //
 // Direction codes are one byte per cell (state 0..4 in bits 0-2, gap-continuation flags in bits 3-6): the reference's
-// traceback needs all seven bits to stay bit-exact.  Layout: stripe-major, then step, then lane, so the 32 lanes of a
-// step write 32 consecutive bytes (one coalesced sector).  Cells the reference never writes (outside the band and
-// the band's last column) are never read: the traceback's bounds test returns 255 for them.
+// traceback needs all seven bits to stay bit-exact.  Layout: stripe-major, then step, then lane, one 32-bit word per
+// lane and step holding its four rows, so the 32 lanes of a step write 128 consecutive bytes.  Cells the reference
+// never writes (outside the band and the band's last column) are never read: the traceback's bounds test returns 255
+// for them.
 //
 // Row-level decisions (running maximum, z-drop, empty row) depend on all earlier rows, so each stripe is computed
-// first and its 32 rows are then evaluated in order; rows after a stop are discarded.  Rows past n2 + w have an empty
+// first and its 128 rows are then evaluated in order; rows after a stop are discarded.  Rows past n2 + w have an empty
 // band: the reference then scores only the last column from a stale cell of column n2-1, which is replayed exactly
 // from the two values the DP left there.
 #include "device_common.cuh"
 
 namespace dcns {
 
+constexpr int kSgNW = 8;             // warps per CTA; one CTA runs one DP, warp w owns stripes w, w+8, ...
+constexpr int kSgD = 2;              // super-steps between the starts of consecutive stripes
+constexpr int kSgR = 4;              // rows per lane
+constexpr int kSgRows = 32 * kSgR;  // rows per stripe
+
+// Wavefront steps of one stripe (columns its rows span, plus the 31-step lane skew), an upper bound for every stripe.
 __host__ __device__ inline int64_t sg_stride_steps(int n2, int w) {
-  return (int64_t)(n2 < 2 * w + 32 ? n2 : 2 * w + 32) + 32;
+  return (int64_t)(n2 < 2 * w + kSgRows ? n2 : 2 * w + kSgRows) + 32;
 }
 
 int64_t sg_tb_bytes(int n1, int n2, int w) {
   if (n1 <= 0 || n2 <= 0) return 0;
-  return (int64_t)((n1 + 31) / 32) * sg_stride_steps(n2, w) * 32;
+  return (int64_t)((n1 + kSgRows - 1) / kSgRows) * sg_stride_steps(n2, w) * 32 * kSgR;
 }
-
-constexpr int kSgNW = 8;  // warps per CTA; one CTA runs one DP, warp w owns stripes w, w+8, ...
-constexpr int kSgD = 2;   // super-steps between the starts of consecutive stripes
 
 struct SgRec {
   int m, f1, f2;
@@ -39,12 +46,15 @@ struct SgRec {
 
 // Super-step length K (wavefront steps between CTA barriers) for a DP whose stripes take at most smax steps:
 //  * a warp finishes stripe s before stripe s+8 starts:   kSgD * kSgNW * K >= smax
-//  * every boundary cell is written at least one barrier before the consumer stages it 32-63 steps ahead of use:
-//    (kSgD - 1) * K >= 127
+//  * every boundary cell is written at least one barrier before the consumer stages it 32-63 steps ahead of use.
+//    Stripe s writes column j at its step j - jstart_s + 31; stripe s+1, which starts kSgD super-steps later, stages
+//    it at step j - jstart_{s+1} - 63 or later, and jstart_{s+1} - jstart_s <= kSgRows; so the producer is at most
+//    kSgRows + 94 steps ahead of that read, which must be at most (kSgD - 1) * K:  K >= kSgRows + 96
 __host__ __device__ inline int sg_superstep(int n2, int w) {
-  const int smax = (n2 < 2 * w + 32 ? n2 : 2 * w + 32) + 31;
+  const int smax = (n2 < 2 * w + kSgRows ? n2 : 2 * w + kSgRows) + 31;
   const int k = (smax + kSgD * kSgNW - 1) / (kSgD * kSgNW);
-  return k > 128 ? k : 128;
+  static_assert(kSgD == 2, "the lower bound below assumes two super-steps between stripe starts");
+  return k > kSgRows + 96 ? k : kSgRows + 96;
 }
 
 // One CTA per DP, on a fixed schedule: stripe s runs steps [(g - 2s) K, (g - 2s + 1) K) in super-step g, and all
@@ -55,8 +65,9 @@ __global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tas
                                                          int n, Arena ar, Params P, uint8_t *__restrict__ tb,
                                                          SgRec *__restrict__ bnd_all, int64_t bnd_stride,
                                                          int *__restrict__ counter) {
-  __shared__ SgRec stage[kSgNW][2][32];      // per warp: boundary cells of the next two 32-column chunks
-  __shared__ int row_best[kSgNW][32], row_bestj[kSgNW][32];
+  __shared__ SgRec stage[kSgNW][2][32];  // per warp: boundary cells of the next two 32-column chunks
+  __shared__ int stage_c[kSgNW][2][32];  // and the query codes of those columns
+  __shared__ int row_best[kSgNW][kSgRows], row_bestj[kSgNW][kSgRows];
   __shared__ int done_stripe[kSgNW];
   __shared__ int s_max, s_end1, s_end2, s_rows, s_next_eval, s_stop, s_stale_last, s_stale_prev, s_task;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -79,39 +90,46 @@ __global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tas
     const bool codes = T.want_codes != 0;
     const int r_last = n2 - 1 + w;
     const int n1_eff = (n1 <= 0 || n2 <= 0) ? 0 : min(n1, n2 + w);  // rows with a non-empty band
-    const int nstripes = (n1_eff + 31) / 32;
+    const int nstripes = (n1_eff + kSgRows - 1) / kSgRows;
     const int64_t stride = sg_stride_steps(n2, w);
     const int K = sg_superstep(n2, w);
     // per-warp stripe state (registers persist across super-steps)
     int cs = warp;  // this warp's current stripe
-    int i = 0, c0 = 0, c1 = 0, jstart = 0, nsteps = 0, upB = 0, ci = 0, tdone = 0;
+    int i0 = 0, jstart = 0, nsteps = 0, upB = 0, tdone = 0;
     bool live = false, produce = false;
-    int e1 = kOut, e2 = kOut, best = 0, bestj = 0, diag = kOut;
-    int outM = kOut, outF1 = kOut, outF2 = kOut, outC = 0;
+    int ci[kSgR], c0[kSgR], c1[kSgR], e1[kSgR], e2[kSgR], best[kSgR], bestj[kSgR], prevM[kSgR];
+    bool liver[kSgR];
+    int diag = kOut, outM = kOut, outF1 = kOut, outF2 = kOut, outC = 0;
     SgRec *bup = nullptr, *bdown = nullptr;
-    uint8_t *trow = nullptr;
+    uint32_t *trow = nullptr;
     auto stage_chunk = [&](int chunk) {  // columns jstart + 32*chunk + lane of the row above, into stage[chunk & 1]
       const int j = jstart + 32 * chunk + lane;
       SgRec r{kOut, kOut, kOut};
       if (cs > 0 && j >= 1 && j <= upB) r = bup[j];
       stage[warp][chunk & 1][lane] = r;
+      stage_c[warp][chunk & 1][lane] = (j >= 1 && j <= n2) ? s2.at(ar, j - 1) : 0;
     };
     auto begin_stripe = [&]() {
       const int s = cs;
-      i = 32 * s + 1 + lane;
-      live = i <= n1_eff;
-      c0 = max(i - w, 1);
-      c1 = min(i + w, n2);
-      const int r0 = 32 * s + 1, rl = min(32 * s + 32, n1_eff);
+      i0 = kSgRows * s + 1 + kSgR * lane;
+      live = i0 <= n1_eff;
+#pragma unroll
+      for (int k = 0; k < kSgR; ++k) {
+        const int i = i0 + k;
+        liver[k] = i <= n1_eff;
+        c0[k] = max(i - w, 1);
+        c1[k] = min(i + w, n2);
+        ci[k] = liver[k] ? s1.at(ar, i - 1) : 0;
+        e1[k] = kOut, e2[k] = kOut, best[k] = 0, bestj[k] = 0, prevM[k] = kOut;
+      }
+      const int r0 = kSgRows * s + 1, rl = min(kSgRows * s + kSgRows, n1_eff);
       jstart = max(r0 - w, 1);
       nsteps = min(rl + w, n2) - jstart + 1 + 31;
-      upB = min(32 * s + w, n2);  // the row above (32s) holds columns [max(32s - w, 1), upB]
+      upB = min(kSgRows * s + w, n2);  // the row above (128s) holds columns [max(128s - w, 1), upB]
       produce = s + 1 < nstripes;
-      ci = live ? s1.at(ar, i - 1) : 0;
-      trow = tb + T.tb_off + (int64_t)s * stride * 32;
+      trow = reinterpret_cast<uint32_t *>(tb + T.tb_off) + (int64_t)s * stride * 32;
       bup = bnd + (int64_t)((s + kSgNW - 1) % kSgNW) * bnd_stride;
       bdown = bnd + (int64_t)(s % kSgNW) * bnd_stride;
-      e1 = kOut, e2 = kOut, best = 0, bestj = 0;
       diag = (lane == 0 && s > 0 && jstart > 1) ? bup[jstart - 1].m : kOut;
       outM = kOut, outF1 = kOut, outF2 = kOut, outC = 0;
       tdone = 0;
@@ -119,7 +137,7 @@ __global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tas
       stage_chunk(1);
       __syncwarp();
     };
-    const int nsuper = nstripes > 0 ? kSgD * (nstripes - 1) + (sg_stride_steps(n2, w) + K - 1) / K + 1 : 0;
+    const int nsuper = nstripes > 0 ? kSgD * (nstripes - 1) + (int)((stride + K - 1) / K) + 1 : 0;
     bool started = false;
     for (int g = 0; g < nsuper; ++g) {
       // ---- compute: the warp's current stripe, if it is scheduled in this super-step
@@ -142,51 +160,66 @@ __global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tas
           if (lane == 0) {
             const SgRec r = stage[warp][(t >> 5) & 1][t & 31];
             upM = r.m, upF1 = r.f1, upF2 = r.f2;
-            cj = j <= n2 ? s2.at(ar, j - 1) : 0;
+            cj = stage_c[warp][(t >> 5) & 1][t & 31];
           }
-          int cM = kOut, cF1 = kOut, cF2 = kOut;
-          uint8_t code = 255;
-          if (live && j >= c0 && j <= c1) {
-            const int dg = (j == 1) ? (i == 1 ? 0 : kOut) : diag;
-            const bool last = (j == c1);
-            const int fin1 = last ? kOut : upF1, fin2 = last ? kOut : upF2;
-            int v = score_of(ci, cj, P.match, P.mismatch) + dg;
-            int d = 0;
-            if (!(v > fin1)) d = 1, v = fin1;
-            if (!(v > e1)) d = 2, v = e1;
-            if (!(v > fin2)) d = 3, v = fin2;
-            if (!(v > e2)) d = 4, v = e2;
-            cM = v;
-            if (v > best) best = v, bestj = j;
-            if (j == n2 - 1) {
-              if (i == r_last) s_stale_last = v;
-              if (i == r_last - 1) s_stale_prev = v;
+          // the lane's rows top to bottom; (aM, aF1, aF2) = the cell above, dg = the diagonal cell
+          int aF1 = upF1, aF2 = upF2, dg = diag;
+          uint32_t word = 0xFFFFFFFFu;
+#pragma unroll
+          for (int k = 0; k < kSgR; ++k) {
+            const int i = i0 + k;
+            int cM = kOut, cF1 = kOut, cF2 = kOut;
+            if (liver[k] && j >= c0[k] && j <= c1[k]) {
+              const int dgv = (j == 1) ? (i == 1 ? 0 : kOut) : dg;
+              const bool last = (j == c1[k]);
+              const int fin1 = last ? kOut : aF1, fin2 = last ? kOut : aF2;
+              int v = score_of(ci[k], cj, P.match, P.mismatch) + dgv;
+              int d = 0;
+              bool pr;
+              v = __vibmax_s32(fin1, v, &pr);  // pr: !(v > fin1)
+              d = pr ? 1 : d;
+              v = __vibmax_s32(e1[k], v, &pr);
+              d = pr ? 2 : d;
+              v = __vibmax_s32(fin2, v, &pr);
+              d = pr ? 3 : d;
+              v = __vibmax_s32(e2[k], v, &pr);
+              d = pr ? 4 : d;
+              cM = v;
+              if (v > best[k]) best[k] = v, bestj[k] = j;
+              if (j == n2 - 1) {
+                if (i == r_last) s_stale_last = v;
+                if (i == r_last - 1) s_stale_prev = v;
+              }
+              if (!last) {
+                const int h = v + o1, h2 = v + o2;
+                cF1 = __vibmax_s32(fin1 + x1, h, &pr);
+                d |= pr ? 8 : 0;
+                e1[k] = __vibmax_s32(e1[k] + x1, h, &pr);
+                d |= pr ? 16 : 0;
+                cF2 = __vibmax_s32(fin2 + x2, h2, &pr);
+                d |= pr ? 32 : 0;
+                e2[k] = __vibmax_s32(e2[k] + x2, h2, &pr);
+                d |= pr ? 64 : 0;
+                word = (word & ~(0xFFu << (8 * k))) | ((uint32_t)d << (8 * k));
+              }
+              if (k == kSgR - 1 && lane == 31 && produce) bdown[j] = SgRec{cM, cF1, cF2};
             }
-            if (!last) {
-              const int h = v + o1, f = fin1 + x1;
-              if (f >= h) d |= 8;
-              cF1 = f >= h ? f : h;
-              e1 += x1;
-              if (e1 >= h) d |= 16;
-              e1 = e1 >= h ? e1 : h;
-              const int h2 = v + o2, f2 = fin2 + x2;
-              if (f2 >= h2) d |= 32;
-              cF2 = f2 >= h2 ? f2 : h2;
-              e2 += x2;
-              if (e2 >= h2) d |= 64;
-              e2 = e2 >= h2 ? e2 : h2;
-              code = (uint8_t)d;
-            }
-            if (lane == 31 && produce) bdown[j] = SgRec{cM, cF1, cF2};
+            dg = prevM[k];  // row k at column j - 1: the diagonal of row k + 1
+            prevM[k] = cM;
+            aF1 = cF1, aF2 = cF2;
+            if (k == kSgR - 1) outM = cM;
           }
-          if (codes && live) trow[(int64_t)t * 32 + lane] = code;
+          if (codes && live) trow[(int64_t)t * 32 + lane] = word;
           diag = upM;
-          outM = cM, outF1 = cF1, outF2 = cF2, outC = cj;
+          outF1 = aF1, outF2 = aF2, outC = cj;
         }
         tdone = tend;
         if (tdone == nsteps) {  // stripe complete: publish its rows for the in-order evaluation
-          row_best[cs % kSgNW][lane] = best;
-          row_bestj[cs % kSgNW][lane] = bestj;
+#pragma unroll
+          for (int k = 0; k < kSgR; ++k) {
+            row_best[cs % kSgNW][kSgR * lane + k] = best[k];
+            row_bestj[cs % kSgNW][kSgR * lane + k] = bestj[k];
+          }
           __syncwarp();
           if (lane == 0) done_stripe[cs % kSgNW] = cs;
           cs += kSgNW;
@@ -199,8 +232,8 @@ __global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tas
         int mx = s_max, e1r = s_end1, e2r = s_end2, rows = s_rows, ne = s_next_eval;
         bool stop = false;
         while (!stop && ne < nstripes && done_stripe[ne % kSgNW] == ne) {
-          for (int r = 0; r < 32 && !stop; ++r) {
-            const int ii = 32 * ne + 1 + r;
+          for (int r = 0; r < kSgRows && !stop; ++r) {
+            const int ii = kSgRows * ne + 1 + r;
             if (ii > n1_eff) break;
             const int tm = row_best[ne % kSgNW][r], tj = row_bestj[ne % kSgNW][r];
             if (tm > mx) mx = tm, e1r = ii, e2r = tj;
@@ -295,10 +328,10 @@ __global__ void sg_traceback_kernel(SgTask *__restrict__ tasks, const int *__res
     int code = 255;
     const int c0 = max(ii - w, 1), c1 = min(ii + w, n2);
     if (ii <= T.rows && jj >= c0 && jj < c1) {
-      const int s = (ii - 1) >> 5, l = (ii - 1) & 31;
-      const int jstart = max(32 * s + 1 - w, 1);
+      const int s = (ii - 1) / kSgRows, rr = (ii - 1) % kSgRows, l = rr / kSgR, k = rr % kSgR;
+      const int jstart = max(kSgRows * s + 1 - w, 1);
       const int64_t t = jj - jstart + l;
-      code = tb[T.tb_off + ((int64_t)s * stride + t) * 32 + l];
+      code = tb[T.tb_off + (((int64_t)s * stride + t) * 32 + l) * kSgR + k];
     }
     if (state == 0)
       state = code & 7;
