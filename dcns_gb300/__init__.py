@@ -156,6 +156,8 @@ def _bind(lib):
     lib.dcns_results_free.argtypes = [P(Results)]
     lib.dcns_last_stats.argtypes = [C.c_void_p, P(Stats)]
     lib.dcns_ctx_set_lanes.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    lib.dcns_autotune.argtypes = [C.c_void_p, C.c_void_p, P(Params), C.c_int, P(C.c_int), P(C.c_int),
+                                  P(C.c_double)]
     lib.dcns_smith_waterman_batch.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(Params), _I32P]
     lib.dcns_xextend_batch.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(Params), C.c_int, _I32P, _U32P, C.c_int64,
                                        _I64P]
@@ -318,6 +320,13 @@ class Engine:
     def set_lanes(self, lanes: int, bins: int):
         """Concurrent lanes and work bins for batches of at least 4096 pairs (results do not depend on them)."""
         self._check(self.lib.dcns_ctx_set_lanes(self.h, int(lanes), int(bins)))
+
+    def autotune(self, batch, mode=MODE_ONE_GAP, **kw) -> dict:
+        """Times the resident batch under candidate lane/bin shapes and keeps the fastest (results are unchanged)."""
+        lanes, bins, ratio = C.c_int(), C.c_int(), C.c_double()
+        self._check(self.lib.dcns_autotune(self.h, batch, C.byref(params(**kw)), mode, C.byref(lanes),
+                                           C.byref(bins), C.byref(ratio)))
+        return {"lanes": lanes.value, "bins": bins.value, "bin_ratio": ratio.value}
 
     def last_stats(self) -> dict:
         s = Stats()

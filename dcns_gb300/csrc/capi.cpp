@@ -287,6 +287,17 @@ int dcns_ctx_set_lanes(dcns_ctx *ctx, int lanes, int bins) {
   return DCNS_OK;
 }
 
+int dcns_autotune(dcns_ctx *ctx, dcns_batch *batch, const dcns_params *params, int mode, int *lanes, int *bins,
+                  double *bin_ratio) {
+  if (!ctx || !batch || !params) return DCNS_ERR_INVALID;
+  return guarded(ctx, [&] {
+    autotune(ctx->C, batch->B, to_params(params), mode);
+    if (lanes) *lanes = ctx->C.max_lanes;
+    if (bins) *bins = ctx->C.bins;
+    if (bin_ratio) *bin_ratio = ctx->C.bin_ratio;
+  });
+}
+
 int dcns_last_stats(const dcns_ctx *ctx, dcns_stats *out) {
   if (!ctx || !out) return DCNS_ERR_INVALID;
   *out = ctx->C.stats;

@@ -1540,6 +1540,35 @@ void align_batch(Context &C, Batch &B, const Params &P, int mode, std::vector<st
   C.stats.ms_total = ms_since(t0);
 }
 
+void autotune(Context &C, Batch &B, const Params &P, int mode) {
+  struct Shape {
+    int lanes, bins;
+    double ratio;
+  };
+  auto run = [&](const Shape &sh) {
+    C.max_lanes = sh.lanes, C.bins = sh.bins, C.bin_ratio = sh.ratio;
+    std::vector<std::vector<FragOut>> out;
+    const auto t0 = Clock::now();
+    align_batch(C, B, P, mode, out);
+    return ms_since(t0);
+  };
+  const Shape first[] = {{1, 1, 0.6}, {2, 2, 0.6}, {3, 3, 0.6}, {4, 4, 0.6}, {4, 6, 0.6}, {6, 6, 0.6}};
+  run(Shape{C.max_lanes, C.bins, C.bin_ratio});  // warm: buffers of the current shape
+  Shape best = first[0];
+  double best_ms = 1e300;
+  for (const Shape &sh : first) {
+    run(sh);  // allocates this shape's lane buffers
+    const double ms = std::min(run(sh), run(sh));
+    if (ms < best_ms) best_ms = ms, best = sh;
+  }
+  for (double r : {0.45, 0.75}) {
+    const Shape sh{best.lanes, best.bins, r};
+    const double ms = std::min(run(sh), run(sh));
+    if (ms < best_ms) best_ms = ms, best = sh;
+  }
+  C.max_lanes = best.lanes, C.bins = best.bins, C.bin_ratio = best.ratio;
+}
+
 void add_stats(dcns_stats &a, const dcns_stats &b) {
   a.cells_scan += b.cells_scan, a.cells_scan_reverse += b.cells_scan_reverse, a.cells_xdrop += b.cells_xdrop;
   a.cells_semiglobal += b.cells_semiglobal, a.tasks_scan += b.tasks_scan;

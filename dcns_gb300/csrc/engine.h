@@ -154,6 +154,8 @@ void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, 
                  std::vector<std::vector<FragOut>> &out);
 void batch_upload(Context &C, const std::vector<PairIn> &pairs, Batch &B);
 void align_batch(Context &C, Batch &B, const Params &P, int mode, std::vector<std::vector<FragOut>> &out);
+// Times the resident batch under candidate (lanes, bins, bin_ratio) shapes and keeps the fastest on C.
+void autotune(Context &C, Batch &B, const Params &P, int mode);
 double measure_issue_rate(int nsm, cudaStream_t st);
 void smith_waterman_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, int32_t *out);
 void xextend_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, bool want_cigar, int32_t *out,

@@ -127,6 +127,13 @@ int dcns_measure_scan_roofline(dcns_ctx *ctx, double *gcups);
  * DCNS_LANES and DCNS_BINS override them when a context is created.  Results do not depend on either value. */
 int dcns_ctx_set_lanes(dcns_ctx *ctx, int lanes, int bins);
 
+/* Autotuner (no counterpart in the reference): aligns the resident batch once per candidate pipeline shape (lanes,
+ * bins, and the geometric ratio of bin sizes), times each call, and keeps the fastest on the context.  The chosen
+ * values are returned (any pointer may be NULL).  Results do not depend on the shape; this only tunes throughput for
+ * batches like this one. */
+int dcns_autotune(dcns_ctx *ctx, dcns_batch *batch, const dcns_params *params, int mode, int *lanes, int *bins,
+                  double *bin_ratio);
+
 /* Stats of the context's last dcns_align_pairs call. */
 int dcns_last_stats(const dcns_ctx *ctx, dcns_stats *out);
 
