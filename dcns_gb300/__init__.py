@@ -156,6 +156,10 @@ def _bind(lib):
     lib.dcns_results_free.argtypes = [P(Results)]
     lib.dcns_last_stats.argtypes = [C.c_void_p, P(Stats)]
     lib.dcns_ctx_set_lanes.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    lib.dcns_format_records.argtypes = [C.c_int64, _I64P, _U32P, _F64P, C.c_char_p, C.c_int64, C.c_char_p,
+                                        C.c_int64, C.c_int, C.c_int, C.c_int32, C.c_int32, C.c_char_p, C.c_char_p,
+                                        P(C.c_void_p), P(C.c_int64), P(C.c_void_p), P(C.c_int64)]
+    lib.dcns_free_text.argtypes = [C.c_void_p]
     lib.dcns_autotune.argtypes = [C.c_void_p, C.c_void_p, P(Params), C.c_int, P(C.c_int), P(C.c_int),
                                   P(C.c_double)]
     lib.dcns_smith_waterman_batch.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(Params), _I32P]
@@ -188,6 +192,37 @@ def library():
                 raise RuntimeError(f"{LIB} is missing: call dcns_gb300.build() (no CPU fallback exists)")
             _lib = _bind(C.CDLL(LIB))
     return _lib
+
+
+def format_records(fragments, ref_text: str, qry_text: str, ref_strand: int = 1, qry_strand: int = 1,
+                   ref_start: int = 1, qry_start: int = 1, ref_chr: str = "ref", qry_chr: str = "query"):
+    """SAM and "o" text of one pair as cut1Gap writes them (outputMasking, controlLayer4.cpp:835-1358): `fragments` of
+    that pair (from align_pairs), the region texts still holding their lower-case 'n' runs, strands (1 +, 0 -),
+    1-based region starts and names.  Host only; returns (sam_text, o_text)."""
+    frs = list(fragments)
+    n = len(frs)
+    frag = np.zeros((max(n, 1), 7), np.int64)
+    cig, pv = [], np.zeros(max(n, 1), np.float64)
+    for k, f in enumerate(frs):
+        frag[k, :5] = (f.start1, f.end1, f.start2, f.end2, f.score)
+        frag[k, 5], frag[k, 6] = len(cig), len(f.cigar)
+        cig.extend(int(c) for c in f.cigar)
+        pv[k] = f.pvalue
+    cg = np.asarray(cig if cig else [0], np.uint32)
+    t1, t2 = ref_text.encode(), qry_text.encode()
+    sam, o, ls, lo = C.c_void_p(), C.c_void_p(), C.c_int64(), C.c_int64()
+    lib = library()
+    rc = lib.dcns_format_records(n, frag.ctypes.data_as(_I64P), cg.ctypes.data_as(_U32P), pv.ctypes.data_as(_F64P),
+                                 t1, len(t1), t2, len(t2), int(ref_strand), int(qry_strand), int(ref_start),
+                                 int(qry_start), ref_chr.encode(), qry_chr.encode(), C.byref(sam), C.byref(ls),
+                                 C.byref(o), C.byref(lo))
+    if rc != 0:
+        raise DcnsError(rc, "format_records failed")
+    try:
+        return C.string_at(sam, ls.value).decode(), C.string_at(o, lo.value).decode()
+    finally:
+        lib.dcns_free_text(sam)
+        lib.dcns_free_text(o)
 
 
 def params(**kw) -> Params:

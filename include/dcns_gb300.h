@@ -181,6 +181,20 @@ int dcns_poll(dcns_ctx *ctx, uint64_t ticket, dcns_results **out);
 int dcns_serve_wait(dcns_ctx *ctx, uint64_t ticket, int64_t timeout_ms, dcns_results **out);
 int dcns_serve_stop(dcns_ctx *ctx);
 
+/* SAM and "o" text of one reference/query pair, as cut1Gap writes them (outputMasking,
+ * controlLayer4.cpp:835-1358; cut1Gap's per-query "#done" trailer, :1430-1432, is left to the caller).  Host only.
+ *   n_frag, frag, cigar, pvalue  one pair's fragments in the dcns_results layout (frag rows of 7: start1, end1, start2,
+ *                                end2, score, cigar offset into `cigar`, cigar length)
+ *   ref_text, qry_text           the region texts as extracted from the genomes, still holding the lower-case 'n'
+ *                                runs that were removed before aligning
+ *   ref_strand, qry_strand       1 = +, 0 = -;  ref_start, qry_start: 1-based region starts;  ref_chr, qry_chr: names
+ * *sam and *o receive malloc'ed NUL-terminated texts (free with dcns_free_text) of *sam_len / *o_len bytes. */
+int dcns_format_records(int64_t n_frag, const int64_t *frag, const uint32_t *cigar, const double *pvalue,
+                        const char *ref_text, int64_t ref_len, const char *qry_text, int64_t qry_len, int ref_strand,
+                        int qry_strand, int32_t ref_start, int32_t qry_start, const char *ref_chr, const char *qry_chr,
+                        char **sam, int64_t *sam_len, char **o, int64_t *o_len);
+void dcns_free_text(char *text);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,3 +25,22 @@ g++ -O2 -mavx2 -std=gnu++14 -include cstdint -fPIC -w -I"$REF" -c "$HERE/ref_har
 wait
 g++ -shared -o "$OUT/libdcns_ref.so" $OBJS "$OUT/ref_harness.o"
 echo "build_ref: $OUT/libdcns_ref.so"
+
+# The reference's record writer (outputMasking, controlLayer4.cpp) links against most of the command-line program:
+# every non-test source of its CMakeLists target except main.cpp, compiled directly.
+CLI="controlLayer4.cpp InputParser.cpp impl/fasta.cpp impl/syntenic.cpp model/Node.cpp model/Graph.cpp
+     impl/longestPath.cpp impl/gffToCategory.cpp model/CnsMasResult.cpp model/MsaGraph.cpp
+     impl/getCnsForMultipleSpecies.cpp model/PairSequenceAlginmentResult.cpp impl/calculateLambda.cpp
+     impl/calculateK.cpp impl/permutationLsqLambdaK.cpp impl/maskGenome.cpp impl/getAllTheCdsPositions.cpp
+     impl/samFileToSeeds.cpp model/FastaIndexEntry.cpp impl/FastaIndexEntryImpl.cpp impl/FastaWithIndex.cpp
+     model/utils.cpp impl/mapCNSToGenome.cpp"
+COBJS=""
+for s in $CLI; do
+  o="$OUT/cli_$(echo "$s" | tr '/' '_').o"
+  g++ -O1 -mavx2 -std=gnu++14 -include cstdint -fPIC -w -I"$REF" -c "$REF/$s" -o "$o" &
+  COBJS="$COBJS $o"
+done
+g++ -O1 -std=gnu++14 -include cstdint -fPIC -w -I"$REF" -c "$HERE/ref_cli_harness.cpp" -o "$OUT/ref_cli_harness.o" &
+wait
+g++ -shared -o "$OUT/libdcns_ref_cli.so" $OBJS $COBJS "$OUT/ref_cli_harness.o" -lpthread
+echo "build_ref: $OUT/libdcns_ref_cli.so"
