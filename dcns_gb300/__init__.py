@@ -396,6 +396,12 @@ class Engine:
         finally:
             self.lib.dcns_results_free(res)
 
+    def align_one_to_many(self, ref, queries, mode=MODE_ONE_GAP, **kw):
+        """One reference against many queries in one batched call, as the multi-species caller
+        (getCnsForMultipleSpecies.cpp:126-135) runs pair by pair; the reference is staged and packed once."""
+        ref = _codes(ref).reshape(-1)
+        return self.align_pairs([(ref, q) for q in queries], mode, **kw)
+
     def upload(self, pairs):
         """Pack pairs into device memory once; returns a handle for align_resident."""
         arr, keep = _pairs(pairs)

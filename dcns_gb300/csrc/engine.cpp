@@ -31,6 +31,7 @@
 #include <condition_variable>
 #include <functional>
 #include <thread>
+#include <unordered_map>
 
 namespace dcns {
 
@@ -323,10 +324,24 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
   std::vector<int64_t> src_off(ns);
   std::vector<int32_t> len(ns);
   int64_t total_src = 0, total_dst = 0;
+  // A sequence passed for several pairs (the same pointer and length: one reference against many queries, as in the
+  // multi-species caller) is staged and packed once; the later pairs point at the first copy.
+  std::unordered_map<const int8_t *, std::pair<int32_t, int64_t>> seen;
   for (int64_t k = 0; k < np; ++k) {
     for (int h = 0; h < 2; ++h) {
       const int32_t n = h ? pairs[k].n2 : pairs[k].n1;
+      const int8_t *src = h ? pairs[k].s2 : pairs[k].s1;
       if (n < 0) throw Error(DCNS_ERR_INVALID, "negative sequence length");
+      if (n > 0) {
+        auto it = seen.find(src);
+        if (it != seen.end() && it->second.first == n) {
+          len[2 * k + h] = 0;  // nothing to stage or pack
+          src_off[2 * k + h] = total_src;
+          seq_base[2 * k + h] = it->second.second;
+          continue;
+        }
+        seen[src] = {n, total_dst};
+      }
       len[2 * k + h] = n;
       src_off[2 * k + h] = total_src;
       seq_base[2 * k + h] = total_dst;

@@ -326,3 +326,21 @@ def test_long_pair_config3_full_size_alone_equals_in_batch(eng):
     assert len(alone) > 50
     assert frag_keys(alone) == frag_keys(mixed)
     assert [f.cigar for f in alone] == [f.cigar for f in mixed]
+
+
+def test_one_reference_many_queries_shared_upload(eng):
+    """The multi-species pattern (one reference x N queries, p-value filter off as that caller sets it): one batched
+    call with the reference packed once gives the per-pair results."""
+    rng = np.random.default_rng(515)
+    ref_txt = W.planted_pair(rng, 6000, 10, 0, 30, 60, 0.9, 0.9, 0.0, 0.1)[0]
+    ref = W.prepare(ref_txt)
+    queries = []
+    for k in range(40):  # species: diverged copies of (part of) the reference
+        lo = int(rng.integers(0, 3000))
+        seg = W.mutate(rng, ref_txt[lo:lo + int(rng.integers(1500, 3000))].encode(), float(rng.uniform(0.7, 0.95)),
+                       0.01)
+        queries.append(W.prepare(seg.decode()))
+    got = eng.align_one_to_many(ref, queries, pvalue=1.0)
+    for k, q in enumerate(queries):
+        exp = eng.align_pairs([(ref.copy(), q)], 1, pvalue=1.0)[0]
+        assert frag_keys(got[k]) == frag_keys(exp), k
