@@ -18,6 +18,7 @@ import ctypes as C
 import os
 import subprocess
 import threading
+from collections.abc import Sequence
 from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
@@ -319,7 +320,40 @@ def _unpack(res):
     pv = np.ctypeslib.as_array(R.pvalue, shape=(nf,)).copy() if nf else np.zeros(0)
     ev = np.ctypeslib.as_array(R.evalue, shape=(nf,)).copy() if nf else np.zeros(0)
     cg = np.ctypeslib.as_array(R.cigar, shape=(nc,)).copy() if nc else np.zeros(0, np.uint32)
-    return [FragmentList(frag, pv, ev, cg, int(off[k]), int(off[k + 1])) for k in range(n)]
+    return BatchResults(off, frag, pv, ev, cg)
+
+
+class BatchResults(Sequence):
+    """Per-pair fragment lists of one call (a read-only sequence indexed like the input pairs); each pair's
+    FragmentList is made when it is accessed.  The flat arrays are public: frag (rows of start1, end1, start2, end2,
+    score, cigar offset, cigar length), pvalue, evalue, cigar, pair_offset."""
+
+    __slots__ = ("pair_offset", "frag", "pvalue", "evalue", "cigar")
+
+    def __init__(self, off, frag, pv, ev, cg):
+        self.pair_offset, self.frag, self.pvalue, self.evalue, self.cigar = off, frag, pv, ev, cg
+
+    def __len__(self):
+        return len(self.pair_offset) - 1
+
+    def __getitem__(self, k):
+        if isinstance(k, slice):
+            return [self[i] for i in range(*k.indices(len(self)))]
+        n = len(self)
+        if k < 0:
+            k += n
+        if not 0 <= k < n:
+            raise IndexError(k)
+        return FragmentList(self.frag, self.pvalue, self.evalue, self.cigar, int(self.pair_offset[k]),
+                            int(self.pair_offset[k + 1]))
+
+    def n_fragments(self) -> int:
+        return int(self.pair_offset[-1])
+
+    def __eq__(self, other):
+        return len(self) == len(other) and all(a == b for a, b in zip(self, other))
+
+    __hash__ = None
 
 
 class Engine:
