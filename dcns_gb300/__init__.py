@@ -157,6 +157,7 @@ def _bind(lib):
     lib.dcns_results_free.argtypes = [P(Results)]
     lib.dcns_last_stats.argtypes = [C.c_void_p, P(Stats)]
     lib.dcns_ctx_set_lanes.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    lib.dcns_align_seeded.argtypes = [C.c_void_p, P(Pair), C.c_int64, _I32P, _I64P, P(Params), P(P(Results))]
     lib.dcns_format_records.argtypes = [C.c_int64, _I64P, _U32P, _F64P, C.c_char_p, C.c_int64, C.c_char_p,
                                         C.c_int64, C.c_int, C.c_int, C.c_int32, C.c_int32, C.c_char_p, C.c_char_p,
                                         P(C.c_void_p), P(C.c_int64), P(C.c_void_p), P(C.c_int64)]
@@ -425,6 +426,26 @@ class Engine:
         p = params(**kw)
         res = C.POINTER(Results)()
         self._check(self.lib.dcns_align_pairs(self.h, arr, len(keep), C.byref(p), mode, C.byref(res)))
+        try:
+            return _unpack(res)
+        finally:
+            self.lib.dcns_results_free(res)
+
+    def align_seeded(self, pairs, seeds, max_align_len=0, **kw):
+        """cut2Gaps2's seeded 2-gap overload: seeds[k] = [(start1, end1, start2, end2), ...] 0-based, for pair k."""
+        arr, keep = _pairs(pairs)
+        flat = np.zeros((max(1, sum(len(s) for s in seeds)), 4), np.int32)
+        off = np.zeros(len(keep) + 1, np.int64)
+        q = 0
+        for k, sd in enumerate(seeds):
+            for x in sd:
+                flat[q] = x
+                q += 1
+            off[k + 1] = q
+        p = params(max_align_len=max_align_len, **kw)
+        res = C.POINTER(Results)()
+        self._check(self.lib.dcns_align_seeded(self.h, arr, len(keep), flat.ctypes.data_as(_I32P),
+                                               off.ctypes.data_as(_I64P), C.byref(p), C.byref(res)))
         try:
             return _unpack(res)
         finally:

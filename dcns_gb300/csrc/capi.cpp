@@ -236,6 +236,27 @@ int dcns_align_pairs(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, con
 
 void dcns_results_free(dcns_results *res) { delete reinterpret_cast<ResultsImpl *>(res); }
 
+int dcns_align_seeded(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, const int32_t *seeds,
+                      const int64_t *seed_offset, const dcns_params *params, dcns_results **out) {
+  if (!ctx || (n_pairs > 0 && (!pairs || !seed_offset)) || !params || !out || n_pairs < 0) return DCNS_ERR_INVALID;
+  *out = nullptr;
+  return guarded(ctx, [&] {
+    std::vector<PairIn> pv = to_pairs(pairs, n_pairs);
+    std::vector<std::vector<Seed4>> sd(n_pairs);
+    for (int64_t k = 0; k < n_pairs; ++k) {
+      if (seed_offset[k + 1] < seed_offset[k] || (seed_offset[k + 1] > seed_offset[k] && !seeds))
+        throw Error(DCNS_ERR_INVALID, "bad seed offsets");
+      for (int64_t q = seed_offset[k]; q < seed_offset[k + 1]; ++q)
+        sd[k].push_back(Seed4{seeds[4 * q], seeds[4 * q + 1], seeds[4 * q + 2], seeds[4 * q + 3]});
+    }
+    std::vector<std::vector<FragOut>> fr;
+    align_seeded(ctx->C, pv, sd, to_params(params), fr);
+    auto *R = new ResultsImpl;
+    R->finish(fr, ctx->C.stats);
+    *out = &R->pub;
+  });
+}
+
 int dcns_batch_upload(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, dcns_batch **out) {
   if (!ctx || !out) return DCNS_ERR_INVALID;
   *out = nullptr;

@@ -21,6 +21,8 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <array>
+#include <map>
 #include <atomic>
 #include <chrono>
 #include <climits>
@@ -1503,7 +1505,129 @@ void two_gap_stage(Context &C, const std::vector<PairIn> &pairs, const Params &P
   }
 }
 
+// The seeded 2-gap overload (findSimilarFragmentsForPairedSequence4.cpp:624-745; cut2Gaps2 with seeds from a SAM
+// file).  The reference walks the seeds in order and skips a seed covered by a fragment it has already accepted, so
+// which DPs run depends on earlier results.  Here every seed's reverse DP and the forward DP of every distinct start
+// run on the device first (a superset of what the reference computes; each result depends only on its own inputs),
+// then the host replays the reference's order, skip test, StartAlignment gate and dedupe over those results.
+// Reverse lengths are min(1 + end, max_align) from the seed's own end; when the two end bases differ the ends move
+// back one base (:663-667).  Where that would read before a sequence start (outside the reference's buffer) the DP
+// is shortened to the bases that exist.  No p-value filter (the overload has none).
+void seeded_two_gap(Context &C, const std::vector<PairIn> &pairs, const std::vector<std::vector<Seed4>> &seeds,
+                    const Params &P, std::vector<std::vector<FragOut>> &out) {
+  const int64_t np = (int64_t)pairs.size();
+  const int32_t cap = P.max_align_len > 0 ? P.max_align_len : INT32_MAX;
+  std::vector<SgTask> Rv;
+  std::vector<std::array<int32_t, 2>> rv_end;  // the (moved) end each reverse DP starts from
+  for (int64_t p = 0; p < np; ++p)
+    for (const Seed4 &x : seeds[p]) {
+      int32_t b1 = x.e1, b2 = x.e2;
+      int32_t l11 = (int32_t)std::min<int64_t>(1 + (int64_t)b1, cap), l12 = (int32_t)std::min<int64_t>(1 + (int64_t)b2, cap);
+      if (b1 >= 0 && b1 < pairs[p].n1 && b2 >= 0 && b2 < pairs[p].n2 && pairs[p].s1[b1] != pairs[p].s2[b2]) --b1, --b2;
+      SgTask g{};
+      g.base1 = C.seq_base[2 * p];
+      g.base2 = C.seq_base[2 * p + 1];
+      g.a1 = b1;
+      g.a2 = b2;
+      g.n1 = std::max(0, std::min(l11, b1 + 1));
+      g.n2 = std::max(0, std::min(l12, b2 + 1));
+      g.dir = 1;
+      Rv.push_back(g);
+      rv_end.push_back({b1, b2});
+    }
+  run_semiglobal(C, Rv, P, false, nullptr);
+  // forward DP per distinct start of each pair
+  std::vector<SgTask> Fw;
+  std::vector<std::map<std::pair<int32_t, int32_t>, int32_t>> fw_of(np);
+  {
+    size_t k = 0;
+    for (int64_t p = 0; p < np; ++p)
+      for (size_t s = 0; s < seeds[p].size(); ++s, ++k) {
+        const int32_t s1 = rv_end[k][0] - (Rv[k].end1 - 1), s2 = rv_end[k][1] - (Rv[k].end2 - 1);
+        if (!fw_of[p].emplace(std::make_pair(s1, s2), (int32_t)Fw.size()).second) continue;
+        SgTask g{};
+        g.base1 = C.seq_base[2 * p];
+        g.base2 = C.seq_base[2 * p + 1];
+        g.a1 = s1;
+        g.a2 = s2;
+        g.n1 = (int32_t)std::max<int64_t>(0, std::min<int64_t>((int64_t)pairs[p].n1 - s1, cap));
+        g.n2 = (int32_t)std::max<int64_t>(0, std::min<int64_t>((int64_t)pairs[p].n2 - s2, cap));
+        if (s1 < 0 || s2 < 0 || s1 > pairs[p].n1 || s2 > pairs[p].n2) g.n1 = g.n2 = 0;
+        g.dir = 0;
+        Fw.push_back(g);
+      }
+  }
+  std::vector<std::vector<uint32_t>> cg;
+  run_semiglobal(C, Fw, P, true, &cg);
+  // the reference's order over the computed results
+  out.assign(np, {});
+  size_t k = 0;
+  for (int64_t p = 0; p < np; ++p) {
+    std::vector<FragOut> &fr = out[p];
+    std::set<std::pair<int32_t, int32_t>> starts;
+    for (size_t s = 0; s < seeds[p].size(); ++s, ++k) {
+      const Seed4 &x = seeds[p][s];
+      bool use = true;
+      for (const FragOut &f : fr)
+        if (f.s1 <= (int64_t)(uint32_t)x.s1 && f.e1 >= (int64_t)(uint32_t)x.e1 && f.s2 <= (int64_t)(uint32_t)x.s2 &&
+            f.e2 >= (int64_t)(uint32_t)x.e2) {
+          use = false;
+          break;
+        }
+      if (!use) continue;
+      const int32_t s1 = rv_end[k][0] - (Rv[k].end1 - 1), s2 = rv_end[k][1] - (Rv[k].end2 - 1);
+      if (!starts.insert({s1, s2}).second) continue;
+      const int32_t q = fw_of[p].at({s1, s2});
+      const SgTask &g = Fw[q];
+      const int32_t e1z = g.end1 - 1, e2z = g.end2 - 1;
+      if (!(cg[q].size() > 0 && e1z > 0 && e2z > 0)) continue;
+      const int64_t e1 = (int64_t)e1z + s1, e2 = (int64_t)e2z + s2;
+      int toRemove = -1;
+      bool found = false;
+      for (int i = 0; i < (int)fr.size(); ++i)
+        if (fr[i].e1 == e1 + 1 && fr[i].e2 == e2 + 1) {
+          found = true;
+          if (s1 + 1 < fr[i].s1 && s2 + 1 < fr[i].s2) toRemove = i;
+        }
+      if (found && toRemove < 0) continue;
+      FragOut f;
+      f.s1 = s1 + 1;
+      f.e1 = e1 + 1;
+      f.s2 = s2 + 1;
+      f.e2 = e2 + 1;
+      f.score = (int64_t)(uint32_t)g.score;
+      f.cigar = cg[q];
+      evalue(P, double(pairs[p].n1), double(pairs[p].n2), g.score, f.e, f.p);
+      if (toRemove >= 0)
+        fr[toRemove] = std::move(f);
+      else
+        fr.push_back(std::move(f));
+    }
+  }
+}
+
 }  // namespace
+
+void align_seeded(Context &C, const std::vector<PairIn> &pairs, const std::vector<std::vector<Seed4>> &seeds,
+                  const Params &P, std::vector<std::vector<FragOut>> &out) {
+  validate(P);
+  for (const PairIn &p : pairs) {
+    if ((p.n1 > 0 && !p.s1) || (p.n2 > 0 && !p.s2)) throw Error(DCNS_ERR_INVALID, "NULL sequence");
+    if (p.n1 >= (1 << 24) - 2 || p.n2 >= (1 << 24) - 2) throw Error(DCNS_ERR_INVALID, "sequences must be < 16M bases");
+  }
+  for (size_t p = 0; p < seeds.size(); ++p)
+    for (const Seed4 &x : seeds[p])
+      if (x.s1 < 0 || x.s2 < 0 || x.e1 < -1 || x.e2 < -1 || x.e1 >= pairs[p].n1 || x.e2 >= pairs[p].n2)
+        throw Error(DCNS_ERR_INVALID, "seed outside its sequences");
+  auto t0 = Clock::now();
+  C.call_t0 = t0;
+  C.stats = dcns_stats{};
+  out.assign(pairs.size(), {});
+  if (pairs.empty()) return;
+  upload(C, pairs);
+  seeded_two_gap(C, pairs, seeds, P, out);
+  C.stats.ms_total = ms_since(t0);
+}
 
 // ------------------------------------------------------------------ entry points
 void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,

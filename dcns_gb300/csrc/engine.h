@@ -154,6 +154,9 @@ void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, 
                  std::vector<std::vector<FragOut>> &out);
 void batch_upload(Context &C, const std::vector<PairIn> &pairs, Batch &B);
 void align_batch(Context &C, Batch &B, const Params &P, int mode, std::vector<std::vector<FragOut>> &out);
+// The seeded 2-gap overload (cut2Gaps2) over many pairs; seeds[p] in the caller's order.
+void align_seeded(Context &C, const std::vector<PairIn> &pairs, const std::vector<std::vector<Seed4>> &seeds,
+                  const Params &P, std::vector<std::vector<FragOut>> &out);
 // Times the resident batch under candidate (lanes, bins, bin_ratio) shapes and keeps the fastest on C.
 void autotune(Context &C, Batch &B, const Params &P, int mode);
 double measure_issue_rate(int nsm, cudaStream_t st);

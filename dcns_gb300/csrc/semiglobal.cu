@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tas
     if (q >= n) break;
     if (threadIdx.x < kSgNW) done_stripe[threadIdx.x] = -1;
     if (threadIdx.x == 0) {
+      // ends are 1-based rows/columns and stay -1 while no cell is positive: the reference then reports -2 (0-based)
       s_max = 0, s_end1 = -1, s_end2 = -1, s_rows = 0, s_next_eval = 0, s_stop = 0;
       s_stale_last = kOut, s_stale_prev = kOut;
     }

@@ -109,6 +109,13 @@ int dcns_align_pairs(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, con
                      dcns_results **out);
 void dcns_results_free(dcns_results *res);
 
+/* The seeded 2-gap overload of cut2Gaps2 (impl/findSimilarFragmentsForPairedSequence4.cpp:624-745; the x-seeds come
+ * from a SAM file, impl/samFileToSeeds.cpp) for many pairs: seeds are (start1, end1, start2, end2) quadruples,
+ * 0-based inclusive, pair k owning seeds[4*seed_offset[k] .. 4*seed_offset[k+1]), in the caller's order.
+ * params->max_align_len (maximumAlignLength; 0 = unlimited) caps every DP's lengths; no p-value filter. */
+int dcns_align_seeded(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, const int32_t *seeds,
+                      const int64_t *seed_offset, const dcns_params *params, dcns_results **out);
+
 /* Resident batches: dcns_batch_upload packs the pairs into device memory once; dcns_align_batch then runs the
  * pipeline on the resident sequences (no sequence upload).  A batch belongs to the context that made it. */
 typedef struct dcns_batch dcns_batch;

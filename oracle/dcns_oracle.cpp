@@ -655,6 +655,65 @@ std::vector<Frag> two_piece_stage(const Pair &pr, const Params &P, const std::ve
   return out;
 }
 
+// The seeded 2-piece overload (findSimilarFragmentsForPairedSequence4.cpp:624-745, driven by cut2Gaps2 with seeds
+// read from a SAM file).  Per seed, in order:
+//   * skipped when an accepted fragment covers it (:651-659: 1-based fragment coordinates compared with the 0-based
+//     seed coordinates, as the reference does);
+//   * reverse 2-piece z-drop from the seed end, both lengths min(1 + end, max_align) from the seed's own end; when the
+//     two end bases differ the ends move back one base first (:663-667) but the lengths stay;
+//   * start = end - reverse end, the StartAlignment gate, a forward 2-piece with CIGAR over
+//     min(length - start, max_align), and the dedupe by end of :686-710.  No p-value filter.
+// Where the moved-back end would make the reverse DP read before the start of a sequence (the reference reads outside
+// its buffer there), the reverse DP is shortened to the bases that exist.
+std::vector<Frag> seeded_two_piece(const Pair &pr, const Params &P, int32_t max_align, const std::vector<Seed4> &seeds,
+                                   Cells &cells) {
+  Score sc{P.match, P.mismatch};
+  std::vector<Frag> out;
+  std::set<std::pair<int32_t, int32_t>> starts;
+  const double L1 = double(pr.n1), L2 = double(pr.n2);
+  for (const Seed4 &x : seeds) {
+    bool use = true;
+    for (const Frag &f : out)
+      if (f.s1 <= x.s1 && f.e1 >= x.e1 && f.s2 <= x.s2 && f.e2 >= x.e2) {
+        use = false;
+        break;
+      }
+    if (!use) continue;
+    int32_t b1 = x.e1, b2 = x.e2;
+    int32_t l11 = std::min(1 + b1, max_align), l12 = std::min(1 + b2, max_align);
+    if (b1 >= 0 && b1 < pr.n1 && b2 >= 0 && b2 < pr.n2 && pr.rc1[pr.n1 - 1 - b1] != pr.rc2[pr.n2 - b2 - 1]) --b1, --b2;
+    l11 = std::max(0, std::min(l11, b1 + 1));
+    l12 = std::max(0, std::min(l12, b2 + 1));
+    SgOut r;
+    semiglobal(pr.rc1.data() + (pr.n1 - 1 - b1), l11, pr.rc2.data() + (pr.n2 - b2 - 1), l12, P, sc, false, r);
+    cells.semiglobal += r.cells;
+    const int32_t s1 = b1 - r.end1, s2 = b2 - r.end2;
+    if (!starts.insert({s1, s2}).second) continue;
+    const int32_t l21 = std::min(pr.n1 - s1, max_align), l22 = std::min(pr.n2 - s2, max_align);
+    SgOut f;
+    semiglobal(pr.s1 + s1, l21, pr.s2 + s2, l22, P, sc, true, f);
+    cells.semiglobal += f.cells;
+    if (!(f.cigar.size() > 0 && f.end1 > 0 && f.end2 > 0)) continue;
+    const int64_t e1 = f.end1 + s1, e2 = f.end2 + s2;
+    int toRemove = -1;
+    bool found = false;
+    for (int i = 0; i < (int)out.size(); ++i)
+      if (out[i].e1 == e1 + 1 && out[i].e2 == e2 + 1) {
+        found = true;
+        if (s1 + 1 < out[i].s1 && s2 + 1 < out[i].s2) toRemove = i;
+      }
+    if (found && toRemove < 0) continue;
+    double ev, pv;
+    evalue(P, L1, L2, f.score, ev, pv);
+    Frag fr{s1 + 1, e1 + 1, s2 + 1, e2 + 1, (int64_t)(uint32_t)f.score, f.cigar, pv, ev};
+    if (toRemove >= 0)
+      out[toRemove] = fr;
+    else
+      out.push_back(fr);
+  }
+  return out;
+}
+
 std::vector<Frag> find_2gap(const Pair &pr, const Params &P, Cells &cells) {
   Score sc{P.match, P.mismatch};
   std::vector<Seed4> xs = all_extend_seeds(pr, P, sc, cells);
@@ -804,6 +863,21 @@ int or_find(const int8_t *s1, int32_t n1, const int8_t *s2, int32_t n2, const in
   pr.init();
   Cells cells;
   std::vector<Frag> fr = two_gap ? find_2gap(pr, P, cells) : find_1gap(pr, P, cells);
+  cells_out(cells, cells_o);
+  return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
+}
+
+// seeds: n_seeds quadruples (start1, end1, start2, end2), 0-based inclusive, in the order the caller read them.
+int or_find_seeded_2gap(const int8_t *s1, int32_t n1, const int8_t *s2, int32_t n2, const int32_t *seeds,
+                        int32_t n_seeds, int32_t max_align, const int32_t *ip, const double *dp, int64_t *frag,
+                        double *pe, uint32_t *cigar, int frag_cap, int cigar_cap, int *n_cigar, int64_t *cells_o) {
+  Params P = params_from(ip, dp);
+  Pair pr{s1, s2, n1, n2, {}, {}};
+  pr.init();
+  std::vector<Seed4> sd(n_seeds);
+  for (int32_t k = 0; k < n_seeds; ++k) sd[k] = Seed4{seeds[4 * k], seeds[4 * k + 1], seeds[4 * k + 2], seeds[4 * k + 3]};
+  Cells cells;
+  std::vector<Frag> fr = seeded_two_piece(pr, P, max_align, sd, cells);
   cells_out(cells, cells_o);
   return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
 }

@@ -254,6 +254,34 @@ int ref_find_2gap(const int8_t *s1, int32_t L1, const int8_t *s2, int32_t L2, in
   return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
 }
 
+// findSimilarFragmentsForPairedSequence, seeded 2-gap overload (cut2Gaps2), impl/findSimilarFragmentsForPairedSequence4.cpp:624.
+// seeds: n_seeds quadruples (start1, end1, start2, end2), 0-based; T is the reference's dense traceback matrix of
+// (max_align + 1)^2 bytes, as cut2Gaps2 allocates it (controlLayer4.cpp:1908).
+int ref_find_seeded_2gap(const int8_t *s1, int32_t L1, const int8_t *s2, int32_t L2, const int32_t *seeds,
+                         int32_t n_seeds, int32_t max_align, int open1, int ext1, int open2, int ext2, int match,
+                         int mismatch, double pvalue, double lambda, double kvalue, int zdrop, int bandwidth,
+                         int64_t *frag, double *pe, uint32_t *cigar, int frag_cap, int cigar_cap, int *n_cigar) {
+  Scorei m((int8_t)match, (int8_t)mismatch);
+  std::vector<int8_t> a = copyseq(s1, L1), b = copyseq(s2, L2);
+  std::vector<int8_t> ar = revcomp(s1, L1), br = revcomp(s2, L2);
+  int32_t l1 = L1, l2 = L2, win = 38, mal = max_align;
+  std::string str1, str2;
+  std::vector<Seed> sd;
+  for (int32_t k = 0; k < n_seeds; ++k) {
+    int32_t a1 = seeds[4 * k], e1 = seeds[4 * k + 1], a2 = seeds[4 * k + 2], e2 = seeds[4 * k + 3];
+    sd.emplace_back(a1, e1, a2, e2);
+  }
+  Matrix T(max_align + 1, max_align + 1);
+  std::vector<PairedSimilarFragment> fr;
+  {
+    Silence quiet;
+    fr = findSimilarFragmentsForPairedSequence(a.data(), ar.data(), b.data(), br.data(), l1, l2, win, open1, ext1,
+                                               open2, ext2, match, mismatch, m, str1, str2, pvalue, lambda, kvalue,
+                                               zdrop, bandwidth, sd, T, mal);
+  }
+  return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
+}
+
 // slidingWindowAlignment, impl/slidingWindowAlignment.cpp:11.  seqs[0] is the reference; the reference writes
 // "j name score" lines to out_path, which the caller parses.
 int ref_sliding(const int8_t *const *seqs, const int32_t *lens, int nseq, int window, int step, int open, int ext,

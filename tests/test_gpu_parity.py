@@ -344,3 +344,16 @@ def test_one_reference_many_queries_shared_upload(eng):
     for k, q in enumerate(queries):
         exp = eng.align_pairs([(ref.copy(), q)], 1, pvalue=1.0)[0]
         assert frag_keys(got[k]) == frag_keys(exp), k
+
+
+@pytest.mark.parametrize("max_align", [0, 400])
+def test_seeded_two_gap_vs_oracle(eng, oracle, max_align):
+    """cut2Gaps2's seeded overload: reverse DPs of every seed and forward DPs of every distinct start on the device,
+    the reference's order, skip test and dedupe replayed on the host."""
+    from test_oracle_pin import _seeded_cases
+
+    cases = _seeded_cases(oracle, n=4, seed=7)
+    got = eng.align_seeded([(A, B) for A, B, _ in cases], [s for _, _, s in cases], max_align_len=max_align)
+    for k, (A, B, seeds) in enumerate(cases):
+        exp = oracle.find_seeded(A, B, seeds, max_align if max_align > 0 else 1 << 30)
+        assert_same_fragments(got[k], exp, k)

@@ -123,3 +123,41 @@ def test_live_reference_random(oracle, reference):
             got, _ = oracle.find(a, b, two_gap=tg)
             exp = reference.find(a, b, two_gap=tg)
             assert [f.key() for f in got] == [f.key() for f in exp]
+
+
+def _seeded_cases(orc, n=5, seed=1):
+    """Pairs with x-seeds as cut2Gaps2 reads them from SAM: the 1-gap fragments (0-based), plus covered, repeated,
+    stretched (end bases that differ: the reference moves such ends back) seeds, shuffled."""
+    import numpy as np
+    from dcns_gb300 import workloads as W
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        a, b = W.planted_pair(rng, 3000, 3200, 12, 60, 300, 0.85, 0.97, 0.01, 0.0)
+        A, B = W.prepare(a), W.prepare(b)
+        base = [(f.start1 - 1, f.end1 - 1, f.start2 - 1, f.end2 - 1) for f in orc.find(A, B)[0]]
+        extra = []
+        for s1, e1, s2, e2 in base[:5]:
+            extra += [(s1 + 5, e1 - 5, s2 + 5, e2 - 5), (s1, e1, s2, e2), (s1, min(e1 + 3, len(A) - 1), s2,
+                                                                            min(e2 + 1, len(B) - 1))]
+        seeds = base + extra
+        rng.shuffle(seeds)
+        out.append((A, B, [tuple(int(v) for v in x) for x in seeds]))
+    return out
+
+
+def test_seeded_two_gap_matches_reference(oracle, reference):
+    """The seeded 2-gap overload of cut2Gaps2 (findSimilarFragmentsForPairedSequence4.cpp:624-745)."""
+    if reference is None:
+        pytest.skip("reference not built on this host")
+    n = 0
+    for A, B, seeds in _seeded_cases(oracle):
+        for ma in (5000, 400):
+            got = oracle.find_seeded(A, B, seeds, ma)
+            exp = reference.find_seeded(A, B, seeds, ma)
+            assert [f.key() for f in got] == [f.key() for f in exp], ma
+            for x, y in zip(got, exp):
+                assert abs(x.pvalue - y.pvalue) <= 1e-12 * max(1.0, abs(y.pvalue))
+            n += len(got)
+    assert n > 20
