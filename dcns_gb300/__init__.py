@@ -162,6 +162,9 @@ def _bind(lib):
                                         C.c_int64, C.c_int, C.c_int, C.c_int32, C.c_int32, C.c_char_p, C.c_char_p,
                                         P(C.c_void_p), P(C.c_int64), P(C.c_void_p), P(C.c_int64)]
     lib.dcns_free_text.argtypes = [C.c_void_p]
+    lib.dcns_sam_to_seeds.argtypes = [C.c_char_p, C.c_int64, C.c_int, P(C.c_char_p), P(C.c_char_p), _I64P, C.c_int,
+                                      P(C.c_char_p), P(C.c_char_p), _I64P, P(_I32P), P(C.c_int64)]
+    lib.dcns_free_seeds.argtypes = [_I32P]
     lib.dcns_autotune.argtypes = [C.c_void_p, C.c_void_p, P(Params), C.c_int, P(C.c_int), P(C.c_int),
                                   P(C.c_double)]
     lib.dcns_smith_waterman_batch.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(Params), _I32P]
@@ -225,6 +228,34 @@ def format_records(fragments, ref_text: str, qry_text: str, ref_strand: int = 1,
     finally:
         lib.dcns_free_text(sam)
         lib.dcns_free_text(o)
+
+
+def sam_to_seeds(sam_text: str, ref_genome: dict, query_genome: dict):
+    """cut2Gaps2's x-seeds from SAM text (samFileToSeeds): {(strand, ref name, query name): [(start1, end1, start2,
+    end2), ...]} in line order, strand 0 for flag 0 and 1 otherwise; genomes map names to texts with 'n' runs."""
+    rn, qn = list(ref_genome), list(query_genome)
+    rb = [ref_genome[k].encode() for k in rn]
+    qb = [query_genome[k].encode() for k in qn]
+    arr = lambda xs: (C.c_char_p * max(1, len(xs)))(*xs)  # noqa: E731
+    rl = np.array([len(x) for x in rb] or [0], np.int64)
+    ql = np.array([len(x) for x in qb] or [0], np.int64)
+    sam = sam_text.encode()
+    out, n = _I32P(), C.c_int64()
+    lib = library()
+    rc = lib.dcns_sam_to_seeds(sam, len(sam), len(rn), arr([k.encode() for k in rn]), arr(rb), rl.ctypes.data_as(_I64P),
+                               len(qn), arr([k.encode() for k in qn]), arr(qb), ql.ctypes.data_as(_I64P),
+                               C.byref(out), C.byref(n))
+    if rc != 0:
+        raise DcnsError(rc, "sam_to_seeds failed")
+    try:
+        recs = np.ctypeslib.as_array(out, shape=(max(1, n.value) * 7,))[:n.value * 7].reshape(-1, 7).copy()
+    finally:
+        lib.dcns_free_seeds(out)
+    seeds = {}
+    for r in recs:
+        key = (int(r[2]), rn[r[0]] if r[0] >= 0 else None, qn[r[1]] if r[1] >= 0 else None)
+        seeds.setdefault(key, []).append(tuple(int(v) for v in r[3:]))
+    return seeds
 
 
 def params(**kw) -> Params:

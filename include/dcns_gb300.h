@@ -116,6 +116,16 @@ void dcns_results_free(dcns_results *res);
 int dcns_align_seeded(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, const int32_t *seeds,
                       const int64_t *seed_offset, const dcns_params *params, dcns_results **out);
 
+/* x-seeds of cut2Gaps2 from SAM text (samFileToSeeds, impl/samFileToSeeds.cpp:19-141): the reference and query
+ * genomes are given by name with their texts (still holding lower-case 'n' runs).  *seeds receives a malloc'ed array
+ * (free with dcns_free_seeds) of *n_seeds records of 7 int32 in line order: reference index, query index (-1 when the
+ * name is not among the given ones), strand (0: flag 0, 1: any other flag), start1, end1, start2, end2 (0-based, on
+ * the sequences with 'n' removed; the query coordinates of strand 1 on its reverse complement). */
+int dcns_sam_to_seeds(const char *sam, int64_t sam_len, int n_ref, const char *const *ref_names,
+                      const char *const *ref_texts, const int64_t *ref_lens, int n_qry, const char *const *qry_names,
+                      const char *const *qry_texts, const int64_t *qry_lens, int32_t **seeds, int64_t *n_seeds);
+void dcns_free_seeds(int32_t *seeds);
+
 /* Resident batches: dcns_batch_upload packs the pairs into device memory once; dcns_align_batch then runs the
  * pipeline on the resident sequences (no sequence upload).  A batch belongs to the context that made it. */
 typedef struct dcns_batch dcns_batch;

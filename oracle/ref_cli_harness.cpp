@@ -6,6 +6,12 @@
 #include <string>
 #include <vector>
 
+#include <cstdio>
+#include <iostream>
+#include <fstream>
+#include <map>
+
+#include "impl/samFileToSeeds.h"
 #include "model/PairedSimilarFragment.h"
 
 // defined in controlLayer4.cpp (no header declares it)
@@ -36,4 +42,37 @@ extern "C" int ref_output_masking(const char *prefix, int64_t n_frag, const int6
   std::string s1 = without_n(t1), s2 = without_n(t2);
   outputMasking(prefix, frs, ref_strand, qry_strand, ref_start, qry_start, ref_chr, qry_chr, s1, s2, t1, t2);
   return 0;
+}
+
+// samFileToSeeds (impl/samFileToSeeds.cpp:19): reads the SAM file at sam_path; genomes by name.  Writes records of
+// 7 int32 (strand 0 positive / 1 negative, reference index, query index, start1, end1, start2, end2) in the order of
+// the reference's maps (strand, then reference name, then query name, then insertion); returns the count, or -1
+// when cap is too small.
+extern "C" int ref_sam_to_seeds(const char *sam_path, int n_ref, const char *const *ref_names,
+                                const char *const *ref_texts, int n_qry, const char *const *qry_names,
+                                const char *const *qry_texts, int32_t *out, int cap) {
+  std::map<std::string, std::map<std::string, std::vector<Seed>>> pos, neg;
+  std::map<std::string, std::string> rg, qg;
+  std::map<std::string, int> ri, qi;
+  for (int k = 0; k < n_ref; ++k) rg[ref_names[k]] = ref_texts[k], ri[ref_names[k]] = k;
+  for (int k = 0; k < n_qry; ++k) qg[qry_names[k]] = qry_texts[k], qi[qry_names[k]] = k;
+  std::string path(sam_path);
+  {
+    std::streambuf *old = std::cout.rdbuf(nullptr);  // the reader prints progress to stdout
+    samFileToSeeds(path, pos, neg, rg, qg);
+    std::cout.rdbuf(old);
+  }
+  int n = 0;
+  for (int strand = 0; strand < 2; ++strand)
+    for (auto &a : strand ? neg : pos)
+      for (auto &b : a.second)
+        for (Seed &sd : b.second) {
+          if (n >= cap) return -1;
+          int32_t *r = out + 7 * n++;
+          r[0] = strand;
+          r[1] = ri.count(a.first) ? ri[a.first] : -1;
+          r[2] = qi.count(b.first) ? qi[b.first] : -1;
+          r[3] = sd.getStart1(), r[4] = sd.getEnd1(), r[5] = sd.getStart2(), r[6] = sd.getEnd2();
+        }
+  return n;
 }

@@ -78,3 +78,51 @@ def test_records_live_reference_writer(tmp_path):
         for rs, qs in G.STRANDS:
             exp = G.reference_records(lib, frs, a, b, rs, qs, 11, 23, "c", "q")
             assert D.format_records(frs, a, b, rs, qs, 11, 23, "c", "q") == exp, (k, rs, qs)
+
+
+def _sam_corpus():
+    """SAM text as cut1Gap writes it (dCNS's own records, both strands, hard clip first), plus header, short,
+    unclipped and N/S-operator lines; genomes keyed by name."""
+    from dcns_gb300 import workloads as W
+    from oracle import oracle as O
+
+    orc = O.Oracle()
+    rng = np.random.default_rng(4321)
+    ref_g, qry_g, lines = {}, {}, ["@HD\tVN:1.6", "@SQ\tSN:chr1\tLN:100", "short"]
+    for k in range(3):
+        a, b = W.planted_pair(rng, 4000, 3800, 20, 50, 250, 0.88, 0.98, 0.01, 0.2, mask_lo=5, mask_hi=60)
+        rname, qname = f"chr{k + 1}", f"ctg{k + 1}"
+        ref_g[rname], qry_g[qname] = a, b
+        frs = orc.find(W.prepare(a), W.prepare(b))[0]
+        for qs in (1, 0):
+            sam, _ = D.format_records(frs, a, b, 1, qs, 1, 1, rname, qname)
+            lines += sam.splitlines()
+    lines += ["ctg1\t0\tchr1\t500\t60\t40M2D10M\t*\t0\t0\tACGT\t*",          # no leading clip: ignored
+              "ctg2\t0\tchr2\t700\t60\t12S30M5N20M3I8M\t*\t0\t0\tACGT\t*",   # soft clip, N and I
+              "ctg9\t0\tchr1\t100\t60\t7H20M\t*\t0\t0\tACGT\t*",             # query not among the genomes
+              "ctg3\t256\tchr3\t900\t60\t3H25M1D9M\t*\t0\t0\tACGT\t*"]       # any non-zero flag
+    return "\n".join(lines) + "\n", ref_g, qry_g
+
+
+def test_sam_to_seeds_matches_reference_reader(tmp_path):
+    cli = os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libdcns_ref_cli.so")
+    if not os.path.exists(cli):
+        pytest.skip("reference reader not built on this host")
+    import ctypes as C
+
+    sam, ref_g, qry_g = _sam_corpus()
+    path = tmp_path / "in.sam"
+    path.write_text(sam)
+    lib = C.CDLL(cli)
+    rn, qn = list(ref_g), list(qry_g)
+    arr = lambda xs: (C.c_char_p * len(xs))(*[x.encode() for x in xs])  # noqa: E731
+    out = np.zeros((4096, 7), np.int32)
+    n = lib.ref_sam_to_seeds(str(path).encode(), len(rn), arr(rn), arr([ref_g[k] for k in rn]), len(qn), arr(qn),
+                             arr([qry_g[k] for k in qn]), out.ctypes.data_as(C.POINTER(C.c_int32)), 4096)
+    assert n > 20
+    exp = {}
+    for r in out[:n]:
+        key = (int(r[0]), rn[r[1]] if r[1] >= 0 else None, qn[r[2]] if r[2] >= 0 else None)
+        exp.setdefault(key, []).append(tuple(int(v) for v in r[3:]))
+    got = D.sam_to_seeds(sam, ref_g, qry_g)
+    assert got == exp
