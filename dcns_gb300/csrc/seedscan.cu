@@ -4,11 +4,17 @@
 //
 // Kernels
 //   pack_kernel         int8 dCNS codes -> 2-bit + N-mask arena (64-base aligned sequences)
-//   scan_kernel<W>      the hot loop: one thread owns two window tasks of one pair as the two int16 halves of every
-//                       register, scanning the same absolute reference rows; 6.5 DPX/ALU instructions per 2 cells
+//   scan_kernel<W, M>   the hot loop: one thread owns two window tasks of one pair as the two int16 halves of every
+//                       register, scanning the same absolute reference rows; per cell pair one score word from the
+//                       thread's query profile in shared memory (a 128-bit load per four columns), fused add-max DPX
+//                       instructions for H, E, the merged H and the next F, and a three-way row maximum every second
+//                       column.  M = 1: level-0 tiles derived from the per-pair table; M = 2: recursion rounds from
+//                       the duo table
 //   scan_generic_kernel int32 lanes, any window width, both reference semantics (striped / scalar); used where the
 //                       fast kernel's static int16 bound or width does not hold
 //   reverse_kernel      the reverse-complement re-scan that fixes each seed's start (getSeeds :156-166)
+//   l0_*_kernel         device selection of the level-0 windows that reached min_score (count, scan, emit in window
+//                       order) and their reverse re-scans, one thread per selected window
 //
 // Semantics reproduced exactly (striped kernels of the reference): per reference row i
 //   Hpre[p] = max(H[i-1][p-1] + s(ref_i, read_p), E[p], 0)
