@@ -14,6 +14,7 @@ namespace dcns {
 
 constexpr int32_t kOut = -536870912;  // score of cells outside a band (impl/sequenceAlignment3.cpp:34)
 constexpr int kScanW = 38;            // window width the fast seed-scan kernel is specialised for
+constexpr int kScanThreads = 64;      // threads per block of the fast seed-scan kernel
 
 struct Params {
   int32_t match, mismatch, open1, ext1, open2, ext2;

@@ -434,7 +434,8 @@ void run_scan_round(Context &C, ScanState &S, const Params &P, int64_t first, in
     C.d_counter.ensure(C, 64);
     h2d(C, C.d_tiles, duos, (size_t)nduo);
     DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int), C.st));
-    const int grid = (int)std::min<int64_t>((int64_t)C.nsm * C.scan_blocks_per_sm, (ntiles + 127) / 128);
+    const int grid = (int)std::min<int64_t>((int64_t)C.nsm * C.scan_blocks_per_sm,
+                                            (ntiles + kScanThreads - 1) / kScanThreads);
     const RecDesc D{C.d_tiles.as<RecDuo>(), C.d_tasks.as<ScanTask>(), C.seqbase_dev, (int32_t)nduo, chunk, warm, 0};
     DCNS_CK(cudaEventRecord(C.ev0, C.st));
     launch_scan(D, ntiles, C.arena, P, C.d_keys.as<unsigned long long>(), C.d_counter.as<int>(), std::max(grid, 1),
@@ -517,7 +518,7 @@ void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
     drows[d] = hi - lo;
     total_rows += hi - lo;
   }
-  const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * 128;
+  const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * kScanThreads;
   const int64_t want_tiles = 8 * resident;
   const int K = warmup_rows(P, kScanW);
   int64_t chunk = INT32_MAX;
@@ -632,7 +633,7 @@ int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, 
     nduo += (nfast[p] + 1) / 2;
     total_rows += (int64_t)((nfast[p] + 1) / 2) * pairs[p].n1;
   }
-  const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * 128;
+  const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * kScanThreads;
   const int K = warmup_rows(P, kScanW);
   int64_t chunk = INT32_MAX;
   if (nduo < 8 * resident && K != INT_MAX && total_rows > 0)
@@ -683,7 +684,7 @@ int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, 
   L0Desc D{C.d_tiles.as<L0Pair>(), (int32_t)np, P.step, P.window, (int32_t)chunk, K, 0};
   // One thread per tile (not a persistent grid): blocks retire as they finish, so the short kernels of other lanes,
   // on higher-priority streams, are scheduled in between instead of waiting for the whole level-0 scan.
-  const int64_t grid = std::max<int64_t>(1, (ntiles + 127) / 128);
+  const int64_t grid = std::max<int64_t>(1, (ntiles + kScanThreads - 1) / kScanThreads);
   cudaStream_t bulk = C.st_bulk;
   if (C.l0_turn) {  // a bin of a binned call: wait for the earlier bins' level-0 scans to be enqueued
     std::unique_lock<std::mutex> lk(C.l0_turn->mu);

@@ -25,6 +25,7 @@
 #include <climits>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "device_common.cuh"
 
@@ -164,9 +165,8 @@ __device__ __forceinline__ ScanTile rec_tile(const RecDesc &D, int64_t t) {
 }
 
 // MODE 1: level-0 tiles from the per-pair table; MODE 2: round tiles from the duo table.
-constexpr int kScanThreads = 128;
 constexpr int kProfGroups = (kScanW + 3) / 4;  // query columns in groups of four (one 128-bit shared load)
-constexpr int kProfSyms = 5;                   // reference symbols A, C, G, T (2-bit codes 0..3) and N
+constexpr int kProfSyms = 4;                   // reference symbols A, C, G, T (2-bit codes 0..3); N rows below
 constexpr size_t kProfBytes = sizeof(uint4) * kProfSyms * kProfGroups * kScanThreads;
 
 template <int W, int MODE>
@@ -177,8 +177,10 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(RecDesc rec, L0Desc 
   // byte 5 = 0xC0 and byte 6 = 0x00, which the padding selector (6, 5) turns into the lane value -16384.
   __shared__ uint32_t tab[16];
   // Per-thread query profile of the current tile: prof[(sym * kProfGroups + g) * kScanThreads + thread] holds the
-  // int16x2 score words (s - open, both halves) of columns 4g..4g+3 against reference symbol sym.  Each thread reads
-  // and writes only its own entries.
+  // int16x2 score words (s - open, both halves) of columns 4g..4g+3 against reference symbol sym (A, C, G, T).  Each
+  // thread reads and writes only its own entries.  A reference N scores 0 against everything: its row takes the
+  // words 0 - open (-16384 in padding columns) from registers instead, on a separate path (N rows are rare: masked
+  // runs are removed before alignment), which keeps the profile at 40 KB per 64-thread block and five blocks per SM.
   extern __shared__ uint4 prof[];
   if (threadIdx.x < 8) {
     const int idx = threadIdx.x;
@@ -208,6 +210,8 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(RecDesc rec, L0Desc 
     // horizontal candidate H + open is G itself, and H + open = max(F + open, Hpre + open) is one fused op.
     // Two banks of G alternate between rows (row r reads Ga and writes Gb, row r+1 the reverse), so the previous
     // row's values stay in place while the new row is written: no register copies in the column loop.
+    const int tw0 = tl.tw[0], tw1 = tl.tw[1];
+    const uint32_t nlo = (uint32_t)(uint16_t)(-open), nhi = (uint32_t)(uint16_t)(-open) << 16;  // s(N, x) - open
     uint32_t Ga[W], Gb[W], E[W];
     {
       uint32_t sel[4 * kProfGroups];
@@ -276,8 +280,8 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(RecDesc rec, L0Desc 
         if (ce1 == r) cmpb = (cmpb & 0x0000FFFFu) | 0x7FFF0000u;
         nev = min_above(r, zr0, zr1, cs0, ce0, cs1, ce1);
       }
-      const int sym = (ncur & 1u) ? 4 : (int)(wcur & 3u);
-      const uint4 *pr = prof + sym * (kProfGroups * kScanThreads) + threadIdx.x;
+      const bool nrow = (ncur & 1u) != 0;
+      const uint4 *pr = prof + (int)(wcur & 3u) * (kProfGroups * kScanThreads) + threadIdx.x;
       ++rk;
       wcur >>= 2;
       ncur >>= 1;
@@ -288,25 +292,36 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(RecDesc rec, L0Desc 
       // before it feeds the next column), i.e. F[p] = max(F[p-1] + max(ext, open), Hpre[p-1] + open): one add-max
       // per column on the serial chain, and F[0] = max(ext, open) from the zero boundary.
       uint32_t gd = open2, F = fext2, rmax = open2, gprev = open2;
-      uint4 q4 = make_uint4(0, 0, 0, 0);
+      auto columns = [&](auto is_n) {
+        uint4 q4 = make_uint4(0, 0, 0, 0);
 #pragma unroll
-      for (int p = 0; p < W; ++p) {
-        if ((p & 3) == 0) q4 = pr[(p >> 2) * kScanThreads];
-        const uint32_t s = (p & 3) == 0 ? q4.x : (p & 3) == 1 ? q4.y : (p & 3) == 2 ? q4.z : q4.w;
-        const uint32_t hp = __viaddmax_s16x2_relu(gd, s, E[p]);  // max(H[i-1][p-1] + s, E, 0)
-        gd = Gi[p];
-        const uint32_t tv = __vadd2(hp, open2);
-        E[p] = __viaddmax_s16x2(E[p], ext2, tv);            // max(E + ext, Hpre + open)
-        const uint32_t g = __viaddmax_s16x2(F, open2, tv);  // max(F, Hpre) + open
-        F = __viaddmax_s16x2(F, fext2, tv);                 // F of the next column
-        Go[p] = g;
-        if (p & 1)
-          rmax = __vimax3_s16x2(rmax, gprev, g);
-        else if (p == W - 1)
-          rmax = __vmaxs2(rmax, g);
-        else
-          gprev = g;
-      }
+        for (int p = 0; p < W; ++p) {
+          uint32_t s;
+          if constexpr (decltype(is_n)::value) {
+            s = (p < tw0 ? nlo : 0xC000u) | (p < tw1 ? nhi : 0xC0000000u);
+          } else {
+            if ((p & 3) == 0) q4 = pr[(p >> 2) * kScanThreads];
+            s = (p & 3) == 0 ? q4.x : (p & 3) == 1 ? q4.y : (p & 3) == 2 ? q4.z : q4.w;
+          }
+          const uint32_t hp = __viaddmax_s16x2_relu(gd, s, E[p]);  // max(H[i-1][p-1] + s, E, 0)
+          gd = Gi[p];
+          const uint32_t tv = __vadd2(hp, open2);
+          E[p] = __viaddmax_s16x2(E[p], ext2, tv);            // max(E + ext, Hpre + open)
+          const uint32_t g = __viaddmax_s16x2(F, open2, tv);  // max(F, Hpre) + open
+          F = __viaddmax_s16x2(F, fext2, tv);                 // F of the next column
+          Go[p] = g;
+          if (p & 1)
+            rmax = __vimax3_s16x2(rmax, gprev, g);
+          else if (p == W - 1)
+            rmax = __vmaxs2(rmax, g);
+          else
+            gprev = g;
+        }
+      };
+      if (nrow)
+        columns(std::true_type{});
+      else
+        columns(std::false_type{});
       const uint32_t gt = __vcmpgts2(rmax, cmpb);
       if (gt) {
         if (gt & 0xFFFFu) {
