@@ -142,6 +142,7 @@ _I32P = C.POINTER(C.c_int32)
 _I64P = C.POINTER(C.c_int64)
 _U32P = C.POINTER(C.c_uint32)
 _F64P = C.POINTER(C.c_double)
+P16 = C.POINTER(C.c_int16)
 
 
 def _bind(lib):
@@ -157,6 +158,8 @@ def _bind(lib):
     lib.dcns_results_free.argtypes = [P(Results)]
     lib.dcns_last_stats.argtypes = [C.c_void_p, P(Stats)]
     lib.dcns_ctx_set_lanes.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    lib.dcns_align_weighted.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(C.c_int16), _I32P, C.c_int32, C.c_int,
+                                        P(Params), P(P(Results))]
     lib.dcns_align_seeded.argtypes = [C.c_void_p, P(Pair), C.c_int64, _I32P, _I64P, P(Params), P(P(Results))]
     lib.dcns_format_records.argtypes = [C.c_int64, _I64P, _U32P, _F64P, C.c_char_p, C.c_int64, C.c_char_p,
                                         C.c_int64, C.c_int, C.c_int, C.c_int32, C.c_int32, C.c_char_p, C.c_char_p,
@@ -457,6 +460,23 @@ class Engine:
         p = params(**kw)
         res = C.POINTER(Results)()
         self._check(self.lib.dcns_align_pairs(self.h, arr, len(keep), C.byref(p), mode, C.byref(res)))
+        try:
+            return _unpack(res)
+        finally:
+            self.lib.dcns_results_free(res)
+
+    def align_weighted(self, pairs, weights, cats, pieces=2, **kw):
+        """weighted1Gap (pieces=1) / weighted2Gaps (pieces=2): weights[k] = category id per base of pair k's seq1,
+        cats = [(match, mismatch, open1, ext1, open2, ext2, zdrop), ...]."""
+        arr, keep = _pairs(pairs)
+        wt = np.concatenate([np.asarray(w, np.int16).reshape(-1) for w in weights]) if weights else np.zeros(1, np.int16)
+        if wt.size == 0:
+            wt = np.zeros(1, np.int16)
+        ct = np.ascontiguousarray(cats, np.int32).reshape(-1, 7)
+        p = params(**kw)
+        res = C.POINTER(Results)()
+        self._check(self.lib.dcns_align_weighted(self.h, arr, len(keep), wt.ctypes.data_as(P16), ct.ctypes.data_as(_I32P),
+                                                 len(ct), int(pieces), C.byref(p), C.byref(res)))
         try:
             return _unpack(res)
         finally:

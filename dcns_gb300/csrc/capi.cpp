@@ -236,6 +236,30 @@ int dcns_align_pairs(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, con
 
 void dcns_results_free(dcns_results *res) { delete reinterpret_cast<ResultsImpl *>(res); }
 
+int dcns_align_weighted(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, const int16_t *weights,
+                        const int32_t *cats, int32_t n_cats, int pieces, const dcns_params *params,
+                        dcns_results **out) {
+  if (!ctx || (n_pairs > 0 && !pairs) || !params || !out || n_pairs < 0 || n_cats < 1 || !cats)
+    return DCNS_ERR_INVALID;
+  *out = nullptr;
+  return guarded(ctx, [&] {
+    std::vector<PairIn> pv = to_pairs(pairs, n_pairs);
+    std::vector<const int16_t *> wp(n_pairs);
+    int64_t off = 0;
+    for (int64_t k = 0; k < n_pairs; ++k) {
+      if (pv[k].n1 > 0 && !weights) throw Error(DCNS_ERR_INVALID, "NULL weights");
+      wp[k] = weights ? weights + off : nullptr;
+      off += std::max(pv[k].n1, 0);
+    }
+    std::vector<int32_t> cv(cats, cats + 7 * (int64_t)n_cats);
+    std::vector<std::vector<FragOut>> fr;
+    align_weighted(ctx->C, pv, wp, cv, pieces, to_params(params), fr);
+    auto *R = new ResultsImpl;
+    R->finish(fr, ctx->C.stats);
+    *out = &R->pub;
+  });
+}
+
 int dcns_align_seeded(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, const int32_t *seeds,
                       const int64_t *seed_offset, const dcns_params *params, dcns_results **out) {
   if (!ctx || (n_pairs > 0 && (!pairs || !seed_offset)) || !params || !out || n_pairs < 0) return DCNS_ERR_INVALID;

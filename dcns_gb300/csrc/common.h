@@ -120,7 +120,19 @@ struct SgTask {
   int32_t status, ncig;
   int64_t cig_off;
   int32_t cig_cap, pad;
+  // weighted variants: category ids of this DP's seq1 (the whole sequence, wlen bases) at wbase in the weight array
+  int64_t wbase;
+  int32_t wlen, wpad;
 };
+
+// Weighted 2-piece / 1-piece DPs (impl/sequenceAlignment3.cpp:1483-1890): per-base category ids of seq1 and, per
+// category, match, mismatch, open1, ext1, open2, ext2, zdrop.
+struct SgWeights {
+  const int16_t *weights;
+  const int32_t *cats;
+  int32_t n_cats, pieces;
+};
+constexpr int kSgwMaxCats = 64;
 
 // ---- kernel launchers (defined in the .cu files)
 void launch_pack(const int8_t *codes, const int64_t *src_off, const int64_t *dst_base, const int32_t *len, int nseq,
@@ -157,7 +169,11 @@ void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p,
 int sg_ctas_per_sm();
 int64_t sg_bnd_bytes(int grid, int max_n2);
 void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, uint32_t *cig,
-                         cudaStream_t st);
+                         cudaStream_t st, bool weighted_layout = false);
 int64_t sg_tb_bytes(int n1, int n2, int w);
+int64_t sgw_tb_bytes(int n1, int n2, int w);
+int64_t sgw_bnd_bytes(int warps, int max_n2);
+void launch_semiglobal_weighted(SgTask *tasks, const int *idx, int n, Arena ar, Params p, SgWeights wt, uint8_t *tb,
+                                void *bnd, int max_n2, int *work_counter, int warps, cudaStream_t st);
 
 }  // namespace dcns

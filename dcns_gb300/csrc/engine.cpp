@@ -91,7 +91,8 @@ void HostBuf::release() {
 
 Context::~Context() {
   DevBuf *bufs[] = {&d_codes, &d_srcoff, &d_dstbase, &d_len, &d_pk, &d_nm, &d_seqbase, &d_flag, &d_tasks, &d_keys,
-                    &d_tiles, &d_counter, &d_idx, &d_scratch, &d_x, &d_tb, &d_cig, &d_sg, &d_sgtb, &d_bnd};
+                    &d_tiles, &d_counter, &d_idx, &d_scratch, &d_x, &d_tb, &d_cig, &d_sg, &d_sgtb, &d_bnd,
+                    &d_wts, &d_cats};
   for (DevBuf *b : bufs) b->release(*this);
   h_codes.release();
   h_misc.release();
@@ -1349,7 +1350,7 @@ int64_t sg_band_cells(int rows, int w, int n2) { return band_cells(rows, w, n2);
 
 // Runs 2-piece semi-global DPs; with codes, bounded by the memory budget per launch (admission by traceback bytes).
 void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool want_codes,
-                    std::vector<std::vector<uint32_t>> *cigars) {
+                    std::vector<std::vector<uint32_t>> *cigars, const SgWeights *W = nullptr) {
   if (G.empty()) return;
   auto t0 = Clock::now();
   const int64_t n = (int64_t)G.size();
@@ -1362,7 +1363,8 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
   while (k0 < n) {
     int64_t bytes = 0, k1 = k0;
     while (k1 < n) {
-      const int64_t b = want_codes ? sg_tb_bytes(G[k1].n1, G[k1].n2, P.bandwidth) : 0;
+      const int64_t b =
+          !want_codes ? 0 : W ? sgw_tb_bytes(G[k1].n1, G[k1].n2, P.bandwidth) : sg_tb_bytes(G[k1].n1, G[k1].n2, P.bandwidth);
       if (k1 > k0 && bytes + b > cap_bytes) break;
       G[k1].tb_off = bytes;
       G[k1].tb_bytes = b;
@@ -1372,10 +1374,11 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
     }
     const int64_t m = k1 - k0;
     if (want_codes) C.d_sgtb.ensure(C, (size_t)std::max<int64_t>(bytes, 1));
-    const int grid = (int)std::min<int64_t>(m, (int64_t)C.nsm * sg_ctas_per_sm());
+    // unweighted: one 8-warp CTA per DP; weighted: one warp per DP, 16 warps per SM
+    const int grid = (int)std::min<int64_t>(m, W ? (int64_t)C.nsm * 16 : (int64_t)C.nsm * sg_ctas_per_sm());
     int maxn2 = 1;
     for (int64_t q = k0; q < k1; ++q) maxn2 = std::max(maxn2, G[q].n2);
-    C.d_bnd.ensure(C, (size_t)sg_bnd_bytes(grid, maxn2));
+    C.d_bnd.ensure(C, (size_t)(W ? sgw_bnd_bytes((grid + 3) / 4 * 4, maxn2) : sg_bnd_bytes(grid, maxn2)));
     C.d_counter.ensure(C, 64);
     DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int), C.st));
     // largest DPs first: the CTA work queue then finishes with the small ones
@@ -1389,8 +1392,12 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
     C.d_idx.ensure(C, sizeof(int32_t) * m);
     h2d(C, C.d_idx, idx.data(), (size_t)m);
     h2d(C, C.d_sg, G.data(), (size_t)n);
-    launch_semiglobal(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, C.d_sgtb.as<uint8_t>(),
-                      C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, C.st);
+    if (W)
+      launch_semiglobal_weighted(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, *W,
+                                 C.d_sgtb.as<uint8_t>(), C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, C.st);
+    else
+      launch_semiglobal(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, C.d_sgtb.as<uint8_t>(),
+                        C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, C.st);
     C.stats.kernel_launches += 1;
     C.stats.semiglobal_dps += m;
     if (want_codes) {
@@ -1405,7 +1412,7 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
       C.d_cig.ensure(C, sizeof(uint32_t) * std::max<int64_t>(cw, 1));
       h2d(C, C.d_sg, G.data(), (size_t)n);
       launch_sg_traceback(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, P.bandwidth, C.d_sgtb.as<uint8_t>(),
-                          C.d_cig.as<uint32_t>(), C.st);
+                          C.d_cig.as<uint32_t>(), C.st, W != nullptr);
       C.stats.kernel_launches += 1;
       C.h_out.ensure(sizeof(uint32_t) * std::max<int64_t>(cw, 1));
       d2h(C, G.data(), C.d_sg, (size_t)n);
@@ -1481,6 +1488,89 @@ void two_gap_stage(Context &C, const std::vector<PairIn> &pairs, const Params &P
     const int32_t s1 = fw_start[q].first, s2 = fw_start[q].second;
     const int32_t e1z = g.end1 - 1, e2z = g.end2 - 1;  // 0-based as returned by SemiGlobal
     if (!(cg[q].size() > 0 && e1z > 0 && e2z > 0)) continue;
+    const int64_t e1 = (int64_t)e1z + s1, e2 = (int64_t)e2z + s2;
+    std::vector<FragOut> &fr = out[p];
+    int toRemove = -1;
+    bool found = false;
+    for (int i = 0; i < (int)fr.size(); ++i)
+      if (fr[i].e1 == e1 + 1 && fr[i].e2 == e2 + 1) {
+        found = true;
+        if (s1 + 1 < fr[i].s1 && s2 + 1 < fr[i].s2) toRemove = i;
+      }
+    if (found && toRemove < 0) continue;
+    FragOut f;
+    f.s1 = s1 + 1;
+    f.e1 = e1 + 1;
+    f.s2 = s2 + 1;
+    f.e2 = e2 + 1;
+    f.score = (int64_t)(uint32_t)g.score;
+    f.cigar = cg[q];
+    evalue(P, double(pairs[p].n1), double(pairs[p].n2), g.score, f.e, f.p);
+    if (toRemove >= 0)
+      fr[toRemove] = std::move(f);
+    else
+      fr.push_back(std::move(f));
+  }
+}
+
+// The weighted drivers (findSimilarFragmentsForPairedSequence4.cpp:784-881, pieces 1; :883-975, pieces 2): per
+// x-seed a weighted reverse DP from its end, the StartAlignment gate, a weighted forward DP with CIGAR.  The 1-piece
+// driver keeps every forward result; the 2-piece one needs a CIGAR and positive ends.
+void weighted_stage(Context &C, const std::vector<PairIn> &pairs, const Params &P,
+                    const std::vector<std::vector<Seed4>> &xs, const WeightSet &W,
+                    std::vector<std::vector<FragOut>> &out) {
+  const int64_t np = (int64_t)pairs.size();
+  std::vector<SgTask> Rv;
+  for (int64_t p = 0; p < np; ++p)
+    for (const Seed4 &x : xs[p]) {
+      SgTask g{};
+      g.base1 = C.seq_base[2 * p];
+      g.base2 = C.seq_base[2 * p + 1];
+      g.a1 = x.e1;
+      g.a2 = x.e2;
+      g.n1 = 1 + x.e1;
+      g.n2 = 1 + x.e2;
+      g.dir = 1;
+      g.wbase = W.wbase[p];
+      g.wlen = pairs[p].n1;
+      Rv.push_back(g);
+    }
+  run_semiglobal(C, Rv, P, false, nullptr, &W.dev);
+  std::vector<SgTask> Fw;
+  std::vector<int32_t> fw_pair;
+  std::vector<std::pair<int32_t, int32_t>> fw_start;
+  {
+    size_t k = 0;
+    for (int64_t p = 0; p < np; ++p) {
+      std::set<std::pair<int32_t, int32_t>> starts;
+      for (size_t s = 0; s < xs[p].size(); ++s, ++k) {
+        const int32_t s1 = xs[p][s].e1 - (Rv[k].end1 - 1), s2 = xs[p][s].e2 - (Rv[k].end2 - 1);
+        if (!starts.insert({s1, s2}).second) continue;
+        SgTask g{};
+        g.base1 = C.seq_base[2 * p];
+        g.base2 = C.seq_base[2 * p + 1];
+        g.a1 = s1;
+        g.a2 = s2;
+        g.n1 = pairs[p].n1 - s1;
+        g.n2 = pairs[p].n2 - s2;
+        g.dir = 0;
+        g.wbase = W.wbase[p];
+        g.wlen = pairs[p].n1;
+        Fw.push_back(g);
+        fw_pair.push_back((int32_t)p);
+        fw_start.push_back({s1, s2});
+      }
+    }
+  }
+  std::vector<std::vector<uint32_t>> cg;
+  run_semiglobal(C, Fw, P, true, &cg, &W.dev);
+  out.assign(np, {});
+  for (size_t q = 0; q < Fw.size(); ++q) {
+    const int32_t p = fw_pair[q];
+    const SgTask &g = Fw[q];
+    const int32_t s1 = fw_start[q].first, s2 = fw_start[q].second;
+    const int32_t e1z = g.end1 - 1, e2z = g.end2 - 1;
+    if (W.dev.pieces == 2 && !(cg[q].size() > 0 && e1z > 0 && e2z > 0)) continue;
     const int64_t e1 = (int64_t)e1z + s1, e2 = (int64_t)e2z + s2;
     std::vector<FragOut> &fr = out[p];
     int toRemove = -1;
@@ -1627,6 +1717,87 @@ void align_seeded(Context &C, const std::vector<PairIn> &pairs, const std::vecto
   if (pairs.empty()) return;
   upload(C, pairs);
   seeded_two_gap(C, pairs, seeds, P, out);
+  C.stats.ms_total = ms_since(t0);
+}
+
+// getAllExtendSeed's p-value filter and x-seed merge (findSimilarFragmentsForPairedSequence4.cpp:395-427).
+std::vector<std::vector<Seed4>> merge_x_seeds(const std::vector<PairIn> &pairs, const Params &P,
+                                              std::vector<std::vector<XSeedOut>> &xr) {
+  const int64_t np = (int64_t)pairs.size();
+  std::vector<std::vector<Seed4>> xs(np);
+  for (int64_t p = 0; p < np; ++p) {
+    const double L1 = double(pairs[p].n1), L2 = double(pairs[p].n2);
+    for (XSeedOut &x : xr[p]) {
+      if (!x.ok) continue;
+      double ev, pv;
+      evalue(P, L1, L2, x.score, ev, pv);
+      if (!(pv < P.pvalue)) continue;
+      bool fresh = true;
+      for (Seed4 &y : xs[p]) {
+        if (y.s1 == x.start1 && y.s2 == x.start2) {
+          fresh = false;
+          if (x.end1 > y.e1 && x.end2 > y.e2) y.e1 = x.end1, y.e2 = x.end2;
+        } else if (y.e1 == x.end1 && y.e2 == x.end2) {
+          if (x.start1 < y.s1 && x.start2 < y.s2) y.s1 = x.start1, y.s2 = x.start2;
+          fresh = false;
+        }
+      }
+      if (fresh) xs[p].push_back(Seed4{x.start1, x.end1, x.start2, x.end2});
+    }
+  }
+  return xs;
+}
+
+void align_single(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,
+                  std::vector<std::vector<FragOut>> &out);
+
+void align_weighted(Context &C, const std::vector<PairIn> &pairs, const std::vector<const int16_t *> &weights,
+                    const std::vector<int32_t> &cats, int pieces, const Params &P,
+                    std::vector<std::vector<FragOut>> &out) {
+  validate(P);
+  if (pieces != 1 && pieces != 2) throw Error(DCNS_ERR_INVALID, "pieces must be 1 or 2");
+  const int32_t ncat = (int32_t)(cats.size() / 7);
+  if (ncat < 1 || ncat > kSgwMaxCats || (int64_t)cats.size() != 7 * (int64_t)ncat)
+    throw Error(DCNS_ERR_INVALID, "1 to 64 categories of 7 values are needed");
+  int64_t total = 0;
+  for (size_t p = 0; p < pairs.size(); ++p) {
+    if ((pairs[p].n1 > 0 && (!pairs[p].s1 || !weights[p])) || (pairs[p].n2 > 0 && !pairs[p].s2))
+      throw Error(DCNS_ERR_INVALID, "NULL sequence or weights");
+    if (pairs[p].n1 >= (1 << 24) - 2 || pairs[p].n2 >= (1 << 24) - 2)
+      throw Error(DCNS_ERR_INVALID, "sequences must be < 16M bases");
+    for (int32_t i = 0; i < pairs[p].n1; ++i)
+      if (weights[p][i] < 0 || weights[p][i] >= ncat) throw Error(DCNS_ERR_INVALID, "weight category out of range");
+    total += pairs[p].n1;
+  }
+  auto t0 = Clock::now();
+  C.call_t0 = t0;
+  C.stats = dcns_stats{};
+  out.assign(pairs.size(), {});
+  if (pairs.empty()) return;
+  upload(C, pairs);
+  WeightSet W;
+  W.wbase.resize(pairs.size());
+  std::vector<int16_t> flat((size_t)std::max<int64_t>(total, 1));
+  int64_t off = 0;
+  for (size_t p = 0; p < pairs.size(); ++p) {
+    W.wbase[p] = off;
+    if (pairs[p].n1 > 0) std::memcpy(flat.data() + off, weights[p], sizeof(int16_t) * pairs[p].n1);
+    off += pairs[p].n1;
+  }
+  C.d_wts.ensure(C, sizeof(int16_t) * flat.size());
+  C.d_cats.ensure(C, sizeof(int32_t) * cats.size());
+  DCNS_CK(cudaMemcpyAsync(C.d_wts.p, flat.data(), sizeof(int16_t) * flat.size(), cudaMemcpyHostToDevice, C.st));
+  DCNS_CK(cudaMemcpyAsync(C.d_cats.p, cats.data(), sizeof(int32_t) * cats.size(), cudaMemcpyHostToDevice, C.st));
+  sync(C);
+  W.dev = SgWeights{C.d_wts.as<int16_t>(), C.d_cats.as<int32_t>(), ncat, pieces};
+  C.weights = &W;
+  try {
+    align_single(C, pairs, P, DCNS_MODE_TWO_GAP, out);
+  } catch (...) {
+    C.weights = nullptr;
+    throw;
+  }
+  C.weights = nullptr;
   C.stats.ms_total = ms_since(t0);
 }
 
@@ -1883,29 +2054,12 @@ void align_single(Context &C, const std::vector<PairIn> &pairs, const Params &P,
       }
     });
   } else {
-    // getAllExtendSeed's filter and x-seed merge (:395-427), then the 2-piece stage
-    std::vector<std::vector<Seed4>> xs(np);
-    for (int64_t p = 0; p < np; ++p) {
-      const double L1 = double(pairs[p].n1), L2 = double(pairs[p].n2);
-      for (XSeedOut &x : xr[p]) {
-        if (!x.ok) continue;
-        double ev, pv;
-        evalue(P, L1, L2, x.score, ev, pv);
-        if (!(pv < P.pvalue)) continue;
-        bool fresh = true;
-        for (Seed4 &y : xs[p]) {
-          if (y.s1 == x.start1 && y.s2 == x.start2) {
-            fresh = false;
-            if (x.end1 > y.e1 && x.end2 > y.e2) y.e1 = x.end1, y.e2 = x.end2;
-          } else if (y.e1 == x.end1 && y.e2 == x.end2) {
-            if (x.start1 < y.s1 && x.start2 < y.s2) y.s1 = x.start1, y.s2 = x.start2;
-            fresh = false;
-          }
-        }
-        if (fresh) xs[p].push_back(Seed4{x.start1, x.end1, x.start2, x.end2});
-      }
-    }
-    two_gap_stage(C, pairs, P, xs, out);
+    // getAllExtendSeed's filter and x-seed merge (:395-427), then the 2-piece stage (weighted when weights are set)
+    std::vector<std::vector<Seed4>> xs = merge_x_seeds(pairs, P, xr);
+    if (C.weights)
+      weighted_stage(C, pairs, P, xs, *C.weights, out);
+    else
+      two_gap_stage(C, pairs, P, xs, out);
   }
 }
 

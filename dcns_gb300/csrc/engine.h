@@ -85,6 +85,12 @@ struct SeedLess {
 };
 using SeedSet = std::set<Seed4, SeedLess>;
 
+// Weighted variants: device category ids of every pair's seq1 (pair p at wbase[p]) and the category table.
+struct WeightSet {
+  SgWeights dev{};
+  std::vector<int64_t> wbase;
+};
+
 struct Context {
   int device = 0;
   cudaStream_t st = nullptr;       // every launch and copy of the context (high priority)
@@ -99,7 +105,8 @@ struct Context {
   // device buffers
   DevBuf d_codes, d_srcoff, d_dstbase, d_len, d_pk, d_nm, d_seqbase, d_flag;
   DevBuf d_tasks, d_keys, d_tiles, d_counter, d_idx, d_scratch;
-  DevBuf d_x, d_tb, d_cig, d_sg, d_sgtb, d_bnd;
+  DevBuf d_x, d_tb, d_cig, d_sg, d_sgtb, d_bnd, d_wts, d_cats;
+  const WeightSet *weights = nullptr;  // set during a weighted call
   // pinned staging
   HostBuf h_codes, h_misc, h_out, h_tasks, h_tiles;
 
@@ -154,6 +161,10 @@ void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, 
                  std::vector<std::vector<FragOut>> &out);
 void batch_upload(Context &C, const std::vector<PairIn> &pairs, Batch &B);
 void align_batch(Context &C, Batch &B, const Params &P, int mode, std::vector<std::vector<FragOut>> &out);
+// The weighted drivers (pieces 1 or 2): weights[p] = category id per seq1 base of pair p; cats = 7 ints per category.
+void align_weighted(Context &C, const std::vector<PairIn> &pairs, const std::vector<const int16_t *> &weights,
+                    const std::vector<int32_t> &cats, int pieces, const Params &P,
+                    std::vector<std::vector<FragOut>> &out);
 // The seeded 2-gap overload (cut2Gaps2) over many pairs; seeds[p] in the caller's order.
 void align_seeded(Context &C, const std::vector<PairIn> &pairs, const std::vector<std::vector<Seed4>> &seeds,
                   const Params &P, std::vector<std::vector<FragOut>> &out);

@@ -304,13 +304,16 @@ void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p,
 }
 
 // ------------------------------------------------------------------ traceback (:869-914)
+// R: rows per lane of the layout that wrote the codes (kSgR for sg_kernel, 1 for the weighted kernel).
+template <int R>
 __global__ void sg_traceback_kernel(SgTask *__restrict__ tasks, const int *__restrict__ idx, int n, int w,
                                     const uint8_t *__restrict__ tb, uint32_t *__restrict__ cig) {
+  constexpr int kRows = 32 * R;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   SgTask &T = tasks[idx[k]];
   const int n2 = T.n2;
-  const int64_t stride = sg_stride_steps(n2, w);
+  const int64_t stride = (int64_t)(n2 < 2 * w + kRows ? n2 : 2 * w + kRows) + 32;
   int ii = T.end1, jj = T.end2, state = 0, nc = 0;
   uint32_t *out = cig + T.cig_off;
   uint32_t last = 0xFFFFFFFFu;
@@ -328,11 +331,12 @@ __global__ void sg_traceback_kernel(SgTask *__restrict__ tasks, const int *__res
   while (ii > 0 && jj > 0) {
     int code = 255;
     const int c0 = max(ii - w, 1), c1 = min(ii + w, n2);
-    if (ii <= T.rows && jj >= c0 && jj < c1) {
-      const int s = (ii - 1) / kSgRows, rr = (ii - 1) % kSgRows, l = rr / kSgR, k = rr % kSgR;
-      const int jstart = max(kSgRows * s + 1 - w, 1);
+    // the unweighted DP writes no code for the band's last column (it reads 255); the weighted DP does
+    if (ii <= T.rows && jj >= c0 && (jj < c1 || (R == 1 && jj == c1))) {
+      const int s = (ii - 1) / kRows, rr = (ii - 1) % kRows, l = rr / R, kk = rr % R;
+      const int jstart = max(kRows * s + 1 - w, 1);
       const int64_t t = jj - jstart + l;
-      code = tb[T.tb_off + (((int64_t)s * stride + t) * 32 + l) * kSgR + k];
+      code = tb[T.tb_off + (((int64_t)s * stride + t) * 32 + l) * R + kk];
     }
     if (state == 0)
       state = code & 7;
@@ -362,9 +366,177 @@ __global__ void sg_traceback_kernel(SgTask *__restrict__ tasks, const int *__res
 }
 
 void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, uint32_t *cig,
-                         cudaStream_t st) {
+                         cudaStream_t st, bool weighted_layout) {
   if (n <= 0) return;
-  sg_traceback_kernel<<<(n + 127) / 128, 128, 0, st>>>(tasks, idx, n, bandwidth, tb, cig);
+  if (weighted_layout)
+    sg_traceback_kernel<1><<<(n + 127) / 128, 128, 0, st>>>(tasks, idx, n, bandwidth, tb, cig);
+  else
+    sg_traceback_kernel<kSgR><<<(n + 127) / 128, 128, 0, st>>>(tasks, idx, n, bandwidth, tb, cig);
+}
+
+// ------------------------------------------------------------------ weighted DPs (one warp per DP)
+// SemiGlobal with weights (impl/sequenceAlignment3.cpp:1483-1709, pieces = 2) and SemiGlobal_single_gap_penalty
+// (:1710-1890, pieces = 1).  Row i takes the category of its seq1 base for the substitution, the horizontal gap
+// states and the z-drop, and the category of the next base for the vertical gap states it leaves (a row at the end
+// of seq1 keeps its own).  Every band column, the last included, updates the gap states and writes its code; a row
+// with an empty band ends the DP (no stale column, unlike the unweighted DP).
+//
+// One warp runs one DP: 32-row stripes one after another, lane l owning row 32s+1+l as an anti-diagonal wavefront,
+// the stripe's last row kept for the next stripe in the warp's global scratch (each column is read by lane 0 at least
+// 31 steps before lane 31 overwrites it).  Rows are evaluated in order after each stripe; the DP ends at the stop row.
+// Codes: one byte per cell, stripe / step / lane, the traceback layout of 32-row stripes.
+__host__ __device__ inline int64_t sgw_stride_steps(int n2, int w) {
+  return (int64_t)(n2 < 2 * w + 32 ? n2 : 2 * w + 32) + 32;
+}
+
+int64_t sgw_tb_bytes(int n1, int n2, int w) {
+  if (n1 <= 0 || n2 <= 0) return 0;
+  return (int64_t)((n1 + 31) / 32) * sgw_stride_steps(n2, w) * 32;
+}
+
+int64_t sgw_bnd_bytes(int warps, int max_n2) { return (int64_t)warps * ((int64_t)max_n2 + 2) * sizeof(SgRec); }
+
+__device__ __forceinline__ int sgw_cat(const SgTask &T, const int16_t *__restrict__ wt, int i) {
+  // category of DP row i (1-based): forward rows follow seq1 from a1, reverse rows go down from a1
+  const int64_t pos = T.dir == 0 ? (int64_t)T.a1 + i - 1 : (int64_t)T.a1 - (i - 1);
+  return wt[T.wbase + pos];
+}
+
+__device__ __forceinline__ int sgw_next_cat(const SgTask &T, const int16_t *__restrict__ wt, int i, int own) {
+  const int64_t pos = T.dir == 0 ? (int64_t)T.a1 + i : (int64_t)T.a1 - i;
+  return (pos < 0 || pos >= T.wlen) ? own : wt[T.wbase + pos];
+}
+
+__global__ void __launch_bounds__(128) sgw_kernel(SgTask *__restrict__ tasks, const int *__restrict__ idx, int n,
+                                                  Arena ar, Params P, SgWeights W, uint8_t *__restrict__ tb,
+                                                  SgRec *__restrict__ bnd_all, int64_t bnd_stride,
+                                                  int *__restrict__ counter) {
+  __shared__ int cat[kSgwMaxCats][7];
+  for (int k = threadIdx.x; k < W.n_cats * 7; k += blockDim.x) cat[k / 7][k % 7] = W.cats[k];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  SgRec *bnd = bnd_all + (int64_t)gw * bnd_stride;
+  const int w = P.bandwidth;
+  const bool two = W.pieces == 2;
+  for (;;) {
+    int q = 0;
+    if (lane == 0) q = atomicAdd(counter, 1);
+    q = __shfl_sync(0xFFFFFFFFu, q, 0);
+    if (q >= n) break;
+    SgTask &T = tasks[idx[q]];
+    const int n1 = T.n1, n2 = T.n2;
+    const SeqView s1{T.base1, T.a1, T.dir}, s2{T.base2, T.a2, T.dir};
+    const bool codes = T.want_codes != 0;
+    const int64_t stride = sgw_stride_steps(n2, w);
+    const int nstripes = (n1 > 0 && n2 > 0) ? (n1 + 31) / 32 : 0;
+    int mx = 0, e1r = -1, e2r = -1, rows = 0;  // lane 0's running evaluation
+    bool stop = false;
+    for (int s = 0; s < nstripes && !stop; ++s) {
+      const int i = 32 * s + 1 + lane;
+      const bool live = i <= n1;
+      const int c0 = max(i - w, 1), c1 = min(i + w, n2);
+      const int ci = live ? s1.at(ar, i - 1) : 0;
+      const int rc = live ? sgw_cat(T, W.weights, i) : 0;
+      const int nc = live ? sgw_next_cat(T, W.weights, i, rc) : 0;
+      const int mt = cat[rc][0], mm = cat[rc][1], o1h = cat[rc][2], x1h = cat[rc][3], o2h = cat[rc][4], x2h = cat[rc][5];
+      const int o1v = cat[nc][2], x1v = cat[nc][3], o2v = cat[nc][4], x2v = cat[nc][5];
+      const int r0 = 32 * s + 1, rl = min(32 * s + 32, n1);
+      const int jstart = max(r0 - w, 1), jend = min(rl + w, n2);
+      const int nsteps = jend >= jstart ? jend - jstart + 1 + 31 : 0;
+      uint8_t *trow = tb + T.tb_off + (int64_t)s * stride * 32;
+      int e1 = kOut, e2 = kOut, best = 0, bestj = two ? kOut : -1;
+      int diag = (lane == 0 && s > 0 && jstart > 1) ? bnd[jstart - 1].m : kOut;
+      int outM = kOut, outF1 = kOut, outF2 = kOut, outC = 0;
+      for (int t = 0; t < nsteps; ++t) {
+        int upM = __shfl_up_sync(0xFFFFFFFFu, outM, 1);
+        int upF1 = __shfl_up_sync(0xFFFFFFFFu, outF1, 1);
+        int upF2 = __shfl_up_sync(0xFFFFFFFFu, outF2, 1);
+        int cj = __shfl_up_sync(0xFFFFFFFFu, outC, 1);
+        const int j = jstart + t - lane;
+        if (lane == 0) {
+          upM = kOut, upF1 = kOut, upF2 = kOut;
+          if (s > 0 && j >= 1 && j <= n2) {
+            const SgRec r = bnd[j];
+            upM = r.m, upF1 = r.f1, upF2 = r.f2;
+          }
+          cj = (j >= 1 && j <= n2) ? s2.at(ar, j - 1) : 0;
+        }
+        int cM = kOut, cF1 = kOut, cF2 = kOut;
+        uint8_t code = 255;
+        if (live && j >= c0 && j <= c1) {
+          const int dg = (j == 1) ? (i == 1 ? 0 : kOut) : diag;
+          const bool last = (j == c1);
+          const int fin1 = last ? kOut : upF1, fin2 = last ? kOut : upF2;
+          int v = ((ci == 2 || cj == 2) ? 0 : (ci == cj ? mt : mm)) + dg;
+          int d = 0;
+          bool pr;
+          v = __vibmax_s32(fin1, v, &pr);
+          d = pr ? 1 : d;
+          v = __vibmax_s32(e1, v, &pr);
+          d = pr ? 2 : d;
+          if (two) {
+            v = __vibmax_s32(fin2, v, &pr);
+            d = pr ? 3 : d;
+            v = __vibmax_s32(e2, v, &pr);
+            d = pr ? 4 : d;
+          }
+          cM = v;
+          if (v > best) best = v, bestj = j;
+          cF1 = __vibmax_s32(fin1 + x1v, v + o1v, &pr);
+          d |= pr ? 8 : 0;
+          e1 = __vibmax_s32(e1 + x1h, v + o1h, &pr);
+          d |= pr ? 16 : 0;
+          if (two) {
+            cF2 = __vibmax_s32(fin2 + x2v, v + o2v, &pr);
+            d |= pr ? 32 : 0;
+            e2 = __vibmax_s32(e2 + x2h, v + o2h, &pr);
+            d |= pr ? 64 : 0;
+          }
+          code = (uint8_t)d;
+        }
+        if (codes && live) trow[(int64_t)t * 32 + lane] = code;
+        __syncwarp();
+        if (lane == 31 && live && j >= c0 && j <= c1) bnd[j] = SgRec{cM, cF1, cF2};
+        __syncwarp();
+        diag = upM;
+        outM = cM, outF1 = cF1, outF2 = cF2, outC = cj;
+      }
+      // the stripe's rows in order (lane 0 decides; every lane takes part in the shuffles)
+      for (int r = 0; r < 32; ++r) {
+        const int tm = __shfl_sync(0xFFFFFFFFu, best, r), tj = __shfl_sync(0xFFFFFFFFu, bestj, r);
+        const int zd = __shfl_sync(0xFFFFFFFFu, cat[rc][6], r), xr = __shfl_sync(0xFFFFFFFFu, x2h, r);
+        const int ii = 32 * s + 1 + r;
+        if (stop || ii > n1) continue;
+        if (tm > mx) mx = tm, e1r = ii, e2r = tj;
+        rows = ii;
+        if (two) {
+          int l = (ii - e1r) - (tj - e2r);
+          l = l > 0 ? l : -l;
+          if (mx - tm > zd + l * xr) stop = true;
+        } else if (mx - tm > zd) {
+          stop = true;
+        }
+        if (!stop && tj <= 0) stop = true;
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      T.score = mx;
+      T.end1 = e1r;
+      T.end2 = e2r;
+      T.rows = rows;
+      T.status = 0;
+    }
+    __syncwarp();
+  }
+}
+
+void launch_semiglobal_weighted(SgTask *tasks, const int *idx, int n, Arena ar, Params p, SgWeights wt, uint8_t *tb,
+                                void *bnd, int max_n2, int *work_counter, int warps, cudaStream_t st) {
+  if (n <= 0) return;
+  sgw_kernel<<<(warps + 3) / 4, 128, 0, st>>>(tasks, idx, n, ar, p, wt, tb, (SgRec *)bnd, (int64_t)max_n2 + 2,
+                                              work_counter);
 }
 
 }  // namespace dcns

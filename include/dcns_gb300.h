@@ -109,6 +109,17 @@ int dcns_align_pairs(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, con
                      dcns_results **out);
 void dcns_results_free(dcns_results *res);
 
+/* The weighted drivers of weighted1Gap / weighted2Gaps (findSimilarFragmentsForPairedSequence_wighted_1gap,
+ * impl/findSimilarFragmentsForPairedSequence4.cpp:784, pieces = 1; findSimilarFragmentsForPairedSequence_wighted, :883,
+ * pieces = 2) for many pairs: the 2-gap x-seeds, then per x-seed the weighted reverse and forward DPs
+ * (impl/sequenceAlignment3.cpp:1483-1890) whose rows score with the category of their seq1 base.  weights: n1 category
+ * ids (0 .. n_cats-1) per pair, concatenated in pair order; cats: 7 int32 per category, as a Score folder file holds
+ * them (model/Score.cpp:3-60): match, mismatch, open1, ext1, open2, ext2, zdrop.  At most 64 categories.  The DP
+ * bandwidth is params->bandwidth; the z-drop of each row comes from its category. */
+int dcns_align_weighted(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, const int16_t *weights,
+                        const int32_t *cats, int32_t n_cats, int pieces, const dcns_params *params,
+                        dcns_results **out);
+
 /* The seeded 2-gap overload of cut2Gaps2 (impl/findSimilarFragmentsForPairedSequence4.cpp:624-745; the x-seeds come
  * from a SAM file, impl/samFileToSeeds.cpp) for many pairs: seeds are (start1, end1, start2, end2) quadruples,
  * 0-based inclusive, pair k owning seeds[4*seed_offset[k] .. 4*seed_offset[k+1]), in the caller's order.

@@ -371,6 +371,97 @@ void semiglobal(const int8_t *s1, int32_t n1, const int8_t *s2, int32_t n2, cons
 }
 
 // ---------------------------------------------------------------- seeds
+// ---------------------------------------------------------------- weighted semi-global (per-row categories)
+// One scoring category of the weighted variants (model/Score.cpp:3-60: a matrixList entry): match / mismatch (N
+// scores 0), both gap models and the z-drop.
+struct WCat {
+  int32_t match, mismatch, open1, ext1, open2, ext2, zdrop;
+};
+
+// SemiGlobal (impl/sequenceAlignment3.cpp:1483-1709, pieces = 2) and SemiGlobal_single_gap_penalty (:1710-1890,
+// pieces = 1).  Row i (1-based) scores with the category of weights[i-1]: substitution, the horizontal gap states and
+// the z-drop test; the vertical gap states it leaves for the next row use the category of weights[i].  Every band
+// column, the last included, updates the gap states and writes its code (F of the last column starts from OUT); an
+// empty band ends the DP.  weights must hold n1 + 1 entries: the caller repeats the final category where the
+// reference reads one past its array.  The bandwidth is P.bandwidth; the z-drop comes from the categories.
+void weighted_semiglobal(int pieces, const int8_t *s1, int32_t n1, const int8_t *s2, int32_t n2,
+                         const int16_t *weights, const WCat *cats, int32_t w, bool want_cigar, SgOut &o) {
+  BandStore T;
+  if (want_cigar) T.reset();
+  std::vector<int32_t> prev(std::max(n2, 0) + 1, OUT), cur(std::max(n2, 0) + 1, OUT);
+  std::vector<int32_t> F1(std::max(n2, 0) + 1, OUT), F2(std::max(n2, 0) + 1, OUT);
+  prev[0] = 0;
+  o.score = 0;
+  o.end1 = -1;
+  o.end2 = -1;
+  o.cells = 0;
+  for (int32_t i = 1; i <= n1; ++i) {
+    const WCat &rc = cats[weights[i - 1]], &nc = cats[weights[i]];
+    int32_t best = 0, bestj = pieces == 2 ? OUT : -1;
+    const int32_t c0 = std::max(i - w, 1), c1 = std::min(i + w, n2);
+    int32_t e1 = OUT, e2 = OUT;
+    if (c1 >= 0) F1[c1] = OUT, F2[c1] = OUT;
+    if (want_cigar) T.begin_row(i, c0);
+    for (int32_t j = c0; j <= c1; ++j) {
+      const int32_t sub = (s1[i - 1] == 2 || s2[j - 1] == 2) ? 0 : (s1[i - 1] == s2[j - 1] ? rc.match : rc.mismatch);
+      int32_t v = sub + prev[j - 1];
+      uint8_t d = 0;
+      if (!(v > F1[j])) d = 1, v = F1[j];
+      if (!(v > e1)) d = 2, v = e1;
+      if (pieces == 2) {
+        if (!(v > F2[j])) d = 3, v = F2[j];
+        if (!(v > e2)) d = 4, v = e2;
+      }
+      cur[j] = v;
+      if (v > best) best = v, bestj = j;
+      int32_t h = v + nc.open1, f = F1[j] + nc.ext1;
+      if (f >= h) d |= 1 << 3;
+      F1[j] = f >= h ? f : h;
+      h = v + rc.open1;
+      e1 += rc.ext1;
+      if (e1 >= h) d |= 1 << 4;
+      e1 = e1 >= h ? e1 : h;
+      if (pieces == 2) {
+        int32_t h2 = v + nc.open2, f2 = F2[j] + nc.ext2;
+        if (f2 >= h2) d |= 1 << 5;
+        F2[j] = f2 >= h2 ? f2 : h2;
+        h2 = v + rc.open2;
+        e2 += rc.ext2;
+        if (e2 >= h2) d |= 1 << 6;
+        e2 = e2 >= h2 ? e2 : h2;
+      }
+      if (want_cigar) T.push(i, d);
+    }
+    o.cells += std::max(c1 - c0 + 1, 0);
+    if (best > o.score) {
+      o.score = best;
+      o.end1 = i;
+      o.end2 = bestj;
+    }
+    if (pieces == 2) {
+      int32_t l = (i - o.end1) - (bestj - o.end2);
+      l = l > 0 ? l : -l;
+      if (o.score - best > rc.zdrop + l * rc.ext2) break;
+    } else if (o.score - best > rc.zdrop) {
+      break;
+    }
+    if (bestj <= 0) break;
+    std::swap(prev, cur);
+    prev[0] = OUT;
+    cur[0] = OUT;
+  }
+  o.cigar.clear();
+  if (want_cigar) {
+    int32_t ii = o.end1, jj = o.end2;
+    walk_codes(T, ii, jj, o.cigar);
+    while (ii > 0) cigar_push(o.cigar, 2), --ii;
+    while (jj > 0) cigar_push(o.cigar, 1), --jj;
+    std::reverse(o.cigar.begin(), o.cigar.end());
+  }
+  o.end1 -= 1;
+  o.end2 -= 1;
+}
+
 struct Seed4 {
   int32_t s1, e1, s2, e2;
 };
@@ -714,6 +805,48 @@ std::vector<Frag> seeded_two_piece(const Pair &pr, const Params &P, int32_t max_
   return out;
 }
 
+// The weighted drivers (findSimilarFragmentsForPairedSequence4.cpp:784-881 with pieces = 1, :883-975 with
+// pieces = 2): the 2-gap x-seeds, then per x-seed a weighted reverse DP from its end (reverse-complement weights),
+// the StartAlignment gate and a weighted forward DP with CIGAR; the 1-piece driver keeps a result without checking
+// its CIGAR or ends, the 2-piece one requires a CIGAR and positive ends.  wf / wr: the forward and reverse weights
+// of seq1, n1 + 1 entries each (the last repeating the final category).
+std::vector<Frag> weighted_stage(int pieces, const Pair &pr, const Params &P, const std::vector<Seed4> &xs,
+                                 const int16_t *wf, const int16_t *wr, const WCat *cats, Cells &cells) {
+  std::vector<Frag> out;
+  std::set<std::pair<int32_t, int32_t>> starts;
+  const double L1 = double(pr.n1), L2 = double(pr.n2);
+  for (const Seed4 &x : xs) {
+    const int32_t b1 = x.e1, b2 = x.e2;
+    SgOut r;
+    weighted_semiglobal(pieces, pr.rc1.data() + (pr.n1 - 1 - b1), 1 + b1, pr.rc2.data() + (pr.n2 - b2 - 1), b2 + 1,
+                        wr + (pr.n1 - 1 - b1), cats, P.bandwidth, false, r);
+    cells.semiglobal += r.cells;
+    const int32_t s1 = b1 - r.end1, s2 = b2 - r.end2;
+    if (!starts.insert({s1, s2}).second) continue;
+    SgOut f;
+    weighted_semiglobal(pieces, pr.s1 + s1, pr.n1 - s1, pr.s2 + s2, pr.n2 - s2, wf + s1, cats, P.bandwidth, true, f);
+    cells.semiglobal += f.cells;
+    if (pieces == 2 && !(f.cigar.size() > 0 && f.end1 > 0 && f.end2 > 0)) continue;
+    const int64_t e1 = (int64_t)f.end1 + s1, e2 = (int64_t)f.end2 + s2;
+    int toRemove = -1;
+    bool found = false;
+    for (int i = 0; i < (int)out.size(); ++i)
+      if (out[i].e1 == e1 + 1 && out[i].e2 == e2 + 1) {
+        found = true;
+        if (s1 + 1 < out[i].s1 && s2 + 1 < out[i].s2) toRemove = i;
+      }
+    if (found && toRemove < 0) continue;
+    double ev, pv;
+    evalue(P, L1, L2, f.score, ev, pv);
+    Frag fr{s1 + 1, e1 + 1, s2 + 1, e2 + 1, (int64_t)(uint32_t)f.score, f.cigar, pv, ev};
+    if (toRemove >= 0)
+      out[toRemove] = fr;
+    else
+      out.push_back(fr);
+  }
+  return out;
+}
+
 std::vector<Frag> find_2gap(const Pair &pr, const Params &P, Cells &cells) {
   Score sc{P.match, P.mismatch};
   std::vector<Seed4> xs = all_extend_seeds(pr, P, sc, cells);
@@ -878,6 +1011,29 @@ int or_find_seeded_2gap(const int8_t *s1, int32_t n1, const int8_t *s2, int32_t 
   for (int32_t k = 0; k < n_seeds; ++k) sd[k] = Seed4{seeds[4 * k], seeds[4 * k + 1], seeds[4 * k + 2], seeds[4 * k + 3]};
   Cells cells;
   std::vector<Frag> fr = seeded_two_piece(pr, P, max_align, sd, cells);
+  cells_out(cells, cells_o);
+  return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
+}
+
+// Weighted drivers.  weights: n1 category ids of seq1 (0 .. n_cats-1); cats: 7 ints per category (match, mismatch,
+// open1, ext1, open2, ext2, zdrop).  pieces 1 = the 1-gap weighted driver, 2 = the 2-gap one.
+int or_find_weighted(int pieces, const int8_t *s1, int32_t n1, const int8_t *s2, int32_t n2, const int16_t *weights,
+                     const int32_t *cats, int32_t n_cats, const int32_t *ip, const double *dp, int64_t *frag,
+                     double *pe, uint32_t *cigar, int frag_cap, int cigar_cap, int *n_cigar, int64_t *cells_o) {
+  Params P = params_from(ip, dp);
+  Pair pr{s1, s2, n1, n2, {}, {}};
+  pr.init();
+  std::vector<WCat> cv(n_cats);
+  for (int32_t k = 0; k < n_cats; ++k)
+    cv[k] = WCat{cats[7 * k], cats[7 * k + 1], cats[7 * k + 2], cats[7 * k + 3], cats[7 * k + 4], cats[7 * k + 5],
+                 cats[7 * k + 6]};
+  std::vector<int16_t> wf(n1 + 1), wr(n1 + 1);
+  for (int32_t i = 0; i < n1; ++i) wf[i] = weights[i], wr[i] = weights[n1 - 1 - i];
+  if (n1 > 0) wf[n1] = wf[n1 - 1], wr[n1] = wr[n1 - 1];
+  Cells cells;
+  Score sc{P.match, P.mismatch};
+  std::vector<Seed4> xs = all_extend_seeds(pr, P, sc, cells);
+  std::vector<Frag> fr = weighted_stage(pieces, pr, P, xs, wf.data(), wr.data(), cv.data(), cells);
   cells_out(cells, cells_o);
   return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
 }

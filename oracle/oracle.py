@@ -118,6 +118,8 @@ class Oracle(_Lib):
                                     I32P, U64P, I64P]
         L.or_sliding.argtypes = [I8P, C.c_int32, I8P, C.c_int32, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                  F64P, I32P, C.c_int]
+        L.or_find_weighted.argtypes = [C.c_int, I8P, C.c_int32, I8P, C.c_int32, C.POINTER(C.c_int16), I32P, C.c_int32,
+                                       I32P, F64P, I64P, F64P, U32P, C.c_int, C.c_int, I32P, I64P]
         L.or_find_seeded_2gap.argtypes = [I8P, C.c_int32, I8P, C.c_int32, I32P, C.c_int32, C.c_int32, I32P, F64P, I64P,
                                           F64P, U32P, C.c_int, C.c_int, I32P, I64P]
 
@@ -176,6 +178,26 @@ class Oracle(_Lib):
         assert n >= 0, "fragment buffer too small"
         return _unflatten(n, frag, pe, cg), dict(zip(("scan", "scan_rev", "xdrop", "semiglobal"), map(int, cells)))
 
+    def find_weighted(self, s1, s2, weights, cats, pieces=2, **kw):
+        """The weighted drivers: weights = category id per base of s1, cats = [(match, mismatch, open1, ext1, open2,
+        ext2, zdrop), ...]; pieces 1 = the 1-gap weighted driver, 2 = the 2-gap one."""
+        _, ip, dp = params(**kw)
+        s1, s2 = _i8(s1), _i8(s2)
+        wt = np.ascontiguousarray(weights, np.int16)
+        ct = np.ascontiguousarray(cats, np.int32).reshape(-1, 7)
+        fcap, ccap = 4096, 1 << 20
+        frag = np.zeros((fcap, 8), np.int64)
+        pe = np.zeros((fcap, 2), np.float64)
+        cg = np.zeros(ccap, np.uint32)
+        nc = np.zeros(1, np.int32)
+        cells = np.zeros(4, np.int64)
+        n = self.lib.or_find_weighted(pieces, _p(s1, I8P), len(s1), _p(s2, I8P), len(s2),
+                                      wt.ctypes.data_as(C.POINTER(C.c_int16)), _p(ct, I32P), len(ct), _p(ip, I32P),
+                                      _p(dp, F64P), _p(frag, I64P), _p(pe, F64P), _p(cg, U32P), fcap, ccap,
+                                      _p(nc, I32P), _p(cells, I64P))
+        assert n >= 0, "fragment buffer too small"
+        return _unflatten(n, frag, pe, cg)
+
     def find_seeded(self, s1, s2, seeds, max_align=20000, **kw):
         """The seeded 2-piece overload (cut2Gaps2): seeds = [(start1, end1, start2, end2)] 0-based, in order."""
         _, ip, dp = params(**kw)
@@ -227,6 +249,9 @@ class Reference(_Lib):
         L = self.lib
         L.ref_sw.argtypes = [I8P, C.c_int32, I8P, C.c_int32, C.c_int, C.c_int, C.c_int, C.c_int, I32P]
         L.ref_sw_scalar.argtypes = L.ref_sw.argtypes
+        L.ref_find_weighted.argtypes = [C.c_int, I8P, C.c_int32, I8P, C.c_int32, C.POINTER(C.c_int16), I32P,
+                                        C.c_int32, C.c_char_p] + [C.c_int] * 7 + [C.c_double] * 3 + \
+            [C.c_int] * 4 + [I64P, F64P, U32P, C.c_int, C.c_int, I32P]
         L.ref_find_seeded_2gap.argtypes = [I8P, C.c_int32, I8P, C.c_int32, I32P, C.c_int32, C.c_int32] + \
             [C.c_int] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int, I64P, F64P, U32P, C.c_int, C.c_int, I32P]
         L.ref_xextend.argtypes = [I8P, C.c_int32, I8P, C.c_int32, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
@@ -312,6 +337,27 @@ class Reference(_Lib):
                                        d["open1"], d["ext1"], d["match"], d["mismatch"], d["step"], d["pvalue"],
                                        d["lambda_"], d["kvalue"], d["w"], d["xdrop"], _p(frag, I64P), _p(pe, F64P),
                                        _p(cg, U32P), fcap, ccap, _p(nc, I32P))
+        assert n >= 0, "fragment buffer too small"
+        return _unflatten(n, frag, pe, cg)
+
+    def find_weighted(self, s1, s2, weights, cats, pieces=2, **kw):
+        import tempfile
+        d, _, _ = params(**kw)
+        s1, s2 = _i8(s1), _i8(s2)
+        wt = np.ascontiguousarray(weights, np.int16)
+        ct = np.ascontiguousarray(cats, np.int32).reshape(-1, 7)
+        fcap, ccap = 4096, 1 << 20
+        frag = np.zeros((fcap, 8), np.int64)
+        pe = np.zeros((fcap, 2), np.float64)
+        cg = np.zeros(ccap, np.uint32)
+        nc = np.zeros(1, np.int32)
+        with tempfile.TemporaryDirectory() as sd:
+            n = self.lib.ref_find_weighted(pieces, _p(s1, I8P), len(s1), _p(s2, I8P), len(s2),
+                                           wt.ctypes.data_as(C.POINTER(C.c_int16)), _p(ct, I32P), len(ct),
+                                           sd.encode(), d["window"], d["min_score"], d["open1"], d["ext1"],
+                                           d["match"], d["mismatch"], d["step"], d["pvalue"], d["lambda_"],
+                                           d["kvalue"], d["zdrop"], d["bandwidth"], d["w"], d["xdrop"],
+                                           _p(frag, I64P), _p(pe, F64P), _p(cg, U32P), fcap, ccap, _p(nc, I32P))
         assert n >= 0, "fragment buffer too small"
         return _unflatten(n, frag, pe, cg)
 

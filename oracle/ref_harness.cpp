@@ -10,6 +10,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <fstream>
 #include <iostream>
 #include <set>
 #include <sstream>
@@ -17,6 +18,7 @@
 #include <vector>
 
 #include "impl/findSimilarFragmentsForPairedSequence.h"
+#include "model/Score.h"
 #include "impl/sequenceAlignment.h"
 #include "impl/slidingWindowAlignment.h"
 
@@ -278,6 +280,49 @@ int ref_find_seeded_2gap(const int8_t *s1, int32_t L1, const int8_t *s2, int32_t
     fr = findSimilarFragmentsForPairedSequence(a.data(), ar.data(), b.data(), br.data(), l1, l2, win, open1, ext1,
                                                open2, ext2, match, mismatch, m, str1, str2, pvalue, lambda, kvalue,
                                                zdrop, bandwidth, sd, T, mal);
+  }
+  return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
+}
+
+// The weighted drivers, impl/findSimilarFragmentsForPairedSequence4.cpp:784 (pieces 1) and :883 (pieces 2).  The
+// categories are written as a Score folder (matrixList + one 7-line file per category, model/Score.cpp:3) under
+// score_dir.  The weight arrays get one extra entry on each side repeating the end categories, so the reference's
+// reads one before and one past them (at the first and last row) see defined values.
+int ref_find_weighted(int pieces, const int8_t *s1, int32_t L1, const int8_t *s2, int32_t L2, const int16_t *weights,
+                      const int32_t *cats, int32_t n_cats, const char *score_dir, int window, int min_score, int open1,
+                      int ext1, int match, int mismatch, int step, double pvalue, double lambda, double kvalue,
+                      int zdrop, int bandwidth, int w, int xdrop, int64_t *frag, double *pe, uint32_t *cigar,
+                      int frag_cap, int cigar_cap, int *n_cigar) {
+  {
+    std::ofstream list(std::string(score_dir) + "/matrixList");
+    for (int32_t k = 0; k < n_cats; ++k) {
+      list << k << "\n";
+      std::ofstream f(std::string(score_dir) + "/" + std::to_string(k));
+      for (int q = 0; q < 7; ++q) f << cats[7 * k + q] << "\n";
+    }
+  }
+  Score score(score_dir);
+  Scorei m((int8_t)match, (int8_t)mismatch);
+  std::vector<int8_t> a = copyseq(s1, L1), b = copyseq(s2, L2);
+  std::vector<int8_t> ar = revcomp(s1, L1), br = revcomp(s2, L2);
+  std::vector<int16_t> wf(L1 + 2), wr(L1 + 2);
+  for (int32_t i = 0; i < L1; ++i) wf[i + 1] = weights[i], wr[i + 1] = weights[L1 - 1 - i];
+  if (L1 > 0) wf[0] = wf[1], wf[L1 + 1] = wf[L1], wr[0] = wr[1], wr[L1 + 1] = wr[L1];
+  int32_t l1 = L1, l2 = L2, win = window, mbd = 0, ww = w;
+  std::string str1, str2;
+  std::vector<PairedSimilarFragment> fr;
+  {
+    Silence quiet;
+    if (pieces == 1)
+      fr = findSimilarFragmentsForPairedSequence_wighted_1gap(a.data(), ar.data(), b.data(), br.data(), l1, l2, win,
+                                                              min_score, mbd, open1, ext1, match, mismatch, m, step,
+                                                              str1, str2, pvalue, lambda, kvalue, zdrop, bandwidth,
+                                                              ww, xdrop, score, wf.data() + 1, wr.data() + 1);
+    else
+      fr = findSimilarFragmentsForPairedSequence_wighted(a.data(), ar.data(), b.data(), br.data(), l1, l2, win,
+                                                         min_score, mbd, open1, ext1, match, mismatch, m, step, str1,
+                                                         str2, pvalue, lambda, kvalue, zdrop, bandwidth, ww, xdrop,
+                                                         score, wf.data() + 1, wr.data() + 1);
   }
   return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
 }

@@ -357,3 +357,16 @@ def test_seeded_two_gap_vs_oracle(eng, oracle, max_align):
     for k, (A, B, seeds) in enumerate(cases):
         exp = oracle.find_seeded(A, B, seeds, max_align if max_align > 0 else 1 << 30)
         assert_same_fragments(got[k], exp, k)
+
+
+@pytest.mark.parametrize("pieces,bandwidth", [(1, 20000), (2, 20000), (2, 30), (1, 30)])
+def test_weighted_drivers_vs_oracle(eng, oracle, pieces, bandwidth):
+    """weighted1Gap / weighted2Gaps: per-row categories (substitution, gap models, z-drop), one warp per DP."""
+    from test_oracle_pin import WEIGHT_CATS, _weighted_cases
+
+    cases = _weighted_cases(n=5, seed=11)
+    got = eng.align_weighted([(A, B) for A, B, _ in cases], [w for _, _, w in cases], WEIGHT_CATS, pieces,
+                             bandwidth=bandwidth)
+    for k, (A, B, wts) in enumerate(cases):
+        exp = oracle.find_weighted(A, B, wts, WEIGHT_CATS, pieces, bandwidth=bandwidth)
+        assert_same_fragments(got[k], exp, k)

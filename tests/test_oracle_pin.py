@@ -161,3 +161,41 @@ def test_seeded_two_gap_matches_reference(oracle, reference):
                 assert abs(x.pvalue - y.pvalue) <= 1e-12 * max(1.0, abs(y.pvalue))
             n += len(got)
     assert n > 20
+
+
+WEIGHT_CATS = [(2, -3, -4, -2, -45, 0, 100), (3, -4, -6, -2, -60, -1, 50), (1, -2, -3, -1, -30, 0, 200)]
+
+
+def _weighted_cases(n=6, seed=3):
+    """Masked-free planted pairs with categories in runs along seq1 (as GFF annotations give them)."""
+    import numpy as np
+    from dcns_gb300 import workloads as W
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        a, b = W.planted_pair(rng, 2500, 2600, 12, 60, 300, 0.85, 0.97, 0.01, 0.0)
+        A, B = W.prepare(a), W.prepare(b)
+        wts = np.zeros(len(A), np.int16)
+        pos = 0
+        while pos < len(A):
+            L = int(rng.integers(50, 600))
+            wts[pos:pos + L] = int(rng.integers(0, len(WEIGHT_CATS)))
+            pos += L
+        out.append((A, B, wts))
+    return out
+
+
+def test_weighted_drivers_match_reference(oracle, reference):
+    """findSimilarFragmentsForPairedSequence_wighted_1gap / _wighted (per-row categories, 1- and 2-piece)."""
+    if reference is None:
+        pytest.skip("reference not built on this host")
+    n = 0
+    for A, B, wts in _weighted_cases():
+        for pieces in (1, 2):
+            for bw in (20000, 30):
+                got = oracle.find_weighted(A, B, wts, WEIGHT_CATS, pieces, bandwidth=bw)
+                exp = reference.find_weighted(A, B, wts, WEIGHT_CATS, pieces, bandwidth=bw)
+                assert [f.key() for f in got] == [f.key() for f in exp], (pieces, bw)
+                n += len(got)
+    assert n > 30
