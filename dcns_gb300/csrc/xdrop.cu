@@ -415,11 +415,13 @@ void launch_xdrop_iota(int *list, int n, int *count, cudaStream_t st) {
 void launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
                         int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, Arena ar,
                         Params p, uint32_t *tb, int w, int n_bound, int nsm, int32_t *scratch, int64_t per_warp,
-                        int warps, cudaStream_t st) {
+                        int warps, int warp_from, cudaStream_t st) {
   if (n_bound <= 0) return;
   const XLevelArgs L{tasks, list_in, count_in, list_out, count_out, retry, retry_count, tb_cursor, tb_words};
   const int g = (int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * 16);
-  if (w <= 10)
+  if (w > warp_from)
+    xdrop_level_warp_kernel<<<(warps + 3) / 4, 128, 0, st>>>(L, ar, p, tb, scratch, per_warp);
+  else if (w <= 10)
     xdrop_level_kernel<10><<<g, 128, 0, st>>>(L, ar, p, tb);
   else if (w <= 20)
     xdrop_level_kernel<20><<<g, 128, 0, st>>>(L, ar, p, tb);
