@@ -33,7 +33,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "GCUPS & pairs/s, batched vs per-pair launch on 1 GB300, bit-exact; p99 latency"
-WORKLOAD = "batched seed scan + extension: 10,000 pairs, log-normal 0.5-20 kb (cut1Gap path)"
+
+
+def workload_name(n, mode):
+    path = "cut1Gap" if mode == 1 else "cut2Gaps"
+    return f"batched seed scan + extension: {n:,} pairs, log-normal 0.5-20 kb ({path} path)"
 
 
 def parse():
@@ -101,9 +105,9 @@ def workload(n_pairs, rank=0):
     return W.config2(n_pairs=n_pairs, seed=shard_seed(rank))
 
 
-# DRAM bytes per algorithmic cell of the level-0 scan launch: ncu, 3,000 pairs of this workload, 18.15 MB read and 0
+# DRAM bytes per algorithmic cell of the level-0 scan launch: ncu, 3,000 pairs of this workload, 18.51 MB read and 0
 # written for 161.25 G cells (profiles/scan_kernel_config2_3000pairs.md); traffic grows with the cells.
-SCAN_DRAM_BYTES_PER_CELL = 18.152192e6 / 161254407231
+SCAN_DRAM_BYTES_PER_CELL = 18.51392e6 / 161254407231
 
 
 def level0_cells(pairs, window=38, step=8):
@@ -133,11 +137,18 @@ def cpu_baseline(pairs, mode, target_s, threads=None):
     orc.find_batch(probe, two_gap=(mode == 2), threads=threads)
     dt = max(time.perf_counter() - t, 1e-3)
     n = int(min(len(pairs), max(len(probe), len(probe) * target_s / dt)))
-    sample = pairs[:n]
-    t = time.perf_counter()
-    _, _, cells = orc.find_batch(sample, two_gap=(mode == 2), threads=threads)
-    dt = time.perf_counter() - t
-    tot = cells["scan"] + cells["scan_rev"] + cells["xdrop"] + cells["semiglobal"]
+    # the probe's first pairs need not be typical: keep adding chunks of the workload in order until the sample
+    # has run for about target_s
+    done, tot, dt = 0, 0, 0.0
+    while True:
+        t = time.perf_counter()
+        _, _, cells = orc.find_batch(pairs[done:n], two_gap=(mode == 2), threads=threads)
+        dt += time.perf_counter() - t
+        tot += cells["scan"] + cells["scan_rev"] + cells["xdrop"] + cells["semiglobal"]
+        done = n
+        if dt >= 0.8 * target_s or n >= len(pairs):
+            break
+        n = int(min(len(pairs), n + max(threads, n / dt * (target_s - dt))))
     return {"value": tot / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port",
             "pairs_per_s": n / dt, "seconds": dt,
             "sample": f"first {n} of {len(pairs)} pairs of the same workload, {threads} threads"}
@@ -160,7 +171,7 @@ def run_reference(args, rank, world):
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1000 * statistics.median(s["seconds"] for s in steps), 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "mode": args.mode, "pairs": args.pairs,
+            "data": "synthetic (seeded)", "config": {"workload": workload_name(args.pairs, args.mode), "mode": args.mode, "pairs": args.pairs,
                                                     "l2": "cpu"},
             "pairs_per_s": round(statistics.median(s["pairs_per_s"] for s in steps), 2),
             "cpu_baseline": cb, "e2e": {"value": round(val, 4), "unit": "GCUPS", "h2d_bytes_per_step": 0,
@@ -270,6 +281,7 @@ def main():
                 "traffic": round(SCAN_DRAM_BYTES_PER_CELL * level0_cells(pairs) / 1e9, 4) if args.mode == 1 else None,
                 "traffic_unit": "GB per level-0 launch (ncu bytes per cell x this batch's level-0 cells)",
                 "scan_share_of_single_lane_step": round(scan_ms / single_ms, 4),
+                "single_lane_ms_per_step": round(single_ms / 2, 2),
                 "timing": "CUDA events around each scan launch, two single-lane steps after the timed region"}
 
     extras = {}
@@ -325,7 +337,7 @@ def main():
         "metric": METRIC, "value": round(gcups, 3), "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": round(tot_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int16x2 (seed scan) / int32", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "pairs": n, "mode": args.mode, "parallelism": f"replicas x{world}",
+        "config": {"workload": workload_name(n, args.mode), "pairs": n, "mode": args.mode, "parallelism": f"replicas x{world}",
                    "l2": "flushed (256 MB write) between timed steps", "pipeline": tuned},
         "pairs_per_s": round(pairs_s, 2), "fragments": nfrag,
         "e2e": {"value": round(e2e_all_cells / (e2e_tot * 1e-3) / 1e9, 3), "unit": "GCUPS",
