@@ -331,6 +331,11 @@ def main():
 
         extras["serving"] = serve(2000.0, pairs[:1500], 3)
         extras["serving_high_rate"] = serve(20000.0, pairs[:4000], 4)
+        # the serving workload's own request shapes: a long tail of 50-100 kb requests among short ones
+        from dcns_gb300 import workloads as W
+        extras["serving_long_tail"] = {
+            "workload": "1,200 requests: log-normal median 4 kb, sigma 1.0, 0.2-100 kb, 10 % of 50-100 kb",
+            **serve(1000.0, W.config5(n_requests=1200), 5)}
 
     cb = cpu_baseline(pairs, args.mode, args.cpu_seconds)
     line = {

@@ -323,6 +323,7 @@ bool striped_for_host(int nref, int nread, int open, int ext, int match) {
 // ------------------------------------------------------------------ 1. upload + pack
 void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, DevBuf &d_nm, DevBuf &d_sb,
                  std::vector<int64_t> &seq_base, Arena &arena) {
+  auto tp = Clock::now();
   const int64_t np = (int64_t)pairs.size(), ns = 2 * np;
   seq_base.assign(ns, 0);
   std::vector<int64_t> src_off(ns);
@@ -354,6 +355,7 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
     }
   }
   total_dst += 128;  // lets every kernel read one 64-base block past any sequence end
+  tp = phase(C, "up_index", tp);
   C.h_codes.ensure((size_t)std::max<int64_t>(total_src, 1));
   int8_t *stage = C.h_codes.as<int8_t>();
   // staged copy; the reference indexes its 5x5 score table with the codes, so anything outside 0..4 is rejected
@@ -369,6 +371,7 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
     if (bad) badcode = true;
   });
   if (badcode) throw Error(DCNS_ERR_INVALID, "sequence codes must be dCNS codes 0..4 (A C N G T)");
+  tp = phase(C, "up_stage", tp);
   C.d_codes.ensure(C, (size_t)std::max<int64_t>(total_src, 1));
   C.d_srcoff.ensure(C, sizeof(int64_t) * ns + 8);
   C.d_dstbase.ensure(C, sizeof(int64_t) * ns + 8);
@@ -389,6 +392,7 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
   C.stats.kernel_launches += 1;
   arena.pk = d_pk.as<uint32_t>();
   arena.nm = d_nm.as<uint32_t>();
+  phase(C, "up_enqueue", tp);
 }
 
 // Uploads into the context's own buffers and makes them the current arena.
@@ -1825,6 +1829,7 @@ void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, 
   auto tu = Clock::now();
   upload(C, pairs);
   C.stats.ms_upload = ms_since(tu);
+  print_phases(C, "upload");
   align_core(C, pairs, P, mode, out);
   C.stats.ms_total = ms_since(t0);
 }

@@ -165,6 +165,26 @@ def config4(n_seeds: int = 1000000, seed: int = 20261207):
     return out
 
 
+def config5(n_requests: int = 2000, seed: int = 20261208, long_frac: float = 0.10):
+    """Serving requests: lengths log-normal (median 4 kb, sigma 1.0) clipped to 200 bp-100 kb, drawn independently for
+    both sequences, except that a `long_frac` share of the requests (chosen at random) draws both from U(50, 100] kb:
+    the log-normal alone puts well under 1 % above 50 kb, and the serving configuration fixes 10 %.  Planted 30-300 bp
+    segments at U(70, 95) % identity, Poisson(8) per 3 kb of the shorter sequence (capped at 300), 1 % indels, 15 %
+    masked runs.  Arrival times are drawn by the caller (a Poisson process at the configured rate)."""
+    rng = np.random.default_rng(seed)
+    n1 = lognormal_lengths(rng, n_requests, 4000, 1.0, 200, 100000)
+    n2 = lognormal_lengths(rng, n_requests, 4000, 1.0, 200, 100000)
+    long = rng.random(n_requests) < long_frac
+    n1[long] = rng.integers(50001, 100001, int(long.sum()))
+    n2[long] = rng.integers(50001, 100001, int(long.sum()))
+    out = []
+    for k in range(n_requests):
+        nseg = min(int(rng.poisson(8.0 * min(n1[k], n2[k]) / 3000.0)), 300)
+        a, b = planted_pair(rng, int(n1[k]), int(n2[k]), nseg, 30, 300, 0.70, 0.95, 0.01, 0.15)
+        out.append((prepare(a), prepare(b)))
+    return out
+
+
 def random_pair(rng, n1, n2, alphabet=5):
     """Uniform codes over {0..alphabet-1} (alphabet=5 includes N=2) for exhaustive/edge tests."""
     return (rng.integers(0, alphabet, size=n1).astype(np.int8), rng.integers(0, alphabet, size=n2).astype(np.int8))

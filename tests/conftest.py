@@ -9,6 +9,10 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden", "golden.npz")
+GOLDEN_DIR = os.path.join(ROOT, "tests", "golden")
+if GOLDEN_DIR not in sys.path:
+    sys.path.insert(0, GOLDEN_DIR)
+CONFIGS = os.path.join(GOLDEN_DIR, "configs.npz")
 
 
 def pytest_configure(config):
@@ -36,6 +40,12 @@ def reference():
 @pytest.fixture(scope="session")
 def golden():
     return np.load(GOLDEN)
+
+
+@pytest.fixture(scope="session")
+def configs():
+    """Digests of the reference's outputs on the benchmark workloads (tests/golden/make_config_golden.py)."""
+    return np.load(CONFIGS)
 
 
 def ragged(z, name, i):
