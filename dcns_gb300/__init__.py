@@ -107,7 +107,7 @@ class Stats(C.Structure):
                                           "ms_download", "ms_total", "ms_scan_kernel", "ms_scan_prep",
                                           "ms_scan_xfer", "ms_link")] + \
                [("scan_launches", C.c_int32), ("kernel_launches", C.c_int32), ("scan_rounds", C.c_int32),
-                ("xdrop_rounds", C.c_int32), ("ms_xdrop_kernel", C.c_double)]
+                ("xdrop_rounds", C.c_int32), ("ms_xdrop_kernel", C.c_double), ("bytes_h2d", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

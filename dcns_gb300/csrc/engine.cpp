@@ -332,6 +332,7 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
   // A sequence passed for several pairs (the same pointer and length: one reference against many queries, as in the
   // multi-species caller) is staged and packed once; the later pairs point at the first copy.
   std::unordered_map<const int8_t *, std::pair<int32_t, int64_t>> seen;
+  seen.reserve((size_t)ns);
   for (int64_t k = 0; k < np; ++k) {
     for (int h = 0; h < 2; ++h) {
       const int32_t n = h ? pairs[k].n2 : pairs[k].n1;
@@ -385,6 +386,7 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
   h2d(C, C.d_dstbase, seq_base.data(), ns);
   h2d(C, C.d_len, len.data(), ns);
   h2d(C, d_sb, seq_base.data(), ns);
+  C.stats.bytes_h2d += total_src + (int64_t)ns * (8 + 8 + 4 + 8);
   DCNS_CK(cudaMemsetAsync(d_pk.p, 0, sizeof(uint32_t) * (total_dst / 16), C.st));
   DCNS_CK(cudaMemsetAsync(d_nm.p, 0, sizeof(uint32_t) * (total_dst / 32), C.st));
   launch_pack(C.d_codes.as<int8_t>(), C.d_srcoff.as<int64_t>(), C.d_dstbase.as<int64_t>(), C.d_len.as<int32_t>(),
@@ -1897,6 +1899,7 @@ void add_stats(dcns_stats &a, const dcns_stats &b) {
   a.ms_scan_xfer += b.ms_scan_xfer, a.ms_link += b.ms_link, a.scan_launches += b.scan_launches;
   a.kernel_launches += b.kernel_launches, a.scan_rounds += b.scan_rounds, a.xdrop_rounds += b.xdrop_rounds;
   a.ms_xdrop_kernel += b.ms_xdrop_kernel;
+  a.bytes_h2d += b.bytes_h2d;
 }
 
 // Batches large enough to fill the GPU several times over are split into bins of similar work (pairs dealt

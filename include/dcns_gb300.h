@@ -82,6 +82,7 @@ typedef struct {
   int32_t scan_rounds;     /* seed-scan launches rounds (level 0 + recursion levels), summed over lanes */
   int32_t xdrop_rounds;    /* x-drop launch rounds (band restarts), summed over lanes */
   double ms_xdrop_kernel;  /* device: x-drop pass kernels, CUDA events */
+  int64_t bytes_h2d;       /* host-to-device bytes of the sequence upload (codes and per-sequence offsets) */
 } dcns_stats;
 
 /* Results of one dcns_align_pairs call; owned by the library until dcns_results_free. */
