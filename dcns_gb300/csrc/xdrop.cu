@@ -21,124 +21,234 @@ namespace dcns {
 
 __device__ __forceinline__ int xd_words_per_row(int w) { return (2 * w + 1 + 7) / 8; }
 
+// One pass on the register path (band capacity WC: w <= WC), advanced a row at a time.  The band arrays stay with the
+// caller (locals: registers).
 template <int WC>
-__device__ void xdrop_pass(XTask &T, const Arena &ar, const Params &P, uint32_t *__restrict__ tb, int32_t *Ms,
-                           int32_t *Fs) {
-  const int w = T.w, n1 = T.n1, n2 = T.n2;
-  const int open = P.open1, ext = P.ext1;
-  const SeqView s1{T.base1, T.a1, T.dir}, s2{T.base2, T.a2, T.dir};
-  constexpr int NA = WC > 0 ? 2 * WC + 2 : 1;
-  int32_t Mr[NA], Fr[NA];
-  int32_t *M = WC > 0 ? Mr : Ms;
-  int32_t *F = WC > 0 ? Fr : Fs;
-  const int nk = 2 * w + 1;
-  if (WC > 0) {
+struct XBand {
+  static constexpr int NA = 2 * WC + 2, NK = 2 * WC + 1, NQ = (2 * WC + 1 + 15) / 16;
+};
+
+struct XPassScalars {
+  SeqView s1, s2;
+  int64_t tb_off;
+  int32_t n1, n2, w, nk, wpr, tb_cap, i, score, e1, e2, rows;
+  bool codes;
+};
+
+// M, F: the band of the row above, diagonal-relative; qw: query codes under the band, 4 bits per band cell k
+// (column j = i - w + k).
+template <int WC>
+__device__ __forceinline__ void xd_begin(XPassScalars &x, int32_t (&M)[XBand<WC>::NA], int32_t (&F)[XBand<WC>::NA],
+                                         uint64_t (&qw)[XBand<WC>::NQ], const XTask &T, const Arena &ar) {
+  constexpr int NA = XBand<WC>::NA, NK = XBand<WC>::NK, NQ = XBand<WC>::NQ;
+  x.n1 = T.n1, x.n2 = T.n2, x.w = T.w, x.nk = 2 * T.w + 1, x.wpr = xd_words_per_row(T.w);
+  x.codes = T.want_codes != 0, x.tb_off = T.tb_off, x.tb_cap = T.tb_cap;
+  x.s1 = SeqView{T.base1, T.a1, T.dir}, x.s2 = SeqView{T.base2, T.a2, T.dir};
+  x.score = x.e1 = x.e2 = x.rows = 0;
+  x.i = 1;
 #pragma unroll
-    for (int k = 0; k < NA; ++k) Mr[k] = kOut, Fr[k] = kOut;
-  } else {
-    for (int k = 0; k < nk + 1; ++k) M[k] = kOut, F[k] = kOut;
+  for (int k = 0; k < NA; ++k) M[k] = kOut, F[k] = kOut;
+#pragma unroll
+  for (int u = 0; u < NQ; ++u) qw[u] = 0;
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int j = 1 - x.w + k;
+    if (k < x.nk && j >= 1 && j <= x.n2) qw[k >> 4] |= (uint64_t)x.s2.at(ar, j - 1) << (4 * (k & 15));
   }
-  const int wpr = xd_words_per_row(w);
-  int score = 0, e1 = 0, e2 = 0, rows = 0;
-  T.status = 0;
-  // Register path: the query codes under the band, 4 bits per band cell k (column j = i - w + k), shifted one cell
-  // per row, so each row loads one new code instead of one per cell.
-  constexpr int NQ = WC > 0 ? (2 * WC + 1 + 15) / 16 : 1;
-  uint64_t qw[NQ];
+}
+
+// Row x.i.  Returns -1 to go on, 0 done, 1 band-edge restart, 2 traceback slot too small.
+//
+// The cells are the reference's, with the row's serial chain cut to one add-max per cell: with A = max(s + diag,
+// F above) (the first two comparisons), the e update e' = max(e + ext, max(A, e) + open) equals max(e + g, A + open),
+// g = max(ext, open), whether A > e or not.  Every A comes from the row above, so the chain waits on nothing else; M,
+// F, the codes and the row maximum then follow per cell with the reference's comparisons and tie rules.
+template <int WC>
+__device__ __forceinline__ int xd_row(XPassScalars &x, int32_t (&M)[XBand<WC>::NA], int32_t (&F)[XBand<WC>::NA],
+                                      uint64_t (&qw)[XBand<WC>::NQ], const Arena &ar, const Params &P,
+                                      uint32_t *__restrict__ tb) {
+  constexpr int NK = XBand<WC>::NK, NQ = XBand<WC>::NQ;
+  const int i = x.i, w = x.w, nk = x.nk, n2 = x.n2;
+  if (i > x.n1) return 0;
+  const int c0 = max(i - w, 1), c1 = min(i + w, n2);
+  if (x.codes && (int64_t)i * x.wpr > x.tb_cap) return 2;
+  const int open = P.open1, ext = P.ext1, g = ext > open ? ext : open;
+  const int ci = x.s1.at(ar, i - 1);
+  int best = 0, bestj = -1;
+  int32_t A[NK], E[NK];
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int j = i - w + k;
+    const int cj = (int)((qw[k >> 4] >> (4 * (k & 15))) & 15u);
+    const int32_t diag = (j == 1) ? (i == 1 ? 0 : kOut) : M[k];
+    const int32_t fin = (j == c1) ? kOut : F[k + 1];
+    const int32_t v = score_of(ci, cj, P.match, P.mismatch) + diag;
+    A[k] = v > fin ? v : fin;
+  }
+  int32_t ec = kOut;
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    E[k] = ec;
+    const int j = i - w + k;
+    if (k < nk && j >= c0 && j <= c1) ec = max(ec + g, A[k] + open);
+  }
+  uint32_t cw = 0;
+  int kw = 0;
+  uint32_t *row_codes = tb + x.tb_off + (int64_t)(i - 1) * x.wpr;
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int j = i - w + k;
+    uint32_t nib = 0xFu;
+    if (k < nk && j >= c0 && j <= c1) {
+      // M[k] and F[k + 1] still hold the row above here
+      const int cj = (int)((qw[k >> 4] >> (4 * (k & 15))) & 15u);
+      const int32_t diag = (j == 1) ? (i == 1 ? 0 : kOut) : M[k];
+      const int32_t fin = (j == c1) ? kOut : F[k + 1];
+      const bool ge = !(A[k] > E[k]);  // the horizontal gap wins ties
+      const int32_t v = ge ? E[k] : A[k];
+      uint32_t d = ge ? 2u : (score_of(ci, cj, P.match, P.mismatch) + diag > fin ? 0u : 1u);
+      M[k] = v;
+      if (v > best) {
+        best = v;
+        bestj = j;
+      }
+      const int32_t h = v + open;
+      const int32_t f = fin + ext;
+      if (f >= h) d |= 4u;
+      F[k] = f >= h ? f : h;
+      if (E[k] + ext >= h) d |= 8u;
+      nib = d;
+    }
+    if (x.codes && k < nk) {
+      cw |= nib << (4 * (k & 7));
+      if ((k & 7) == 7 || k == nk - 1) {
+        row_codes[kw++] = cw;
+        cw = 0;
+      }
+    }
+  }
+  // next row's band starts one column to the right: drop cell 0, append column (i + 1) + w
+#pragma unroll
+  for (int u = 0; u < NQ; ++u) qw[u] = (qw[u] >> 4) | (u + 1 < NQ ? qw[u + 1] << 60 : 0ull);
+  const int jn = i + 1 + w;
+  if (jn <= n2) {
+    const int kl = nk - 1;
+#pragma unroll
+    for (int u = 0; u < NQ; ++u)
+      if (u == (kl >> 4)) qw[u] |= (uint64_t)x.s2.at(ar, jn - 1) << (4 * (kl & 15));
+  }
+  x.rows = i;
+  if (bestj != n2 && bestj != 1 && (bestj == c0 || bestj == c1)) return 1;
+  if (best > x.score) {
+    x.score = best;
+    x.e1 = i;
+    x.e2 = bestj;
+  }
+  if (x.score - best > P.xdrop) return 0;
+  if (best <= 0) return 0;
+  x.i = i + 1;
+  return -1;
+}
+
+__device__ __forceinline__ void xd_finish(const XPassScalars &x, XTask &T, int status) {
+  T.status = status;
+  T.rows = x.rows;
+  if (status == 0) {
+    T.score = x.score;
+    T.end1 = x.e1;
+    T.end2 = x.e2;
+  }
+}
+
+template <int WC>
+__device__ void xdrop_pass(XTask &T, const Arena &ar, const Params &P, uint32_t *__restrict__ tb, int32_t *M,
+                           int32_t *F) {
   if constexpr (WC > 0) {
-#pragma unroll
-    for (int u = 0; u < NQ; ++u) qw[u] = 0;
-#pragma unroll
-    for (int k = 0; k < 2 * WC + 1; ++k) {
-      const int j = 1 - w + k;
-      if (k < nk && j >= 1 && j <= n2) qw[k >> 4] |= (uint64_t)s2.at(ar, j - 1) << (4 * (k & 15));
+    XPassScalars x;
+    int32_t Mr[XBand<WC>::NA], Fr[XBand<WC>::NA];
+    uint64_t qw[XBand<WC>::NQ];
+    xd_begin<WC>(x, Mr, Fr, qw, T, ar);
+    int st;
+    while ((st = xd_row<WC>(x, Mr, Fr, qw, ar, P, tb)) < 0) {
     }
-  }
-  for (int i = 1; i <= n1; ++i) {
-    const int c0 = max(i - w, 1), c1 = min(i + w, n2);
-    if (T.want_codes && (int64_t)i * wpr > T.tb_cap) {
-      T.status = 2;
-      T.rows = rows;
-      return;
-    }
-    const int ci = s1.at(ar, i - 1);
-    int best = 0, bestj = -1, e = kOut;
-    uint32_t cw = 0;
-    int kw = 0;
-    uint32_t *row_codes = tb + T.tb_off + (int64_t)(i - 1) * wpr;
-    auto cell = [&](int32_t *Mv, int32_t *Fv, int k, int cj) {
-      const int j = i - w + k;
-      uint32_t nib = 0xFu;
-      if (j >= c0 && j <= c1) {
-        const int32_t diag = (j == 1) ? (i == 1 ? 0 : kOut) : Mv[k];
-        const int32_t fin = (j == c1) ? kOut : Fv[k + 1];
-        int32_t v = score_of(ci, cj, P.match, P.mismatch) + diag;
-        uint32_t d = v > fin ? 0u : 1u;
-        if (!(v > fin)) v = fin;
-        if (!(v > e)) {
-          d = 2u;
-          v = e;
-        }
-        Mv[k] = v;
-        if (v > best) {
-          best = v;
-          bestj = j;
-        }
-        const int32_t h = v + open;
-        const int32_t f = fin + ext;
-        if (f >= h) d |= 4u;
-        Fv[k] = f >= h ? f : h;
-        e += ext;
-        if (e >= h) d |= 8u;
-        e = e >= h ? e : h;
-        nib = d;
+    xd_finish(x, T, st);
+  } else {
+    // wide band in per-thread global scratch (M, F: 2w + 2 ints each)
+    const int w = T.w, n1 = T.n1, n2 = T.n2;
+    const int open = P.open1, ext = P.ext1;
+    const SeqView s1{T.base1, T.a1, T.dir}, s2{T.base2, T.a2, T.dir};
+    const int nk = 2 * w + 1;
+    for (int k = 0; k < nk + 1; ++k) M[k] = kOut, F[k] = kOut;
+    const int wpr = xd_words_per_row(w);
+    int score = 0, e1 = 0, e2 = 0, rows = 0;
+    T.status = 0;
+    for (int i = 1; i <= n1; ++i) {
+      const int c0 = max(i - w, 1), c1 = min(i + w, n2);
+      if (T.want_codes && (int64_t)i * wpr > T.tb_cap) {
+        T.status = 2;
+        T.rows = rows;
+        return;
       }
-      if (T.want_codes) {
-        cw |= nib << (4 * (k & 7));
-        if ((k & 7) == 7 || k == nk - 1) {
-          row_codes[kw++] = cw;
-          cw = 0;
-        }
-      }
-    };
-    if constexpr (WC > 0) {
-#pragma unroll
-      for (int k = 0; k < 2 * WC + 1; ++k)
-        if (k < nk) cell(Mr, Fr, k, (int)((qw[k >> 4] >> (4 * (k & 15))) & 15u));
-      // next row's band starts one column to the right: drop cell 0, append column (i + 1) + w
-#pragma unroll
-      for (int u = 0; u < NQ; ++u) qw[u] = (qw[u] >> 4) | (u + 1 < NQ ? qw[u + 1] << 60 : 0ull);
-      const int jn = i + 1 + w;
-      if (jn <= n2) {
-        const int kl = nk - 1;
-#pragma unroll
-        for (int u = 0; u < NQ; ++u)
-          if (u == (kl >> 4)) qw[u] |= (uint64_t)s2.at(ar, jn - 1) << (4 * (kl & 15));
-      }
-    } else {
+      const int ci = s1.at(ar, i - 1);
+      int best = 0, bestj = -1, e = kOut;
+      uint32_t cw = 0;
+      int kw = 0;
+      uint32_t *row_codes = tb + T.tb_off + (int64_t)(i - 1) * wpr;
       for (int k = 0; k < nk; ++k) {
         const int j = i - w + k;
-        cell(M, F, k, (j >= 1 && j <= n2) ? s2.at(ar, j - 1) : 0);
+        const int cj = (j >= 1 && j <= n2) ? s2.at(ar, j - 1) : 0;
+        uint32_t nib = 0xFu;
+        if (j >= c0 && j <= c1) {
+          const int32_t diag = (j == 1) ? (i == 1 ? 0 : kOut) : M[k];
+          const int32_t fin = (j == c1) ? kOut : F[k + 1];
+          int32_t v = score_of(ci, cj, P.match, P.mismatch) + diag;
+          uint32_t d = v > fin ? 0u : 1u;
+          if (!(v > fin)) v = fin;
+          if (!(v > e)) {
+            d = 2u;
+            v = e;
+          }
+          M[k] = v;
+          if (v > best) {
+            best = v;
+            bestj = j;
+          }
+          const int32_t h = v + open;
+          const int32_t f = fin + ext;
+          if (f >= h) d |= 4u;
+          F[k] = f >= h ? f : h;
+          e += ext;
+          if (e >= h) d |= 8u;
+          e = e >= h ? e : h;
+          nib = d;
+        }
+        if (T.want_codes) {
+          cw |= nib << (4 * (k & 7));
+          if ((k & 7) == 7 || k == nk - 1) {
+            row_codes[kw++] = cw;
+            cw = 0;
+          }
+        }
       }
+      rows = i;
+      if (bestj != n2 && bestj != 1 && (bestj == c0 || bestj == c1)) {
+        T.status = 1;
+        T.rows = rows;
+        return;
+      }
+      if (best > score) {
+        score = best;
+        e1 = i;
+        e2 = bestj;
+      }
+      if (score - best > P.xdrop) break;
+      if (best <= 0) break;
     }
-    rows = i;
-    if (bestj != n2 && bestj != 1 && (bestj == c0 || bestj == c1)) {
-      T.status = 1;
-      T.rows = rows;
-      return;
-    }
-    if (best > score) {
-      score = best;
-      e1 = i;
-      e2 = bestj;
-    }
-    if (score - best > P.xdrop) break;
-    if (best <= 0) break;
+    T.score = score;
+    T.end1 = e1;
+    T.end2 = e2;
+    T.rows = rows;
   }
-  T.score = score;
-  T.end1 = e1;
-  T.end2 = e2;
-  T.rows = rows;
 }
 
 template <int WC>
