@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--mode", type=int, default=1, help="1 = cut1Gap (1-gap), 2 = cut2Gaps (2-piece)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the per-pair and serving comparisons")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the library's default pipeline shape (4 lanes, 4 bins, ratio 0.6) instead of timing "
+                         "candidate shapes first (profiling runs: no trial calls before the warm-up)")
     return ap.parse_args()
 
 
@@ -216,7 +219,8 @@ def main():
 
     # ---- value: resident sequences (pipeline shape chosen by the library's autotuner on this batch first)
     batch = eng.upload(pairs)
-    tuned = eng.autotune(batch, args.mode)
+    tuned = ({"lanes": 4, "bins": 4, "bin_ratio": 0.6, "autotuned": False} if args.no_autotune
+             else eng.autotune(batch, args.mode))
     for _ in range(max(args.warmup, 3)):
         eng.align_resident(batch, args.mode)
     if dist:
