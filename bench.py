@@ -105,11 +105,11 @@ class ClockSampler:
 def workload(n_pairs, rank=0):
     from dcns_gb300 import workloads as W
     from dcns_gb300.ranks import shard_seed
-    return W.config2(n_pairs=n_pairs, seed=shard_seed(rank))
+    return W.batched_pairs(n_pairs=n_pairs, seed=shard_seed(rank))
 
 
 # DRAM bytes per algorithmic cell of the level-0 scan launch: ncu, 3,000 pairs of this workload, 18.51 MB read and 0
-# written for 161.25 G cells (profiles/scan_kernel_config2_3000pairs.md); traffic grows with the cells.
+# written for 161.25 G cells (profiles/scan_kernel_batched_3000pairs.md); traffic grows with the cells.
 SCAN_DRAM_BYTES_PER_CELL = 18.51392e6 / 161254407231
 
 
@@ -339,7 +339,7 @@ def main():
         from dcns_gb300 import workloads as W
         extras["serving_long_tail"] = {
             "workload": "1,200 requests: log-normal median 4 kb, sigma 1.0, 0.2-100 kb, 10 % of 50-100 kb",
-            **serve(1000.0, W.config5(n_requests=1200), 5)}
+            **serve(1000.0, W.serving_requests(n_requests=1200), 5)}
 
     cb = cpu_baseline(pairs, args.mode, args.cpu_seconds)
     line = {

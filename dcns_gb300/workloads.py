@@ -109,7 +109,7 @@ def planted_pair(rng, n1: int, n2: int, nseg: int, seg_lo: int, seg_hi: int, id_
     return a.decode(), b.decode()
 
 
-def config1(seed: int = 20261204):
+def single_pair_5kb(seed: int = 20261204):
     """One 5,000 x 5,000 pair, 20 planted 30-200 bp segments at 85 % identity, 1 % indels, 20 % 'n'-masked in runs of
     20-500 bp.  Returns [(seq1 codes, seq2 codes)]."""
     rng = np.random.default_rng(seed)
@@ -121,7 +121,7 @@ def lognormal_lengths(rng, n, median, sigma, lo, hi):
     return np.clip(np.round(rng.lognormal(np.log(median), sigma, size=n)), lo, hi).astype(int)
 
 
-def config2(n_pairs: int = 10000, seed: int = 20261205, sigma: float = 0.8):
+def batched_pairs(n_pairs: int = 10000, seed: int = 20261205, sigma: float = 0.8):
     """Batched workload: independent pairs with log-normal lengths (median 3 kb, clipped to 0.5-20 kb) drawn
     independently for both sequences, Poisson(8) planted segments capped at 30, 30-300 bp, identity U(70,95)%,
     1 % indels, 15 % masked runs.  sigma=0.8 is this project's choice (the benchmark fixes only the median/clip)."""
@@ -136,7 +136,7 @@ def config2(n_pairs: int = 10000, seed: int = 20261205, sigma: float = 0.8):
     return out
 
 
-def config3(n_pairs: int = 64, length: int = 200000, seed: int = 20261206):
+def long_pairs_200kb(n_pairs: int = 64, length: int = 200000, seed: int = 20261206):
     """Long pairs: 200 kb x 200 kb at GC 45 %, 500 planted 20-400 bp segments at 80 % identity, and 5 duplicated
     2-10 kb blocks inserted into the query."""
     rng = np.random.default_rng(seed)
@@ -147,7 +147,7 @@ def config3(n_pairs: int = 64, length: int = 200000, seed: int = 20261206):
     return out
 
 
-def config4(n_seeds: int = 1000000, seed: int = 20261207):
+def extension_seeds(n_seeds: int = 1000000, seed: int = 20261207):
     """Extension stress: per seed, a 38 bp core with 0-7 substitutions (SW score 41-76 at the default scoring) followed
     by flanks of U(50, 2000) bp whose query copy has identity U(50, 98) % and 1-5 bp indels at rate U(0, 3) %.
     Returns [(seq1 codes, seq2 codes)], each pair starting at the seed as x_extend_seed's forward pass sees it."""
@@ -165,7 +165,7 @@ def config4(n_seeds: int = 1000000, seed: int = 20261207):
     return out
 
 
-def config5(n_requests: int = 2000, seed: int = 20261208, long_frac: float = 0.10):
+def serving_requests(n_requests: int = 2000, seed: int = 20261208, long_frac: float = 0.10):
     """Serving requests: lengths log-normal (median 4 kb, sigma 1.0) clipped to 200 bp-100 kb, drawn independently for
     both sequences, except that a `long_frac` share of the requests (chosen at random) draws both from U(50, 100] kb:
     the log-normal alone puts well under 1 % above 50 kb, and the serving configuration fixes 10 %.  Planted 30-300 bp

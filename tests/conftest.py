@@ -12,7 +12,7 @@ GOLDEN = os.path.join(ROOT, "tests", "golden", "golden.npz")
 GOLDEN_DIR = os.path.join(ROOT, "tests", "golden")
 if GOLDEN_DIR not in sys.path:
     sys.path.insert(0, GOLDEN_DIR)
-CONFIGS = os.path.join(GOLDEN_DIR, "configs.npz")
+DIGESTS = os.path.join(GOLDEN_DIR, "workload_digests.npz")
 
 
 def pytest_configure(config):
@@ -43,9 +43,9 @@ def golden():
 
 
 @pytest.fixture(scope="session")
-def configs():
-    """Digests of the reference's outputs on the benchmark workloads (tests/golden/make_config_golden.py)."""
-    return np.load(CONFIGS)
+def ref_digests():
+    """Digests of the reference's outputs on the benchmark workloads (tests/golden/make_workload_digests.py)."""
+    return np.load(DIGESTS)
 
 
 def ragged(z, name, i):

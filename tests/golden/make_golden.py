@@ -160,7 +160,7 @@ def main(refdir):
     out["sg_prm"] = np.array(prm, np.int32)
 
     # ---- whole pipelines: the config-1 pair plus small planted pairs (1-gap and 2-gap)
-    pairs = list(W.config1())
+    pairs = list(W.single_pair_5kb())
     for t in range(24):
         n1, n2 = int(rng.integers(40, 2500)), int(rng.integers(8, 2500))
         x, y = W.planted_pair(rng, n1, n2, int(rng.integers(0, 10)), 30, 300, 0.7, 0.98, 0.01,

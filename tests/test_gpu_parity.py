@@ -142,8 +142,8 @@ def _oracle_many(oracle, pairs, two_gap):
         return list(ex.map(lambda ab: oracle.find(ab[0], ab[1], two_gap=two_gap)[0], pairs))
 
 
-def test_config2_sample_vs_oracle(eng, oracle):
-    pairs = W.config2(n_pairs=96, seed=4242)
+def test_batched_pairs_sample_vs_oracle(eng, oracle):
+    pairs = W.batched_pairs(n_pairs=96, seed=4242)
     exp = _oracle_many(oracle, pairs, False)
     got = eng.align_pairs(pairs, 1)
     for i in range(len(pairs)):
@@ -153,7 +153,7 @@ def test_config2_sample_vs_oracle(eng, oracle):
 
 
 def test_two_gap_sample_vs_oracle(eng, oracle):
-    pairs = W.config2(n_pairs=24, seed=777)
+    pairs = W.batched_pairs(n_pairs=24, seed=777)
     pairs = [(a[:2500], b[:2500]) for a, b in pairs if len(b) >= 8]
     exp = _oracle_many(oracle, pairs, True)
     got = eng.align_pairs(pairs, 2)
@@ -227,7 +227,7 @@ def test_non_default_scoring(eng, oracle):
 
 def test_serving_same_alone_and_in_mix(eng):
     """Continuous batching: each request's result is identical whether it runs alone or mixed with others."""
-    pairs = W.config2(n_pairs=40, seed=99)
+    pairs = W.batched_pairs(n_pairs=40, seed=99)
     alone = [eng.align_pairs([p], 1)[0] for p in pairs[:6]]
     eng.serve_start(1, max_inflight=16)
     try:
@@ -243,7 +243,7 @@ def test_serving_same_alone_and_in_mix(eng):
 
 
 def test_resident_batch_matches_host_path(eng):
-    pairs = W.config2(n_pairs=64, seed=31)
+    pairs = W.batched_pairs(n_pairs=64, seed=31)
     b = eng.upload(pairs)
     try:
         r1 = eng.align_resident(b, 1)
@@ -293,10 +293,10 @@ def test_binned_two_lane_batch_vs_oracle(eng, oracle):
 
 
 @pytest.mark.parametrize("cigar", [False, True])
-def test_xdrop_stress_config4_vs_oracle(eng, oracle, cigar):
+def test_xdrop_stress_extension_seeds_vs_oracle(eng, oracle, cigar):
     """Extension-stress seeds (flanks 50-2000 bp, identity 50-98 %, indels 0-3 %): band restarts up to wide bands,
     reverse passes longer than the first traceback slot, variable termination."""
-    tasks = W.config4(3000, seed=44)
+    tasks = W.extension_seeds(3000, seed=44)
     out, cigars = eng.SemiGlobal_xextend(tasks, cigar=cigar)
     for k, (a, b) in enumerate(tasks):
         e = oracle.xextend(a, b, cigar=cigar)
@@ -305,10 +305,10 @@ def test_xdrop_stress_config4_vs_oracle(eng, oracle, cigar):
             assert cigars[k] == e["cigar"], k
 
 
-def test_long_pair_config3_subsets_vs_oracle(eng, oracle):
+def test_long_pairs_200kb_subsets_vs_oracle(eng, oracle):
     """Long-pair shapes of the 200 kb workload at sizes the oracle finishes quickly: a 200 kb reference against a 4 kb
     query slice and a 4 kb reference slice against the 200 kb query (row chunking with warm-ups, many windows)."""
-    a, b = W.config3(n_pairs=1)[0]
+    a, b = W.long_pairs_200kb(n_pairs=1)[0]
     pairs = [(a, b[100000:104000]), (a[50000:54000], b), (a[:30000], b[:30000])]
     exp = _oracle_many(oracle, pairs, False)
     got = eng.align_pairs(pairs, 1)
@@ -316,12 +316,12 @@ def test_long_pair_config3_subsets_vs_oracle(eng, oracle):
         assert_same_fragments(got[i], exp[i], i)
 
 
-def test_long_pair_config3_full_size_alone_equals_in_batch(eng):
+def test_long_pairs_200kb_full_size_alone_equals_in_batch(eng):
     """At full size (200 kb x 234 kb) the fragments of a pair do not depend on how its scan is tiled: alone (few
     tiles, rows split into chunks with warm-ups) and inside a batch of other pairs (different chunking)."""
-    a, b = W.config3(n_pairs=1)[0]
+    a, b = W.long_pairs_200kb(n_pairs=1)[0]
     alone = eng.align_pairs([(a, b)], 1)[0]
-    others = W.config2(n_pairs=300, seed=31)
+    others = W.batched_pairs(n_pairs=300, seed=31)
     mixed = eng.align_pairs(others[:150] + [(a, b)] + others[150:], 1)[150]
     assert len(alone) > 50
     assert frag_keys(alone) == frag_keys(mixed)

@@ -23,7 +23,7 @@ def _rank_main(rank, world, port, q):
     try:
         from oracle import oracle as O
 
-        pairs = W.config2(n_pairs=6, seed=R.shard_seed(rank))
+        pairs = W.batched_pairs(n_pairs=6, seed=R.shard_seed(rank))
         pairs = [(a[:1500], b[:1500]) for a, b in pairs]
         orc = O.Oracle()
         nf, ck, cells = orc.find_batch(pairs, threads=1)
