@@ -158,7 +158,7 @@ void launch_xdrop_iota(int *list, int n, int *count, cudaStream_t st);
 void launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
                         int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, Arena ar,
                         Params p, uint32_t *tb, int w, int n_bound, int nsm, int32_t *scratch, int64_t per_warp,
-                        int warps, int warp_from, cudaStream_t st);
+                        int warps, int warp_from, int wave_max_w, cudaStream_t st);
 void launch_xdrop_traceback_all(XTask *tasks, int n, const uint32_t *tb, uint32_t *cig,
                                 unsigned long long *cig_cursor, cudaStream_t st);
 // Packs the CIGARs of every finished task in task order into dense (cig_dense offsets); *total = their words.

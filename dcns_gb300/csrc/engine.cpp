@@ -139,6 +139,7 @@ void init_context(Context &C, int device, size_t budget) {
   if (const char *e = std::getenv("DCNS_BINS")) C.bins = std::max(1, std::min(64, std::atoi(e)));
   if (const char *e = std::getenv("DCNS_TRACE")) C.trace = std::atoi(e);
   if (const char *e = std::getenv("DCNS_XDROP_WARP_FROM")) C.xdrop_warp_from = std::max(0, std::atoi(e));
+  if (const char *e = std::getenv("DCNS_XDROP_WAVE")) C.xdrop_wave_max_w = std::max(0, std::atoi(e));
   if (const char *e = std::getenv("DCNS_BIN_RATIO")) C.bin_ratio = std::max(0.1, std::min(1.0, std::atof(e)));
 }
 
@@ -1165,7 +1166,7 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
     int64_t scratch_ints = 1;
     for (int L = 0; L < nlev; ++L) {
       const int64_t w = (int64_t)w0 << L;
-      if (w <= C.xdrop_warp_from) continue;
+      if (w <= C.xdrop_warp_from || w <= std::min(C.xdrop_wave_max_w, 256)) continue;  // register band / wavefront
       per_warp[L] = 2 * (2 * w + 2);
       const int64_t cap = std::max<int64_t>(32, ((int64_t)512 << 20) / (4 * per_warp[L]));
       warps[L] = (int)(std::min<int64_t>({n, cap, (int64_t)C.nsm * 64}) + 3) / 4 * 4;  // whole blocks of 4 warps
@@ -1193,7 +1194,8 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
       DCNS_CK(cudaMemsetAsync(cnt + out, 0, sizeof(int), C.st));
       launch_xdrop_level(C.d_x.as<XTask>(), lists + in * n, cnt + in, lists + out * n, cnt + out, lists + 2 * n,
                          cnt + 2, cur, want_codes ? tb_words : 0, C.arena, P, C.d_tb.as<uint32_t>(), w0 << L, (int)n,
-                         C.nsm, C.d_scratch.as<int32_t>(), per_warp[L], warps[L], C.xdrop_warp_from, C.st);
+                         C.nsm, C.d_scratch.as<int32_t>(), per_warp[L], warps[L], C.xdrop_warp_from,
+                         C.xdrop_wave_max_w, C.st);
       in = out;
     }
     DCNS_CK(cudaEventRecord(C.ev1, C.st));

@@ -123,6 +123,8 @@ struct Context {
   bool is_lane = false;
   double bin_ratio = 0.6;    // bin b holds a share of the work proportional to bin_ratio^b (later bins smaller)
   int xdrop_warp_from = 20;  // x-drop bands wider than this run one warp per pass (DCNS_XDROP_WARP_FROM)
+  // x-drop bands wider than xdrop_warp_from and up to this run as one-warp wavefronts (DCNS_XDROP_WAVE; 0 = off)
+  int xdrop_wave_max_w = 256;
   // Level-0 turnstile of one binned call: the bins enqueue their level-0 scans on the parent's bulk stream in bin
   // order, so the scans run one after another and the first bins' host work overlaps the later bins' scans.
   struct Turnstile {

@@ -500,6 +500,169 @@ __global__ void __launch_bounds__(128) xdrop_level_warp_kernel(XLevelArgs L, Are
   }
 }
 
+// ------------------------------------------------------------------ band levels as a wavefront (one warp per pass)
+// Rows in stripes of 32, lane l owning row i = r0 + l; at step t the lane computes its band cell k = t - 2l (column
+// j = i - w + k), so the cell above (column j, the previous row's band cell k + 1) was computed by lane l - 1 one step
+// earlier and the diagonal cell (column j - 1, band cell k) two steps earlier: both arrive by __shfl_up_sync, as does
+// the query code of column j.  Lane 0 reads the row above the stripe from the warp's boundary row in shared memory,
+// which lane 31 rewrites (by band index) as it computes the stripe's last row; lane 31 writes index k at step 62 + k,
+// after lane 0 has read it (steps k - 1 and k).  A cell only ever reads in-band cells of the row above (its band is
+// the row above's shifted by one column, clipped to [1, n2]), so nothing else crosses rows.  The cells are exactly
+// the thread pass's; each lane keeps its row's maximum and writes its row's codes, and after each stripe the rows are
+// evaluated in order (slot capacity, band-edge restart, score, x-drop, non-positive maximum) with the thread pass's
+// rules; rows computed past the stop row are discarded (their codes lie in the pass's own slot, after its end row).
+// A row costs (2w + 63) / 32 steps of one cell per lane: a long pass runs several times faster than on one thread.
+constexpr int kXwMaxW = 256;
+
+__device__ void xdrop_wave_pass(XTask &T, const Arena &ar, const Params &P, uint32_t *__restrict__ tb,
+                                int32_t *__restrict__ bM, int32_t *__restrict__ bF, int64_t tb_off, int32_t tb_cap,
+                                int lane) {
+  const int w = T.w, n1 = T.n1, n2 = T.n2, nk = 2 * w + 1, wpr = xd_words_per_row(w);
+  const bool codes = T.want_codes != 0;
+  const SeqView s1{T.base1, T.a1, T.dir}, s2{T.base2, T.a2, T.dir};
+  const int open = P.open1, ext = P.ext1;
+  for (int k = lane; k <= nk; k += 32) bM[k] = kOut, bF[k] = kOut;  // row 0
+  __syncwarp();
+  int score = 0, e1 = 0, e2 = 0, rows = 0, status = 0;
+  bool stop = false;
+  for (int r0 = 1; r0 <= n1 && !stop; r0 += 32) {
+    const int i = r0 + lane;
+    const bool live = i <= n1;
+    const int c0 = max(i - w, 1), c1 = min(i + w, n2);
+    const int ci = live ? s1.at(ar, i - 1) : 0;
+    const bool wcode = codes && live && (int64_t)i * wpr <= tb_cap;  // rows past the slot are never kept
+    uint32_t *row_codes = tb + tb_off + (int64_t)(i - 1) * wpr;
+    int e = kOut, best = 0, bestj = -1, outM = kOut, outF = kOut, outC = 0, prevUp = kOut, kw = 0;
+    uint32_t cw = 0;
+    const int nsteps = nk + 62;
+    for (int t = 0; t < nsteps; ++t) {
+      const int upM = __shfl_up_sync(0xFFFFFFFFu, outM, 1);
+      int upF = __shfl_up_sync(0xFFFFFFFFu, outF, 1);
+      int cj = __shfl_up_sync(0xFFFFFFFFu, outC, 1);
+      const int k = t - 2 * lane, j = i - w + k;
+      int diagv = prevUp;
+      if (lane == 0) {
+        diagv = (k >= 0 && k < nk) ? bM[k] : kOut;
+        upF = (k >= 0 && k + 1 <= nk) ? bF[k + 1] : kOut;
+        cj = (j >= 1 && j <= n2) ? s2.at(ar, j - 1) : 0;
+      }
+      int nM = kOut, nF = kOut;
+      if (k >= 0 && k < nk) {
+        uint32_t nib = 0xFu;
+        if (live && j >= c0 && j <= c1) {
+          const int32_t diag = (j == 1) ? (i == 1 ? 0 : kOut) : diagv;
+          const int32_t fin = (j == c1) ? kOut : upF;
+          int32_t v = score_of(ci, cj, P.match, P.mismatch) + diag;
+          uint32_t d = v > fin ? 0u : 1u;
+          if (!(v > fin)) v = fin;
+          if (!(v > e)) {
+            d = 2u;
+            v = e;
+          }
+          if (v > best) {
+            best = v;
+            bestj = j;
+          }
+          const int32_t h = v + open;
+          const int32_t f = fin + ext;
+          if (f >= h) d |= 4u;
+          nM = v;
+          nF = f >= h ? f : h;
+          e += ext;
+          if (e >= h) d |= 8u;
+          e = e >= h ? e : h;
+          nib = d;
+          if (lane == 31) {
+            bM[k] = nM;
+            bF[k] = nF;
+          }
+        }
+        if (wcode) {
+          cw |= nib << (4 * (k & 7));
+          if ((k & 7) == 7 || k == nk - 1) {
+            row_codes[kw++] = cw;
+            cw = 0;
+          }
+        }
+      }
+      prevUp = upM;
+      outM = nM;
+      outF = nF;
+      outC = cj;
+    }
+    __syncwarp();
+    for (int rr = 0; rr < 32; ++rr) {  // the stripe's rows in order; every lane keeps the same state
+      const int tm = __shfl_sync(0xFFFFFFFFu, best, rr), tj = __shfl_sync(0xFFFFFFFFu, bestj, rr);
+      if (stop) continue;
+      const int ii = r0 + rr;
+      if (ii > n1) {
+        stop = true;
+        continue;
+      }
+      if (codes && (int64_t)ii * wpr > tb_cap) {
+        status = 2;
+        stop = true;
+        continue;
+      }
+      rows = ii;
+      const int cc0 = max(ii - w, 1), cc1 = min(ii + w, n2);
+      if (tj != n2 && tj != 1 && (tj == cc0 || tj == cc1)) {
+        status = 1;
+        stop = true;
+        continue;
+      }
+      if (tm > score) {
+        score = tm;
+        e1 = ii;
+        e2 = tj;
+      }
+      if (score - tm > P.xdrop || tm <= 0) stop = true;
+    }
+  }
+  if (lane == 0) {
+    T.status = status;
+    T.rows = rows;
+    if (status == 0) {
+      T.score = score;
+      T.end1 = e1;
+      T.end2 = e2;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) xdrop_level_wave_kernel(XLevelArgs L, Arena ar, Params P,
+                                                               uint32_t *__restrict__ tb) {
+  __shared__ int32_t sM[4][2 * kXwMaxW + 2], sF[4][2 * kXwMaxW + 2];
+  const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  const int n = *L.count_in;
+  for (int q = gw; q < n; q += nw) {
+    const int id = L.list_in[q];
+    XTask &T = L.tasks[id];
+    int ok = 1, cap = 0;
+    long long off = 0;
+    if (lane == 0) {
+      if (T.want_codes) ok = xd_take_slot(T, L) ? 1 : 0;
+      off = T.tb_off;
+      cap = T.tb_cap;
+    }
+    ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
+    off = __shfl_sync(0xFFFFFFFFu, off, 0);
+    cap = __shfl_sync(0xFFFFFFFFu, cap, 0);
+    if (!ok) {
+      if (lane == 0) {
+        T.status = 2;
+        L.retry[atomicAdd(L.retry_count, 1)] = id;
+      }
+      continue;
+    }
+    xdrop_wave_pass(T, ar, P, tb, sM[wb], sF[wb], off, cap, lane);
+    __syncwarp();
+    if (lane == 0) xd_route(T, id, L);
+    __syncwarp();
+  }
+}
+
 __global__ void xdrop_iota_kernel(int *list, int n, int *count) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) list[k] = k;
@@ -525,11 +688,14 @@ void launch_xdrop_iota(int *list, int n, int *count, cudaStream_t st) {
 void launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
                         int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, Arena ar,
                         Params p, uint32_t *tb, int w, int n_bound, int nsm, int32_t *scratch, int64_t per_warp,
-                        int warps, int warp_from, cudaStream_t st) {
+                        int warps, int warp_from, int wave_max_w, cudaStream_t st) {
   if (n_bound <= 0) return;
   const XLevelArgs L{tasks, list_in, count_in, list_out, count_out, retry, retry_count, tb_cursor, tb_words};
   const int g = (int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * 16);
-  if (w > warp_from)
+  if (w > warp_from && w <= wave_max_w && w <= kXwMaxW)  // wide bands up to 256: the wavefront
+    xdrop_level_wave_kernel<<<(int)std::min<int64_t>((n_bound + 3) / 4, (int64_t)nsm * 16), 128, 0, st>>>(L, ar, p,
+                                                                                                         tb);
+  else if (w > warp_from)
     xdrop_level_warp_kernel<<<(warps + 3) / 4, 128, 0, st>>>(L, ar, p, tb, scratch, per_warp);
   else if (w <= 10)
     xdrop_level_kernel<10><<<g, 128, 0, st>>>(L, ar, p, tb);
