@@ -1,10 +1,13 @@
 // Adaptive-band x-drop seed extension (SemiGlobal_xextend, impl/sequenceAlignment3.cpp:1234-1451, driven by
 // x_extend_seed, impl/findSimilarFragmentsForPairedSequence4.cpp:205-285) and its traceback.
 //
-// One thread runs one pass of one seed.  The band is stored diagonal-relative: index k = j - i + w, so the diagonal
-// predecessor of (i, j) sits at the same index in the previous row and the vertical predecessor at k + 1, and both
-// arrays update in place left to right.  For w <= the template capacity the band lives in registers; wider bands
-// (after several band-edge restarts) use a per-thread global scratch.
+// Three forms of a pass, chosen by band half-width w in the chained levels:
+//   w <= 20      one thread per pass, the band in registers;
+//   20 < w <= 256  one warp per pass as an anti-diagonal wavefront over 32-row stripes (xdrop_level_wave_kernel);
+//   w > 256      one warp per pass across the band, the band rows in global scratch (xdrop_level_warp_kernel).
+// The thread form stores the band diagonal-relative: index k = j - i + w, so the diagonal predecessor of (i, j) sits
+// at the same index in the previous row and the vertical predecessor at k + 1, and both arrays update in place left
+// to right.  Outside the chained levels (retries, the kernel-level entry) wide bands use a per-thread global scratch.
 //
 // A pass ends in one of three states: done, "restart" (the row maximum touched a band edge: the reference recomputes
 // from scratch with 2w, and so does the host by relaunching the seed with the doubled width), or "slot too small"
