@@ -37,13 +37,17 @@ U64P = C.POINTER(C.c_uint64)
 F64P = C.POINTER(C.c_double)
 
 
+# The reference checkout the parity checker is built from (absent on hosts that only run the built files).
+REFERENCE_DIR = os.environ.get("DCNS_REFERENCE", "/root/reference")
+
+
 def build(force: bool = False) -> None:
     """Compile the restatement (always) and the reference harness (where the reference checkout exists)."""
     os.makedirs(BUILD, exist_ok=True)
     src = os.path.join(HERE, "dcns_oracle.cpp")
     if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src):
         subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", src, "-o", ORACLE_SO])
-    if os.path.isdir(os.environ.get("DCNS_REFERENCE", "/root/reference")):
+    if os.path.isdir(REFERENCE_DIR):
         harness = os.path.join(HERE, "ref_harness.cpp")
         if force or not os.path.exists(REF_SO) or os.path.getmtime(REF_SO) < os.path.getmtime(harness):
             subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")], stdout=subprocess.DEVNULL)
