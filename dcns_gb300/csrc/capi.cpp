@@ -199,12 +199,19 @@ void dcns_params_default(dcns_params *p) {
 int dcns_ctx_create(int device, size_t mem_budget, dcns_ctx **out) {
   if (!out) return DCNS_ERR_INVALID;
   *out = nullptr;
-  auto *ctx = new dcns_ctx;
-  try {
+  dcns_ctx *ctx = nullptr;
+  try {  // nothing escapes the C ABI: allocation and thread failures become status codes too
+    ctx = new dcns_ctx;
     init_context(ctx->C, device, mem_budget);
   } catch (const Error &e) {
     delete ctx;
     return e.code;
+  } catch (const std::bad_alloc &) {
+    delete ctx;
+    return DCNS_ERR_NOMEM;
+  } catch (const std::exception &) {
+    delete ctx;
+    return DCNS_ERR_DEVICE;
   }
   *out = ctx;
   return DCNS_OK;

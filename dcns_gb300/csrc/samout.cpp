@@ -97,17 +97,10 @@ char *to_c(const std::string &s, int64_t *len) {
   return p;
 }
 
-}  // namespace
-
-extern "C" int dcns_format_records(int64_t n_frag, const int64_t *frag, const uint32_t *cigar, const double *pvalue,
-                                   const char *ref_text, int64_t ref_len, const char *qry_text, int64_t qry_len,
-                                   int ref_strand, int qry_strand, int32_t ref_start, int32_t qry_start,
-                                   const char *ref_chr, const char *qry_chr, char **sam, int64_t *sam_len, char **o,
-                                   int64_t *o_len) {
-  if (n_frag < 0 || (n_frag > 0 && (!frag || !pvalue)) || !ref_chr || !qry_chr || !sam || !o) return DCNS_ERR_INVALID;
-  if ((ref_len > 0 && !ref_text) || (qry_len > 0 && !qry_text) || ref_len < 0 || qry_len < 0) return DCNS_ERR_INVALID;
-  if ((ref_strand != 0 && ref_strand != 1) || (qry_strand != 0 && qry_strand != 1)) return DCNS_ERR_INVALID;
-  *sam = *o = nullptr;
+int format_records(int64_t n_frag, const int64_t *frag, const uint32_t *cigar, const double *pvalue,
+                   const char *ref_text, int64_t ref_len, const char *qry_text, int64_t qry_len, int ref_strand,
+                   int qry_strand, int32_t ref_start, int32_t qry_start, const char *ref_chr, const char *qry_chr,
+                   char **sam, int64_t *sam_len, char **o, int64_t *o_len) {
   const std::string R(ref_text ? ref_text : "", (size_t)ref_len), Q(qry_text ? qry_text : "", (size_t)qry_len);
   std::ostringstream so, oo;
   oo << "#" << ref_chr << ":" << ref_strand << ":" << ref_start << "-" << qry_chr << ":" << qry_strand << ":"
@@ -175,6 +168,28 @@ extern "C" int dcns_format_records(int64_t n_frag, const int64_t *frag, const ui
     return DCNS_ERR_NOMEM;
   }
   return DCNS_OK;
+}
+
+}  // namespace
+
+extern "C" int dcns_format_records(int64_t n_frag, const int64_t *frag, const uint32_t *cigar, const double *pvalue,
+                                   const char *ref_text, int64_t ref_len, const char *qry_text, int64_t qry_len,
+                                   int ref_strand, int qry_strand, int32_t ref_start, int32_t qry_start,
+                                   const char *ref_chr, const char *qry_chr, char **sam, int64_t *sam_len, char **o,
+                                   int64_t *o_len) {
+  if (n_frag < 0 || (n_frag > 0 && (!frag || !pvalue)) || !ref_chr || !qry_chr || !sam || !o) return DCNS_ERR_INVALID;
+  if ((ref_len > 0 && !ref_text) || (qry_len > 0 && !qry_text) || ref_len < 0 || qry_len < 0) return DCNS_ERR_INVALID;
+  if ((ref_strand != 0 && ref_strand != 1) || (qry_strand != 0 && qry_strand != 1)) return DCNS_ERR_INVALID;
+  *sam = *o = nullptr;
+  try {  // host allocation failures become a status, not an exception through the C ABI
+    return format_records(n_frag, frag, cigar, pvalue, ref_text, ref_len, qry_text, qry_len, ref_strand, qry_strand,
+                          ref_start, qry_start, ref_chr, qry_chr, sam, sam_len, o, o_len);
+  } catch (const std::exception &) {
+    std::free(*sam);
+    std::free(*o);
+    *sam = *o = nullptr;
+    return DCNS_ERR_NOMEM;
+  }
 }
 
 extern "C" void dcns_free_text(char *text) { std::free(text); }
