@@ -1,5 +1,6 @@
 // C ABI of the engine (include/dcns_gb300.h).  Every entry point converts C++ exceptions into status codes and keeps
 // the message in the context.
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -432,17 +433,18 @@ int dcns_submit(dcns_ctx *ctx, const dcns_pair *pair, uint64_t *ticket) {
   if (pair->len1 < 0 || pair->len2 < 0 || (pair->len1 && !pair->seq1) || (pair->len2 && !pair->seq2))
     return DCNS_ERR_INVALID;
   Server &S = *ctx->srv;
-  Server::Req r;
-  r.s1.assign(pair->seq1, pair->seq1 + pair->len1);
-  r.s2.assign(pair->seq2, pair->seq2 + pair->len2);
-  {
-    std::lock_guard<std::mutex> lk(S.mu);
-    r.ticket = S.next++;
-    *ticket = r.ticket;
-    S.queue.push_back(std::move(r));
-  }
-  S.cv_work.notify_one();
-  return DCNS_OK;
+  return guarded(ctx, [&] {
+    Server::Req r;
+    r.s1.assign(pair->seq1, pair->seq1 + pair->len1);
+    r.s2.assign(pair->seq2, pair->seq2 + pair->len2);
+    {
+      std::lock_guard<std::mutex> lk(S.mu);
+      r.ticket = S.next++;
+      *ticket = r.ticket;
+      S.queue.push_back(std::move(r));
+    }
+    S.cv_work.notify_one();
+  });
 }
 
 int dcns_poll(dcns_ctx *ctx, uint64_t ticket, dcns_results **out) {
@@ -469,7 +471,9 @@ int dcns_poll(dcns_ctx *ctx, uint64_t ticket, dcns_results **out) {
 int dcns_serve_wait(dcns_ctx *ctx, uint64_t ticket, int64_t timeout_ms, dcns_results **out) {
   if (!ctx || !out || !ctx->srv) return DCNS_ERR_INVALID;
   Server &S = *ctx->srv;
-  const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
+  // at most about 30 days, so that the deadline cannot overflow the clock
+  const int64_t ms = std::max<int64_t>(0, std::min<int64_t>(timeout_ms, (int64_t)1 << 31));
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(ms);
   {
     std::unique_lock<std::mutex> lk(S.mu);
     if (!S.cv_done.wait_until(lk, deadline, [&] { return S.done.count(ticket) || S.failed.count(ticket); }))
