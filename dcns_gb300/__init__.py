@@ -55,8 +55,20 @@ def _headers():
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile every CUDA/C++ source for sm_103a into dcns_gb300/_lib/libdcnsgpu.so (in-tree, parallel)."""
+    """Compile every CUDA/C++ source for sm_103a into dcns_gb300/_lib/libdcnsgpu.so (in-tree, parallel).  Processes
+    that call this at once (one per rank) take turns on a lock file; the later ones find the library current."""
+    import fcntl
+
     os.makedirs(LIBDIR, exist_ok=True)
+    with open(os.path.join(LIBDIR, ".build.lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            return _build_locked(force, verbose)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _build_locked(force: bool, verbose: bool) -> str:
     srcs = _sources()
     newest = max(os.path.getmtime(p) for p in srcs + _headers())
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
