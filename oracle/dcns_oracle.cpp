@@ -3,7 +3,8 @@
 // CPU baseline ("port") on hosts where the reference itself cannot be built.  Nothing in the product links it.
 //
 // Parity of this restatement is pinned against the unmodified reference (oracle/_ref, built by build_ref.sh from the
-// reference checkout) by tests/test_oracle_pin.py and by the golden fixtures in tests/golden/.
+// reference checkout) by tests/test_oracle_pin.py, by the golden fixtures in tests/golden/, and by the reference's
+// digests of the benchmark workloads (tests/test_workload_digests.py).
 //
 // Reference map (paths inside the dCNS project):
 //   sw_striped_semantics   impl/sequenceAlignment3.cpp:220-337 (AVX2 int8) and :338-460 (AVX2 int16)
