@@ -15,6 +15,7 @@ namespace dcns {
 constexpr int32_t kOut = -536870912;  // score of cells outside a band (impl/sequenceAlignment3.cpp:34)
 constexpr int kScanW = 38;            // window width the fast seed-scan kernel is specialised for
 constexpr int kScanThreads = 64;      // threads per block of the fast seed-scan kernel
+constexpr int32_t kMaxSeqLen = 1 << 28;  // sequences are shorter; semi-global bands are clamped to it
 
 struct Params {
   int32_t match, mismatch, open1, ext1, open2, ext2;
@@ -133,6 +134,13 @@ struct SgWeights {
   int32_t n_cats, pieces;
 };
 constexpr int kSgwMaxCats = 64;
+
+// The semi-global kernel (semiglobal.cu): warps per CTA (one CTA runs one DP, warp w owns stripes w, w+8, ...) and the
+// boundary record a stripe leaves for the next one in global scratch (kSgNW slots of max_n2 + 2 records per CTA).
+constexpr int kSgNW = 8;
+struct SgRec {
+  int m, f1, f2;
+};
 
 // ---- kernel launchers (defined in the .cu files)
 void launch_pack(const int8_t *codes, const int64_t *src_off, const int64_t *dst_base, const int32_t *len, int nseq,

@@ -20,15 +20,11 @@
 
 #include "../../include/dcns_gb300.h"
 #include "device_common.cuh"
+#include "engine.h"
 
 namespace dcns {
 
 constexpr int kNaMaxLen = 16384;
-constexpr int kNaWarps = 8;  // the semi-global kernel's warps per CTA (one CTA runs the DP)
-
-struct NaRec {  // layout of the semi-global kernel's boundary record (three int32)
-  int m, f1, f2;
-};
 
 struct NaScratch {
   SgTask task;
@@ -38,7 +34,7 @@ struct NaScratch {
   int pad;
   uint32_t pk[(2 * (kNaMaxLen + 64) + 128) / 16];
   uint32_t nm[(2 * (kNaMaxLen + 64) + 128) / 32];
-  NaRec bnd[kNaWarps * (kNaMaxLen + 2)];
+  SgRec bnd[kSgNW * (kNaMaxLen + 2)];  // the semi-global kernel's boundary rows of its one CTA
 };
 
 static __device__ __align__(256) unsigned char g_na_scratch[sizeof(NaScratch)];
@@ -124,21 +120,26 @@ extern "C" int dcns_semiglobal_noalloc(const int8_t *d_seq1, int32_t len1, const
     return DCNS_ERR_INVALID;
   if (len1 > kNaMaxLen || len2 > kNaMaxLen) return DCNS_ERR_INVALID;  // the fixed scratch holds at most this much
   Params P;
-  P.match = params->match, P.mismatch = params->mismatch, P.open1 = params->open1, P.ext1 = params->ext1;
-  P.open2 = params->open2, P.ext2 = params->ext2, P.window = params->window, P.min_score = params->min_score;
-  P.step = params->step, P.w = params->w, P.xdrop = params->xdrop, P.zdrop = params->zdrop;
-  P.bandwidth = params->bandwidth, P.max_align_len = params->max_align_len;
-  P.pvalue = params->pvalue, P.lambda = params->lambda, P.kvalue = params->kvalue;
-  if (P.bandwidth < 1 || P.match < 1 || P.match > 127 || P.mismatch < -127 || P.mismatch > 127) return DCNS_ERR_INVALID;
+  try {  // the parameter checks of the allocating entry points, so both accept and reject the same parameters
+    P = to_params(params);
+    validate(P);
+  } catch (const Error &) {
+    return DCNS_ERR_INVALID;
+  }
+  // An error still pending from the caller's earlier CUDA work is reported and left in place for its owner, so that
+  // the check after the launches below reports only this call's own launch errors.
+  if (cudaPeekAtLastError() != cudaSuccess) return DCNS_ERR_DEVICE;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DCNS_ERR_DEVICE;
   NaScratch *S = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_na_mu);
     if (!g_na_ptr[dev]) {
+      // the kernel's boundary scratch for one CTA must fit the fixed array (checked once, with the kernel's own sizing)
+      if (sg_bnd_bytes(1, kNaMaxLen) > (int64_t)sizeof(NaScratch::bnd)) return DCNS_ERR_DEVICE;
       void *p = nullptr;
       if (cudaGetSymbolAddress(&p, g_na_scratch) != cudaSuccess || !p) {
-        (void)cudaGetLastError();
+        (void)cudaGetLastError();  // the failed lookup's own error
         return DCNS_ERR_DEVICE;
       }
       g_na_ptr[dev] = (NaScratch *)p;

@@ -25,24 +25,21 @@
 
 namespace dcns {
 
-constexpr int kSgNW = 8;             // warps per CTA; one CTA runs one DP, warp w owns stripes w, w+8, ...
 constexpr int kSgD = 2;              // super-steps between the starts of consecutive stripes
 constexpr int kSgR = 4;              // rows per lane
 constexpr int kSgRows = 32 * kSgR;  // rows per stripe
 
 // Wavefront steps of one stripe (columns its rows span, plus the 31-step lane skew), an upper bound for every stripe.
+// Computed in 64 bits: 2w + kSgRows does not fit an int for bands near 2^30.
 __host__ __device__ inline int64_t sg_stride_steps(int n2, int w) {
-  return (int64_t)(n2 < 2 * w + kSgRows ? n2 : 2 * w + kSgRows) + 32;
+  const int64_t span = 2 * (int64_t)w + kSgRows;
+  return (n2 < span ? (int64_t)n2 : span) + 32;
 }
 
 int64_t sg_tb_bytes(int n1, int n2, int w) {
   if (n1 <= 0 || n2 <= 0) return 0;
   return (int64_t)((n1 + kSgRows - 1) / kSgRows) * sg_stride_steps(n2, w) * 32 * kSgR;
 }
-
-struct SgRec {
-  int m, f1, f2;
-};
 
 // Super-step length K (wavefront steps between CTA barriers) for a DP whose stripes take at most smax steps:
 //  * a warp finishes stripe s before stripe s+8 starts:   kSgD * kSgNW * K >= smax
@@ -51,7 +48,8 @@ struct SgRec {
 //    it at step j - jstart_{s+1} - 63 or later, and jstart_{s+1} - jstart_s <= kSgRows; so the producer is at most
 //    kSgRows + 94 steps ahead of that read, which must be at most (kSgD - 1) * K:  K >= kSgRows + 96
 __host__ __device__ inline int sg_superstep(int n2, int w) {
-  const int smax = (n2 < 2 * w + kSgRows ? n2 : 2 * w + kSgRows) + 31;
+  const int64_t span = 2 * (int64_t)w + kSgRows;
+  const int smax = (int)(n2 < span ? (int64_t)n2 : span) + 31;
   const int k = (smax + kSgD * kSgNW - 1) / (kSgD * kSgNW);
   static_assert(kSgD == 2, "the lower bound below assumes two super-steps between stripe starts");
   return k > kSgRows + 96 ? k : kSgRows + 96;
@@ -313,7 +311,8 @@ __global__ void sg_traceback_kernel(SgTask *__restrict__ tasks, const int *__res
   if (k >= n) return;
   SgTask &T = tasks[idx[k]];
   const int n2 = T.n2;
-  const int64_t stride = (int64_t)(n2 < 2 * w + kRows ? n2 : 2 * w + kRows) + 32;
+  const int64_t span = 2 * (int64_t)w + kRows;
+  const int64_t stride = (n2 < span ? (int64_t)n2 : span) + 32;
   int ii = T.end1, jj = T.end2, state = 0, nc = 0;
   uint32_t *out = cig + T.cig_off;
   uint32_t last = 0xFFFFFFFFu;
@@ -386,7 +385,8 @@ void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, co
 // 31 steps before lane 31 overwrites it).  Rows are evaluated in order after each stripe; the DP ends at the stop row.
 // Codes: one byte per cell, stripe / step / lane, the traceback layout of 32-row stripes.
 __host__ __device__ inline int64_t sgw_stride_steps(int n2, int w) {
-  return (int64_t)(n2 < 2 * w + 32 ? n2 : 2 * w + 32) + 32;
+  const int64_t span = 2 * (int64_t)w + 32;
+  return (n2 < span ? (int64_t)n2 : span) + 32;
 }
 
 int64_t sgw_tb_bytes(int n1, int n2, int w) {
