@@ -10,11 +10,15 @@ Reported (one JSON line, rank 0):
   e2e     the same through the public call with host buffers (dcns_align_pairs): H2D of the codes, the pipeline,
           and the D2H of the fragments inside the timed region
   roofline  the seed-scan kernel (dominant) against the live-measured integer-issue ceiling of its instruction mix
-  cpu_baseline  the oracle restatement of the reference over all host cores on a bounded sample
+  cpu_baseline  the oracle restatement of the reference over all host cores on a fixed sample of the workload (every
+          k-th pair, 64 per thread)
   per_pair_launch, serving  the one-pair-per-call form and the continuous-batching loop (p50/p99) for comparison
+  two_gap, long_pairs, extension_seeds  the other benchmark configurations (the cut2Gaps path, whole 200 kb pairs,
+          1,000,000 extension seeds), each with its kernel figures, its own CPU baseline and clock record
 
 `--impl reference` times the reference's CPU implementation of the path instead (the oracle restatement, since the
-reference sources are not present on the GPU host), with every host core.
+reference sources are not present on the GPU host), with every host core, each step one pass over the same fixed
+sample the cpu_baseline above times.
 """
 from __future__ import annotations
 
@@ -40,6 +44,23 @@ def workload_name(n, mode):
     return f"batched seed scan + extension: {n:,} pairs, log-normal 0.5-20 kb ({path} path)"
 
 
+L2_NOTE = ("GPU steps: L2 (129 MB) flushed by a 256 MB device write before every timed step; CPU steps: host caches "
+           "not flushed")
+
+
+def bench_config(n, mode, world):
+    """The workload keys shared by both arms' JSON lines (same dict, so the two arms name the same configuration)."""
+    return {"workload": workload_name(n, mode), "pairs": n, "mode": mode, "parallelism": f"replicas x{world}",
+            "l2": L2_NOTE}
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -48,7 +69,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--pairs", type=int, default=10000)
     ap.add_argument("--mode", type=int, default=1, help="1 = cut1Gap (1-gap), 2 = cut2Gaps (2-piece)")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--ext-seeds", type=int, default=1000000, help="seeds of the extension-stress line")
     ap.add_argument("--no-extras", action="store_true", help="skip the per-pair and serving comparisons")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the library's default pipeline shape (4 lanes, 4 bins, ratio 0.6) instead of timing "
@@ -129,57 +150,216 @@ def cells_of(st):
     return st["cells_scan"] + st["cells_scan_reverse"] + st["cells_xdrop"] + st["cells_semiglobal"]
 
 
-def cpu_baseline(pairs, mode, target_s, threads=None):
-    """The oracle restatement over all host cores on a bounded prefix of the workload (~target_s seconds)."""
+def cpu_sample(pairs, threads, per_thread=64):
+    """A fixed sample of the workload for the CPU timings: every k-th pair (so its length mix is the workload's),
+    per_thread pairs per host thread, handed out longest first so that the shared work counter does not end on a long
+    pair.  The same sample every step and in both arms."""
+    n = max(1, min(len(pairs), per_thread * threads))
+    stride = len(pairs) / n
+    idx = sorted({int(i * stride) for i in range(n)}, key=lambda i: (-len(pairs[i][0]) * len(pairs[i][1]), i))
+    desc = (f"every {stride:.2f}th pair of the {len(pairs):,}-pair workload ({len(idx)} pairs, longest first), "
+            f"{threads} threads")
+    return [pairs[i] for i in idx], desc
+
+
+def cpu_baseline(sample, desc, mode, threads):
+    """One pass of the oracle restatement of the reference over the sample, on `threads` host threads."""
     from oracle import oracle as O
     O.build()
     orc = O.Oracle()
-    threads = threads or os.cpu_count() or 1
-    probe = pairs[:max(threads, 8)]
     t = time.perf_counter()
-    orc.find_batch(probe, two_gap=(mode == 2), threads=threads)
-    dt = max(time.perf_counter() - t, 1e-3)
-    n = int(min(len(pairs), max(len(probe), len(probe) * target_s / dt)))
-    # the probe's first pairs need not be typical: keep adding chunks of the workload in order until the sample
-    # has run for about target_s
-    done, tot, dt = 0, 0, 0.0
-    while True:
-        t = time.perf_counter()
-        _, _, cells = orc.find_batch(pairs[done:n], two_gap=(mode == 2), threads=threads)
-        dt += time.perf_counter() - t
-        tot += cells["scan"] + cells["scan_rev"] + cells["xdrop"] + cells["semiglobal"]
-        done = n
-        if dt >= 0.8 * target_s or n >= len(pairs):
-            break
-        n = int(min(len(pairs), n + max(threads, n / dt * (target_s - dt))))
-    return {"value": tot / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port",
-            "pairs_per_s": n / dt, "seconds": dt,
-            "sample": f"first {n} of {len(pairs)} pairs of the same workload, {threads} threads"}
+    _, _, cells = orc.find_batch(sample, two_gap=(mode == 2), threads=threads)
+    dt = max(time.perf_counter() - t, 1e-6)
+    tot = cells["scan"] + cells["scan_rev"] + cells["xdrop"] + cells["semiglobal"]
+    return {"value": tot / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port", "pairs_per_s": len(sample) / dt,
+            "seconds": dt, "sample": desc}
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU implementation of the path (the oracle restatement: the reference sources do not travel
+    to the GPU host) on every host thread, each step one pass over the fixed sample that the GPU arm's cpu_baseline
+    also times; warm-up steps pass over its first eighth."""
     if rank != 0:
         return
     pairs = workload(args.pairs)
-    steps = []
-    cb = None
+    threads = host_threads()
+    sample, desc = cpu_sample(pairs, threads)
     for _ in range(args.warmup):
-        cpu_baseline(pairs, args.mode, min(args.cpu_seconds, 5.0))
-    for _ in range(args.steps):
-        cb = cpu_baseline(pairs, args.mode, args.cpu_seconds / max(args.steps, 1) * 2)
-        steps.append(cb)
+        cpu_baseline(sample[:max(1, len(sample) // 8)], desc, args.mode, threads)
+    steps = [cpu_baseline(sample, desc, args.mode, threads) for _ in range(args.steps)]
     val = statistics.median(s["value"] for s in steps)
-    cb["value"] = val
+    cb = dict(steps[-1], value=val, seconds=statistics.median(s["seconds"] for s in steps))
     line = {"impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": "GCUPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1000 * statistics.median(s["seconds"] for s in steps), 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic (seeded)", "config": {"workload": workload_name(args.pairs, args.mode), "mode": args.mode, "pairs": args.pairs,
-                                                    "l2": "cpu"},
+            "data": "synthetic (seeded)", "config": bench_config(args.pairs, args.mode, world),
             "pairs_per_s": round(statistics.median(s["pairs_per_s"] for s in steps), 2),
             "cpu_baseline": cb, "e2e": {"value": round(val, 4), "unit": "GCUPS", "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def hbm_peak():
+    """The measured copy bandwidth of the GB300s (MEASURED_PEAKS.json), else the stated fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def line_two_gap(eng, timed, pairs, threads, gpu, n=2000, steps=3):
+    """cut2Gaps (2-piece) path over the first n pairs of the batched workload, resident on the device: GCUPS of the
+    whole path, and the semi-global DP kernel (sg_kernel) and its traceback alone (CUDA events)."""
+    sub = pairs[:n]
+    b = eng.upload(sub)
+    eng.align_resident(b, 2)
+    tot_ms, cells, sg_ms, sgtb_ms, sg_cells, sg_bytes = 0.0, 0, 0.0, 0.0, 0, 0
+    with ClockSampler(gpu) as clk:
+        for _ in range(steps):
+            _, t = timed(lambda: eng.align_resident(b, 2))
+            st = eng.last_stats()
+            tot_ms += t
+            cells += cells_of(st)
+            sg_ms += st["ms_sg_kernel"]
+            sgtb_ms += st["ms_sg_tb_kernel"]
+            sg_cells += st["cells_semiglobal"]
+            sg_bytes += st["bytes_codes_sg"]
+    eng.free_batch(b)
+    sample, desc = cpu_sample(sub, threads, per_thread=32)
+    return {"workload": f"batched pairs, first {n:,}, cut2Gaps path (2-piece semi-global after the 1-gap seeds)",
+            "value": round(cells / (tot_ms * 1e-3) / 1e9, 3), "unit": "GCUPS", "steps": steps,
+            "ms_per_step": round(tot_ms / steps, 2), "pairs_per_s": round(n * steps / (tot_ms * 1e-3), 1),
+            "sg_kernel": {"ms_per_step": round(sg_ms / steps, 2), "gcups": round(sg_cells / (sg_ms * 1e-3) / 1e9, 2),
+                          "traceback_ms_per_step": round(sgtb_ms / steps, 2),
+                          "codes_gb_per_s": round(sg_bytes / (sg_ms * 1e-3) / 1e9, 2),
+                          "timing": "CUDA events around each semi-global DP and traceback launch"},
+            "cpu_baseline": cpu_baseline(sample, desc, 2, threads), "clocks": clk.summary()}
+
+
+def line_long_pairs(eng, timed, threads, gpu, scan_peak, n=8, steps=2, cpu_query=2000):
+    """Long pairs: n whole 200 kb x ~234 kb pairs (the long-pair workload's first n), cut1Gap path, resident; the
+    seed-scan kernel's GCUPS against the live integer-issue ceiling.  The CPU baseline aligns the first cpu_query bases
+    of each query of the first `threads` pairs against their whole references (one slice per thread)."""
+    from dcns_gb300 import workloads as W
+    pairs = W.long_pairs_200kb(n_pairs=max(n, threads))
+    b = eng.upload(pairs[:n])
+    eng.align_resident(b, 1)
+    tot_ms, cells, scan_ms, scan_cells, nfrag = 0.0, 0, 0.0, 0, 0
+    with ClockSampler(gpu) as clk:
+        for _ in range(steps):
+            res, t = timed(lambda: eng.align_resident(b, 1))
+            st = eng.last_stats()
+            tot_ms += t
+            cells += cells_of(st)
+            scan_ms += st["ms_scan_kernel"]
+            scan_cells += st["cells_scan"]
+            nfrag = sum(len(f) for f in res)
+    eng.free_batch(b)
+    from oracle import oracle as O
+    O.build()
+    slices = [(a, q[:cpu_query]) for a, q in pairs[:threads]]
+    t0 = time.perf_counter()
+    _, _, cc = O.Oracle().find_batch(slices, threads=threads)
+    dt = time.perf_counter() - t0
+    cpu_cells = cc["scan"] + cc["scan_rev"] + cc["xdrop"] + cc["semiglobal"]
+    achieved = scan_cells / (scan_ms * 1e-3) / 1e9
+    return {"workload": f"long pairs: {n} whole pairs of 200 kb x ~234 kb (GC 45 %, 500 planted segments, 5 "
+                        f"duplicated 2-10 kb blocks), cut1Gap path",
+            "value": round(cells / (tot_ms * 1e-3) / 1e9, 3), "unit": "GCUPS", "steps": steps,
+            "ms_per_step": round(tot_ms / steps, 2), "pairs_per_s": round(n * steps / (tot_ms * 1e-3), 2),
+            "fragments": nfrag,
+            "scan_roofline": {"kernel": "scan_kernel<38> (row-chunked)", "achieved": round(achieved, 1),
+                              "peak": round(scan_peak, 1), "unit": "GCUPS", "frac": round(achieved / scan_peak, 4),
+                              "share_of_step": round(scan_ms / tot_ms, 4)},
+            "cpu_baseline": {"value": cpu_cells / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port",
+                             "seconds": dt, "sample": f"the first {cpu_query} bases of the query of each of the first "
+                                                      f"{len(slices)} pairs against its whole 200 kb reference, one "
+                                                      f"slice per thread"},
+            "clocks": clk.summary()}
+
+
+def _seed_chunk(c):
+    from dcns_gb300 import workloads as W
+    return W.extension_seeds(n_seeds=10000, seed=20261207 + c)
+
+
+def extension_workload(n):
+    """n extension-stress seeds: chunks of 10,000 drawn by the workload's generator with seeds 20261207 + c (chunk 0
+    is the reference-digested set), generated in a process pool."""
+    import multiprocessing as mp
+    chunks = (n + 9999) // 10000
+    with mp.get_context("spawn").Pool(max(1, min(host_threads(), chunks))) as pool:
+        parts = pool.map(_seed_chunk, range(chunks))
+    return [t for p in parts for t in p][:n]
+
+
+def line_extension_seeds(eng, n, threads, gpu, steps=3):
+    """Extension stress: n seeds through x_extend_seed's two SemiGlobal_xextend passes (forward, then with the
+    traceback: 4-bit direction codes written, the traceback walk, CIGARs packed on the device) by the C ABI call on
+    host buffers, so each step includes the upload of the codes and the download of the results."""
+    import ctypes as C
+    import dcns_gb300 as D
+    t0 = time.perf_counter()
+    tasks = extension_workload(n)
+    gen_s = time.perf_counter() - t0
+    arr, keep = eng.prepare(tasks)
+    out = np.zeros((n, 6), np.int32)
+    cap = int(keep[1]["len1"].sum()) + int(keep[1]["len2"].sum()) + 4 * n + 4
+    cig = np.zeros(cap, np.uint32)
+    off = np.zeros(n + 1, np.int64)
+    p = D.params()
+    lib = eng.lib
+
+    def call(want):
+        rc = lib.dcns_xextend_batch(eng.h, arr, n, C.byref(p), want, out.ctypes.data_as(D._I32P),
+                                    cig.ctypes.data_as(D._U32P), cap, off.ctypes.data_as(D._I64P))
+        if rc != 0:
+            raise D.DcnsError(rc, lib.dcns_last_error(eng.h).decode())
+        return eng.last_stats()
+
+    call(0), call(1)
+    wall, cells, k_ms, tb_ms, code_bytes, path_cells = 0.0, 0, 0.0, 0.0, 0, 0
+    with ClockSampler(gpu) as clk:
+        for _ in range(steps):
+            t = time.perf_counter()
+            s0 = call(0)
+            s1 = call(1)
+            wall += time.perf_counter() - t
+            cells += s0["cells_xdrop"] + s1["cells_xdrop"]
+            k_ms += s1["ms_xdrop_kernel"]
+            tb_ms += s1["ms_xdrop_tb_kernel"]
+            code_bytes += s1["bytes_codes_xdrop"]
+            path_cells += int((cig[:off[-1]] >> 4).sum())
+    peak, kind = hbm_peak()
+    codes_gbs = code_bytes / (k_ms * 1e-3) / 1e9
+    tb_gbs = path_cells * 0.5 / (tb_ms * 1e-3) / 1e9
+    per_thread = 5000  # about 10 s of both passes on a Grace core
+    sample = tasks[::max(1, n // (per_thread * threads))][:per_thread * threads]
+    from oracle import oracle as O
+    O.build()
+    t = time.perf_counter()
+    _, _, cpu_cells = O.Oracle().xextend_batch(sample, threads=threads)
+    dt = time.perf_counter() - t
+    return {"workload": f"extension stress: {n:,} seeds (38 bp core, 50-2000 bp flanks at 50-98 % identity), both "
+                        f"x_extend_seed passes per seed",
+            "value": round(cells / wall / 1e9, 3), "unit": "GCUPS", "steps": steps,
+            "ms_per_step": round(wall / steps * 1e3, 2), "seeds_per_s": round(n * steps / wall, 1),
+            "e2e": "C ABI call on host buffers: upload of the codes and download of the results in every step",
+            "xdrop_kernels": {"traceback_pass_level_kernels_ms": round(k_ms / steps, 2),
+                              "traceback_kernels_ms": round(tb_ms / steps, 2),
+                              "codes_written_gb_per_s": round(codes_gbs, 2),
+                              "traceback_read_gb_per_s": round(tb_gbs, 2),
+                              "hbm_peak_gb_per_s": peak, "peak_kind": kind,
+                              "codes_frac_of_peak": round(codes_gbs / peak, 5),
+                              "bytes": "codes: 4 bits per final-width band cell of the traceback pass; traceback: "
+                                       "4 bits per path cell"},
+            "generation_s": round(gen_s, 1),
+            "cpu_baseline": {"value": cpu_cells / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port",
+                             "seconds": dt, "sample": f"every {max(1, n // (per_thread * threads))}th seed "
+                                                      f"({len(sample)} seeds), both passes, {threads} threads"},
+            "clocks": clk.summary()}
 
 
 def main():
@@ -219,8 +399,8 @@ def main():
 
     # ---- value: resident sequences (pipeline shape chosen by the library's autotuner on this batch first)
     batch = eng.upload(pairs)
-    tuned = ({"lanes": 4, "bins": 4, "bin_ratio": 0.6, "autotuned": False} if args.no_autotune
-             else eng.autotune(batch, args.mode))
+    tuned = dict(eng.tuning(), autotuned=False) if args.no_autotune else dict(eng.autotune(batch, args.mode),
+                                                                               autotuned=True)
     for _ in range(max(args.warmup, 3)):
         eng.align_resident(batch, args.mode)
     if dist:
@@ -341,13 +521,20 @@ def main():
             "workload": "1,200 requests: log-normal median 4 kb, sigma 1.0, 0.2-100 kb, 10 % of 50-100 kb",
             **serve(1000.0, W.serving_requests(n_requests=1200), 5)}
 
-    cb = cpu_baseline(pairs, args.mode, args.cpu_seconds)
+        # the other benchmark configurations, each on its own sample with its own CPU baseline and clock record
+        threads = host_threads()
+        extras["two_gap"] = line_two_gap(eng, timed, pairs, threads, local)
+        extras["long_pairs"] = line_long_pairs(eng, timed, threads, local, peak)
+        extras["extension_seeds"] = line_extension_seeds(eng, args.ext_seeds, threads, local)
+
+    threads = host_threads()
+    sample, desc = cpu_sample(pairs, threads)
+    cb = cpu_baseline(sample, desc, args.mode, threads)
     line = {
         "metric": METRIC, "value": round(gcups, 3), "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": round(tot_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int16x2 (seed scan) / int32", "data": "synthetic (seeded)",
-        "config": {"workload": workload_name(n, args.mode), "pairs": n, "mode": args.mode, "parallelism": f"replicas x{world}",
-                   "l2": "flushed (256 MB write) between timed steps", "pipeline": tuned},
+        "config": bench_config(n, args.mode, world), "pipeline": tuned,
         "pairs_per_s": round(pairs_s, 2), "fragments": nfrag,
         "e2e": {"value": round(e2e_all_cells / (e2e_tot * 1e-3) / 1e9, 3), "unit": "GCUPS",
                 "pairs_per_s": round(R.whole_job_rate(n * args.steps, world, e2e_tot), 2),
@@ -355,7 +542,7 @@ def main():
         "roofline": roofline, "cpu_baseline": cb, "gpu_launches": launches, "clocks": clk.summary(),
         "stages_ms": {k: round(last_stats[k], 2) for k in ("ms_scan_kernel", "ms_scan_prep", "ms_scan_xfer",
                                                             "ms_replay", "ms_link", "ms_xdrop", "ms_xdrop_kernel",
-                                                            "ms_semiglobal", "ms_total")},
+                                                            "ms_xdrop_tb_kernel", "ms_semiglobal", "ms_total")},
         "rounds": {k: last_stats[k] for k in ("scan_rounds", "xdrop_rounds", "kernel_launches", "seeds",
                                               "xdrop_passes", "tasks_scan")},
     }

@@ -119,10 +119,34 @@ class Stats(C.Structure):
                                           "ms_download", "ms_total", "ms_scan_kernel", "ms_scan_prep",
                                           "ms_scan_xfer", "ms_link")] + \
                [("scan_launches", C.c_int32), ("kernel_launches", C.c_int32), ("scan_rounds", C.c_int32),
-                ("xdrop_rounds", C.c_int32), ("ms_xdrop_kernel", C.c_double), ("bytes_h2d", C.c_int64)]
+                ("xdrop_rounds", C.c_int32), ("ms_xdrop_kernel", C.c_double), ("bytes_h2d", C.c_int64),
+                ("ms_xdrop_tb_kernel", C.c_double), ("ms_sg_kernel", C.c_double), ("ms_sg_tb_kernel", C.c_double),
+                ("bytes_codes_xdrop", C.c_int64), ("bytes_codes_sg", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServingStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "cancelled", "batches", "max_batch",
+                                         "nomem_splits", "solo_retries", "queued", "pending")] + \
+               [("workers", C.c_int32), ("pad", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("lanes", C.c_int32), ("bins", C.c_int32), ("bin_ratio", C.c_double),
+                ("scan_tiles_per_thread", C.c_int32), ("sg_warps", C.c_int32), ("n_bins_tuned", C.c_int32),
+                ("xdrop_warp_from", C.c_int32 * 16), ("xdrop_wave_max_w", C.c_int32 * 16), ("xdrop_flat", C.c_int32 * 16)]
+
+    def as_dict(self):
+        n = max(self.n_bins_tuned, 1)
+        return {"lanes": self.lanes, "bins": self.bins, "bin_ratio": self.bin_ratio,
+                "scan_tiles_per_thread": self.scan_tiles_per_thread, "sg_warps": self.sg_warps,
+                "xdrop_per_bin": [{"warp_from": self.xdrop_warp_from[b], "wave_max_w": self.xdrop_wave_max_w[b],
+                                   "row_interleaved": bool(self.xdrop_flat[b])} for b in range(n)]}
 
 
 class Results(C.Structure):
@@ -173,6 +197,7 @@ def _bind(lib):
     lib.dcns_align_weighted.argtypes = [C.c_void_p, P(Pair), C.c_int64, P(C.c_int16), _I32P, C.c_int32, C.c_int,
                                         P(Params), P(P(Results))]
     lib.dcns_align_seeded.argtypes = [C.c_void_p, P(Pair), C.c_int64, _I32P, _I64P, P(Params), P(P(Results))]
+    lib.dcns_align_xseeds.argtypes = lib.dcns_align_seeded.argtypes
     lib.dcns_format_records.argtypes = [C.c_int64, _I64P, _U32P, _F64P, C.c_char_p, C.c_int64, C.c_char_p,
                                         C.c_int64, C.c_int, C.c_int, C.c_int32, C.c_int32, C.c_char_p, C.c_char_p,
                                         P(C.c_void_p), P(C.c_int64), P(C.c_void_p), P(C.c_int64)]
@@ -196,6 +221,10 @@ def _bind(lib):
     lib.dcns_poll.argtypes = [C.c_void_p, C.c_uint64, P(P(Results))]
     lib.dcns_serve_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_int64, P(P(Results))]
     lib.dcns_serve_stop.argtypes = [C.c_void_p]
+    lib.dcns_cancel.argtypes = [C.c_void_p, C.c_uint64]
+    lib.dcns_get_tuning.argtypes = [C.c_void_p, P(Tuning)]
+    lib.dcns_serve_set_shape.argtypes = [C.c_void_p, C.c_int, C.c_int64, C.c_int64]
+    lib.dcns_serve_stats.argtypes = [C.c_void_p, P(ServingStats)]
     return lib
 
 
@@ -442,7 +471,13 @@ class Engine:
         lanes, bins, ratio = C.c_int(), C.c_int(), C.c_double()
         self._check(self.lib.dcns_autotune(self.h, batch, C.byref(params(**kw)), mode, C.byref(lanes),
                                            C.byref(bins), C.byref(ratio)))
-        return {"lanes": lanes.value, "bins": bins.value, "bin_ratio": ratio.value}
+        return self.tuning()
+
+    def tuning(self) -> dict:
+        """The context's kernel shapes: pipeline shape, scan tiling, 2-piece warps and the per-bin x-drop forms."""
+        t = Tuning()
+        self._check(self.lib.dcns_get_tuning(self.h, C.byref(t)))
+        return t.as_dict()
 
     def last_stats(self) -> dict:
         s = Stats()
@@ -496,6 +531,14 @@ class Engine:
 
     def align_seeded(self, pairs, seeds, max_align_len=0, **kw):
         """cut2Gaps2's seeded 2-gap overload: seeds[k] = [(start1, end1, start2, end2), ...] 0-based, for pair k."""
+        return self._seeded(self.lib.dcns_align_seeded, pairs, seeds, max_align_len=max_align_len, **kw)
+
+    def align_xseeds(self, pairs, seeds, **kw):
+        """The x-seed overload without maximumAlignLength (findSimilar...4.cpp:532): the 2-piece stage on the given
+        x-seeds (seeds[k] = [(start1, end1, start2, end2), ...] 0-based, for pair k)."""
+        return self._seeded(self.lib.dcns_align_xseeds, pairs, seeds, **kw)
+
+    def _seeded(self, fn, pairs, seeds, **kw):
         arr, keep = _pairs(pairs)
         flat = np.zeros((max(1, sum(len(s) for s in seeds)), 4), np.int32)
         off = np.zeros(len(keep) + 1, np.int64)
@@ -505,10 +548,10 @@ class Engine:
                 flat[q] = x
                 q += 1
             off[k + 1] = q
-        p = params(max_align_len=max_align_len, **kw)
+        p = params(**kw)
         res = C.POINTER(Results)()
-        self._check(self.lib.dcns_align_seeded(self.h, arr, len(keep), flat.ctypes.data_as(_I32P),
-                                               off.ctypes.data_as(_I64P), C.byref(p), C.byref(res)))
+        self._check(fn(self.h, arr, len(keep), flat.ctypes.data_as(_I32P), off.ctypes.data_as(_I64P), C.byref(p),
+                       C.byref(res)))
         try:
             return _unpack(res)
         finally:
@@ -593,9 +636,32 @@ class Engine:
         return sc[:len(keep) - 1, :nw], mx[:len(keep) - 1, :nw]
 
     # -------------------------------------------------------------- serving loop
-    def serve_start(self, mode=MODE_ONE_GAP, max_inflight=256, **kw):
+    def serve_start(self, mode=MODE_ONE_GAP, max_inflight=256, workers=3, batch_cells=0, admit_bytes=0, **kw):
+        """Starts the continuous-batching loop (workers: 1..8; batch_cells / admit_bytes: the batch caps in predicted
+        level-0 scan cells and device bytes, 0 = defaults)."""
+        self._check(self.lib.dcns_serve_set_shape(self.h, int(workers), int(batch_cells), int(admit_bytes)))
         self._serve_params = params(**kw)
         self._check(self.lib.dcns_serve_start(self.h, C.byref(self._serve_params), mode, max_inflight))
+
+    def cancel(self, ticket: int):
+        self._check(self.lib.dcns_cancel(self.h, ticket))
+
+    def poll(self, ticket: int):
+        """The result if done, None while pending (raises on a failed or unknown ticket)."""
+        res = C.POINTER(Results)()
+        rc = self.lib.dcns_poll(self.h, ticket, C.byref(res))
+        if rc == -6:
+            return None
+        self._check(rc)
+        try:
+            return _unpack(res)[0]
+        finally:
+            self.lib.dcns_results_free(res)
+
+    def serve_stats(self) -> dict:
+        s = ServingStats()
+        self._check(self.lib.dcns_serve_stats(self.h, C.byref(s)))
+        return s.as_dict()
 
     def submit(self, seq1, seq2) -> int:
         arr, keep = _pairs([(seq1, seq2)])

@@ -135,8 +135,9 @@ struct SgWeights {
 };
 constexpr int kSgwMaxCats = 64;
 
-// The semi-global kernel (semiglobal.cu): warps per CTA (one CTA runs one DP, warp w owns stripes w, w+8, ...) and the
-// boundary record a stripe leaves for the next one in global scratch (kSgNW slots of max_n2 + 2 records per CTA).
+// The semi-global kernel (semiglobal.cu): the largest of its CTA shapes (2, 4 or kSgNW warps; one CTA runs one DP,
+// warp w owns stripes w, w+nw, ...) and the boundary record a stripe leaves for the next one in global scratch (nw
+// slots of max_n2 + 2 records per CTA).
 constexpr int kSgNW = 8;
 struct SgRec {
   int m, f1, f2;
@@ -163,19 +164,21 @@ void launch_xdrop(XTask *tasks, const int *idx, int n, Arena ar, Params p, uint3
 void launch_xdrop_traceback(XTask *tasks, const int *idx, int n, const uint32_t *tb, uint32_t *cig, cudaStream_t st);
 // Chained x-drop levels (one launch per band width, work lists and counts in device memory).
 void launch_xdrop_iota(int *list, int n, int *count, cudaStream_t st);
+// fetch: the level's pass counter, zero before the launch (the row-interleaved register-band kernel, flat = true).
 void launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
-                        int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, Arena ar,
-                        Params p, uint32_t *tb, int w, int n_bound, int nsm, int32_t *scratch, int64_t per_warp,
-                        int warps, int warp_from, int wave_max_w, cudaStream_t st);
+                        int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int *fetch,
+                        Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm, int32_t *scratch,
+                        int64_t per_warp, int warps, int warp_from, int wave_max_w, bool flat, cudaStream_t st);
 void launch_xdrop_traceback_all(XTask *tasks, int n, const uint32_t *tb, uint32_t *cig,
                                 unsigned long long *cig_cursor, cudaStream_t st);
 // Packs the CIGARs of every finished task in task order into dense (cig_dense offsets); *total = their words.
 void launch_xdrop_cigar_pack(XTask *tasks, int n, const uint32_t *cig, uint32_t *dense, unsigned long long *total,
                              cudaStream_t st);
+// nw: warps per DP (2, 4 or kSgNW); bnd: sg_bnd_bytes(grid, max_n2, nw) bytes.
 void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p, uint8_t *tb, void *bnd,
-                       int max_n2, int *work_counter, int grid, cudaStream_t st);
-int sg_ctas_per_sm();
-int64_t sg_bnd_bytes(int grid, int max_n2);
+                       int max_n2, int *work_counter, int grid, int nw, cudaStream_t st);
+int sg_ctas_per_sm(int nw);
+int64_t sg_bnd_bytes(int grid, int max_n2, int nw);
 void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, uint32_t *cig,
                          cudaStream_t st, bool weighted_layout = false);
 int64_t sg_tb_bytes(int n1, int n2, int w);

@@ -89,11 +89,16 @@ void HostBuf::release() {
   cap = 0;
 }
 
+void release_device_buffers(Context &C) {
+  if (C.st) cudaStreamSynchronize(C.st);  // nothing of the context still reads them
+  DevBuf *bufs[] = {&C.d_codes, &C.d_srcoff, &C.d_dstbase, &C.d_len, &C.d_pk, &C.d_nm, &C.d_seqbase, &C.d_flag,
+                    &C.d_tasks, &C.d_keys, &C.d_tiles, &C.d_counter, &C.d_idx, &C.d_scratch, &C.d_x, &C.d_tb,
+                    &C.d_cig, &C.d_sg, &C.d_sgtb, &C.d_bnd, &C.d_wts, &C.d_cats};
+  for (DevBuf *b : bufs) b->release(C);
+}
+
 Context::~Context() {
-  DevBuf *bufs[] = {&d_codes, &d_srcoff, &d_dstbase, &d_len, &d_pk, &d_nm, &d_seqbase, &d_flag, &d_tasks, &d_keys,
-                    &d_tiles, &d_counter, &d_idx, &d_scratch, &d_x, &d_tb, &d_cig, &d_sg, &d_sgtb, &d_bnd,
-                    &d_wts, &d_cats};
-  for (DevBuf *b : bufs) b->release(*this);
+  release_device_buffers(*this);
   h_codes.release();
   h_misc.release();
   h_out.release();
@@ -101,6 +106,7 @@ Context::~Context() {
   h_tiles.release();
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
+  if (ev2) cudaEventDestroy(ev2);
   if (ev_bulk) cudaEventDestroy(ev_bulk);
   if (st_bulk) cudaStreamDestroy(st_bulk);
   if (st) cudaStreamDestroy(st);
@@ -129,6 +135,7 @@ void init_context(Context &C, int device, size_t budget) {
   DCNS_CK(cudaEventCreateWithFlags(&C.ev_bulk, cudaEventDisableTiming));
   DCNS_CK(cudaEventCreate(&C.ev0));
   DCNS_CK(cudaEventCreate(&C.ev1));
+  DCNS_CK(cudaEventCreate(&C.ev2));
   if (budget == 0) {
     size_t fr = 0, tot = 0;
     DCNS_CK(cudaMemGetInfo(&fr, &tot));
@@ -140,6 +147,12 @@ void init_context(Context &C, int device, size_t budget) {
   if (const char *e = std::getenv("DCNS_TRACE")) C.trace = std::atoi(e);
   if (const char *e = std::getenv("DCNS_XDROP_WARP_FROM")) C.xdrop_warp_from = std::max(0, std::atoi(e));
   if (const char *e = std::getenv("DCNS_XDROP_WAVE")) C.xdrop_wave_max_w = std::max(0, std::atoi(e));
+  if (const char *e = std::getenv("DCNS_XDROP_FLAT")) C.xdrop_flat = std::atoi(e) != 0;
+  if (const char *e = std::getenv("DCNS_SCAN_TILES")) C.scan_tiles_per_thread = std::max(1, std::min(64, std::atoi(e)));
+  if (const char *e = std::getenv("DCNS_SG_WARPS")) {
+    const int v = std::atoi(e);
+    C.sg_warps = (v == 2 || v == 4 || v == kSgNW) ? v : 0;
+  }
   if (const char *e = std::getenv("DCNS_BIN_RATIO")) C.bin_ratio = std::max(0.1, std::min(1.0, std::atof(e)));
 }
 
@@ -157,7 +170,10 @@ Params to_params(const dcns_params *p) {
   P.w = p->w;
   P.xdrop = p->xdrop;
   P.zdrop = p->zdrop;
-  P.bandwidth = p->bandwidth;
+  // A band wider than every sequence gives the same DP as an unbounded one, and sequences are shorter than
+  // kMaxSeqLen (upload_into rejects longer ones), so wider bands are clamped: the kernels' band-edge arithmetic
+  // (i + w, 2w + stripe rows) then stays inside int32.
+  P.bandwidth = std::min(p->bandwidth, kMaxSeqLen);
   P.max_align_len = p->max_align_len;
   P.pvalue = p->pvalue;
   P.lambda = p->lambda;
@@ -339,6 +355,7 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
       const int32_t n = h ? pairs[k].n2 : pairs[k].n1;
       const int8_t *src = h ? pairs[k].s2 : pairs[k].s1;
       if (n < 0) throw Error(DCNS_ERR_INVALID, "negative sequence length");
+      if (n >= kMaxSeqLen) throw Error(DCNS_ERR_INVALID, "sequences must be shorter than 2^28 bases");
       if (n > 0) {
         auto it = seen.find(src);
         if (it != seen.end() && it->second.first == n) {
@@ -528,7 +545,7 @@ void compute_scan_tasks(Context &C, ScanState &S, const Params &P) {
     total_rows += hi - lo;
   }
   const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * kScanThreads;
-  const int64_t want_tiles = 8 * resident;
+  const int64_t want_tiles = (int64_t)C.scan_tiles_per_thread * resident;
   const int K = warmup_rows(P, kScanW);
   int64_t chunk = INT32_MAX;
   if (nd < want_tiles && K != INT_MAX && total_rows > 0)
@@ -645,8 +662,9 @@ int64_t scan_level0(Context &C, ScanState &S, const std::vector<PairIn> &pairs, 
   const int64_t resident = (int64_t)C.nsm * C.scan_blocks_per_sm * kScanThreads;
   const int K = warmup_rows(P, kScanW);
   int64_t chunk = INT32_MAX;
-  if (nduo < 8 * resident && K != INT_MAX && total_rows > 0)
-    chunk = std::min<int64_t>(INT32_MAX, std::max<int64_t>(4 * (int64_t)K, (total_rows + 8 * resident - 1) / (8 * resident)));
+  const int64_t want = (int64_t)C.scan_tiles_per_thread * resident;
+  if (nduo < want && K != INT_MAX && total_rows > 0)
+    chunk = std::min<int64_t>(INT32_MAX, std::max<int64_t>(4 * (int64_t)K, (total_rows + want - 1) / want));
 
   std::vector<int64_t> order(np);
   for (int64_t p = 0; p < np; ++p) order[p] = p;
@@ -1092,13 +1110,20 @@ void run_xdrop_rounds(Context &C, std::vector<XTask> &X, const Params &P, bool w
       C.d_cig.ensure(C, sizeof(uint32_t) * std::max<int64_t>(cw, 1));
       h2d(C, C.d_x, Xc, (size_t)m);
       h2d(C, C.d_idx, fin_c.data(), fin_c.size());
+      DCNS_CK(cudaEventRecord(C.ev1, C.st));
       launch_xdrop_traceback(C.d_x.as<XTask>(), C.d_idx.as<int>(), (int)fin_c.size(), C.d_tb.as<uint32_t>(),
                              C.d_cig.as<uint32_t>(), C.st);
+      DCNS_CK(cudaEventRecord(C.ev2, C.st));
       C.stats.kernel_launches += 1;
       C.h_out.ensure(sizeof(uint32_t) * std::max<int64_t>(cw, 1));
       d2h(C, Xc, C.d_x, (size_t)m);
       d2h(C, C.h_out.as<uint32_t>(), C.d_cig, (size_t)cw);
       sync(C);
+      {
+        float ms = 0;
+        DCNS_CK(cudaEventElapsedTime(&ms, C.ev1, C.ev2));
+        C.stats.ms_xdrop_tb_kernel += ms;
+      }
       tp = phase(C, "xd_tb_sync", tp);
       const uint32_t *hc = C.h_out.as<uint32_t>();
       int64_t total = (int64_t)flat->size();
@@ -1173,7 +1198,7 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
       scratch_ints = std::max(scratch_ints, warps[L] * per_warp[L]);
     }
     C.d_x.ensure(C, sizeof(XTask) * n);
-    C.d_idx.ensure(C, sizeof(int32_t) * (3 * n + 64));
+    C.d_idx.ensure(C, sizeof(int32_t) * (3 * n + 4 + nlev + 64));
     C.d_counter.ensure(C, 64);
     if (want_codes) {
       C.d_tb.ensure(C, sizeof(uint32_t) * tb_words);
@@ -1181,10 +1206,10 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
     }
     if (scratch_ints > 1) C.d_scratch.ensure(C, sizeof(int32_t) * scratch_ints);
     int *lists = C.d_idx.as<int>();
-    int *cnt = lists + 3 * n;  // [0], [1]: the two work-list counts, [2]: retry count
+    int *cnt = lists + 3 * n;  // [0], [1]: the two work-list counts, [2]: retry count, [4 + L]: level L's fetch
     unsigned long long *cur = C.d_counter.as<unsigned long long>();  // [0]: traceback arena, [1]: CIGAR arena
     h2d(C, C.d_x, X.data(), (size_t)n);
-    DCNS_CK(cudaMemsetAsync(cnt, 0, sizeof(int) * 4, C.st));
+    DCNS_CK(cudaMemsetAsync(cnt, 0, sizeof(int) * (4 + nlev), C.st));
     DCNS_CK(cudaMemsetAsync(cur, 0, sizeof(unsigned long long) * 2, C.st));
     launch_xdrop_iota(lists, (int)n, cnt, C.st);
     DCNS_CK(cudaEventRecord(C.ev0, C.st));
@@ -1193,9 +1218,9 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
       const int out = 1 - in;
       DCNS_CK(cudaMemsetAsync(cnt + out, 0, sizeof(int), C.st));
       launch_xdrop_level(C.d_x.as<XTask>(), lists + in * n, cnt + in, lists + out * n, cnt + out, lists + 2 * n,
-                         cnt + 2, cur, want_codes ? tb_words : 0, C.arena, P, C.d_tb.as<uint32_t>(), w0 << L, (int)n,
-                         C.nsm, C.d_scratch.as<int32_t>(), per_warp[L], warps[L], C.xdrop_warp_from,
-                         C.xdrop_wave_max_w, C.st);
+                         cnt + 2, cur, want_codes ? tb_words : 0, cnt + 4 + L, C.arena, P, C.d_tb.as<uint32_t>(),
+                         w0 << L, (int)n, C.nsm, C.d_scratch.as<int32_t>(), per_warp[L], warps[L], C.xdrop_warp_from,
+                         C.xdrop_wave_max_w, C.xdrop_flat, C.st);
       in = out;
     }
     DCNS_CK(cudaEventRecord(C.ev1, C.st));
@@ -1204,6 +1229,7 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
                                  C.st);
       launch_xdrop_cigar_pack(C.d_x.as<XTask>(), (int)n, C.d_cig.as<uint32_t>(), C.d_cig.as<uint32_t>() + cig_words,
                               cur + 1, C.st);
+      DCNS_CK(cudaEventRecord(C.ev2, C.st));
     }
     C.stats.kernel_launches += nlev + 1 + (want_codes ? 3 : 0);
     C.stats.xdrop_rounds += 1;
@@ -1222,6 +1248,10 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
       float ms = 0;
       DCNS_CK(cudaEventElapsedTime(&ms, C.ev0, C.ev1));
       C.stats.ms_xdrop_kernel += ms;
+      if (want_codes) {
+        DCNS_CK(cudaEventElapsedTime(&ms, C.ev1, C.ev2));
+        C.stats.ms_xdrop_tb_kernel += ms;
+      }
     }
     if (hret[0] != 0) throw Error(DCNS_ERR_DEVICE, "x-drop band restarts did not converge");
     std::vector<int32_t> retry(hret + 8, hret + 8 + hret[1]);
@@ -1249,7 +1279,11 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
     run_xdrop_rounds(C, X, P, want_codes, flat, hoff, retry, true);
     tp = phase(C, "xc_retry", tp);
   }
-  for (int64_t k = 0; k < n; ++k) C.stats.cells_xdrop += band_cells(X[k].rows, X[k].w, X[k].n2);
+  for (int64_t k = 0; k < n; ++k) {
+    const int64_t cells = band_cells(X[k].rows, X[k].w, X[k].n2);
+    C.stats.cells_xdrop += cells;
+    if (want_codes) C.stats.bytes_codes_xdrop += (cells + 1) / 2;
+  }
   C.stats.ms_xdrop += ms_since(t0);
 }
 
@@ -1385,10 +1419,13 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
     if (want_codes) C.d_sgtb.ensure(C, (size_t)std::max<int64_t>(bytes, 1));
     // unweighted: one 8-warp CTA per DP; weighted: one warp per DP, 16 warps per SM.  (One warp per DP measured
     // 8.6x slower than the CTA pipeline on the unweighted 2-gap DPs of 2,000 log-normal pairs: 2819 vs 328 ms.)
-    const int grid = (int)std::min<int64_t>(m, W ? (int64_t)C.nsm * 16 : (int64_t)C.nsm * sg_ctas_per_sm());
+    // CTA shape of the unweighted kernel: many DPs run two warps each (short DPs stop within a few stripes, and more
+    // of them run at once); few DPs keep eight warps each for the stripes of long DPs
+    const int nw = C.sg_warps > 0 ? C.sg_warps : (m >= (int64_t)C.nsm * 8 ? 2 : kSgNW);
+    const int grid = (int)std::min<int64_t>(m, W ? (int64_t)C.nsm * 16 : (int64_t)C.nsm * sg_ctas_per_sm(nw));
     int maxn2 = 1;
     for (int64_t q = k0; q < k1; ++q) maxn2 = std::max(maxn2, G[q].n2);
-    C.d_bnd.ensure(C, (size_t)(W ? sgw_bnd_bytes((grid + 3) / 4 * 4, maxn2) : sg_bnd_bytes(grid, maxn2)));
+    C.d_bnd.ensure(C, (size_t)(W ? sgw_bnd_bytes((grid + 3) / 4 * 4, maxn2) : sg_bnd_bytes(grid, maxn2, nw)));
     C.d_counter.ensure(C, 64);
     DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int), C.st));
     // largest DPs first: the CTA work queue then finishes with the small ones
@@ -1402,17 +1439,25 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
     C.d_idx.ensure(C, sizeof(int32_t) * m);
     h2d(C, C.d_idx, idx.data(), (size_t)m);
     h2d(C, C.d_sg, G.data(), (size_t)n);
+    DCNS_CK(cudaEventRecord(C.ev0, C.st));
     if (W)
       launch_semiglobal_weighted(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, *W,
                                  C.d_sgtb.as<uint8_t>(), C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, C.st);
     else
       launch_semiglobal(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, C.d_sgtb.as<uint8_t>(),
-                        C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, C.st);
+                        C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, nw, C.st);
+    DCNS_CK(cudaEventRecord(C.ev1, C.st));
     C.stats.kernel_launches += 1;
     C.stats.semiglobal_dps += m;
+    auto kernel_ms = [&](cudaEvent_t a, cudaEvent_t b) {
+      float ms = 0;
+      DCNS_CK(cudaEventElapsedTime(&ms, a, b));
+      return (double)ms;
+    };
     if (want_codes) {
       d2h(C, G.data(), C.d_sg, (size_t)n);
       sync(C);
+      C.stats.ms_sg_kernel += kernel_ms(C.ev0, C.ev1);
       int64_t cw = 0;
       for (int64_t q = k0; q < k1; ++q) {
         G[q].cig_off = cw;
@@ -1421,13 +1466,16 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
       }
       C.d_cig.ensure(C, sizeof(uint32_t) * std::max<int64_t>(cw, 1));
       h2d(C, C.d_sg, G.data(), (size_t)n);
+      DCNS_CK(cudaEventRecord(C.ev0, C.st));
       launch_sg_traceback(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, P.bandwidth, C.d_sgtb.as<uint8_t>(),
                           C.d_cig.as<uint32_t>(), C.st, W != nullptr);
+      DCNS_CK(cudaEventRecord(C.ev1, C.st));
       C.stats.kernel_launches += 1;
       C.h_out.ensure(sizeof(uint32_t) * std::max<int64_t>(cw, 1));
       d2h(C, G.data(), C.d_sg, (size_t)n);
       d2h(C, C.h_out.as<uint32_t>(), C.d_cig, (size_t)cw);
       sync(C);
+      C.stats.ms_sg_tb_kernel += kernel_ms(C.ev0, C.ev1);
       const uint32_t *hc = C.h_out.as<uint32_t>();
       for (int64_t q = k0; q < k1; ++q) {
         if (G[q].status != 0) throw Error(DCNS_ERR_DEVICE, "semi-global traceback exceeded its CIGAR slot");
@@ -1436,10 +1484,15 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
     } else {
       d2h(C, G.data(), C.d_sg, (size_t)n);
       sync(C);
+      C.stats.ms_sg_kernel += kernel_ms(C.ev0, C.ev1);
     }
     k0 = k1;
   }
-  for (auto &g : G) C.stats.cells_semiglobal += sg_band_cells(g.rows, P.bandwidth, g.n2);
+  for (auto &g : G) {
+    const int64_t cells = sg_band_cells(g.rows, P.bandwidth, g.n2);
+    C.stats.cells_semiglobal += cells;
+    if (want_codes) C.stats.bytes_codes_sg += cells;
+  }
   C.stats.ms_semiglobal += ms_since(t0);
 }
 
@@ -1709,9 +1762,8 @@ void seeded_two_gap(Context &C, const std::vector<PairIn> &pairs, const std::vec
 
 }  // namespace
 
-void align_seeded(Context &C, const std::vector<PairIn> &pairs, const std::vector<std::vector<Seed4>> &seeds,
-                  const Params &P, std::vector<std::vector<FragOut>> &out) {
-  validate(P);
+namespace {
+void check_seeded_inputs(const std::vector<PairIn> &pairs, const std::vector<std::vector<Seed4>> &seeds) {
   for (const PairIn &p : pairs) {
     if ((p.n1 > 0 && !p.s1) || (p.n2 > 0 && !p.s2)) throw Error(DCNS_ERR_INVALID, "NULL sequence");
     if (p.n1 >= (1 << 24) - 2 || p.n2 >= (1 << 24) - 2) throw Error(DCNS_ERR_INVALID, "sequences must be < 16M bases");
@@ -1720,6 +1772,13 @@ void align_seeded(Context &C, const std::vector<PairIn> &pairs, const std::vecto
     for (const Seed4 &x : seeds[p])
       if (x.s1 < 0 || x.s2 < 0 || x.e1 < -1 || x.e2 < -1 || x.e1 >= pairs[p].n1 || x.e2 >= pairs[p].n2)
         throw Error(DCNS_ERR_INVALID, "seed outside its sequences");
+}
+}  // namespace
+
+void align_seeded(Context &C, const std::vector<PairIn> &pairs, const std::vector<std::vector<Seed4>> &seeds,
+                  const Params &P, std::vector<std::vector<FragOut>> &out) {
+  validate(P);
+  check_seeded_inputs(pairs, seeds);
   auto t0 = Clock::now();
   C.call_t0 = t0;
   C.stats = dcns_stats{};
@@ -1727,6 +1786,20 @@ void align_seeded(Context &C, const std::vector<PairIn> &pairs, const std::vecto
   if (pairs.empty()) return;
   upload(C, pairs);
   seeded_two_gap(C, pairs, seeds, P, out);
+  C.stats.ms_total = ms_since(t0);
+}
+
+void align_xseeds(Context &C, const std::vector<PairIn> &pairs, const std::vector<std::vector<Seed4>> &seeds,
+                  const Params &P, std::vector<std::vector<FragOut>> &out) {
+  validate(P);
+  check_seeded_inputs(pairs, seeds);
+  auto t0 = Clock::now();
+  C.call_t0 = t0;
+  C.stats = dcns_stats{};
+  out.assign(pairs.size(), {});
+  if (pairs.empty()) return;
+  upload(C, pairs);
+  two_gap_stage(C, pairs, P, seeds, out);
   C.stats.ms_total = ms_since(t0);
 }
 
@@ -1889,6 +1962,51 @@ void autotune(Context &C, Batch &B, const Params &P, int mode) {
     if (ms < best_ms) best_ms = ms, best = sh;
   }
   C.max_lanes = best.lanes, C.bins = best.bins, C.bin_ratio = best.ratio;
+
+  // Per bin: the x-drop pass forms (register-band levels row-interleaved or one pass per thread, the band where one
+  // warp per pass takes over, the widest band of the wavefront form), chosen by that bin's x-drop kernel time with
+  // each candidate applied to every bin; the bins differ in how many long and wide-band passes they hold.
+  C.bin_tune.clear();
+  if (C.max_lanes > 1 && (int64_t)B.lens.size() >= 4096) {
+    const Context::BinTune cands[] = {{20, 256, true}, {20, 256, false}, {10, 256, true}, {20, 128, true},
+                                      {20, 512, true}};
+    const int nb = std::max(C.bins, C.max_lanes);
+    std::vector<double> best_ms(nb, 1e300);
+    std::vector<Context::BinTune> choice(nb, cands[0]);
+    for (const Context::BinTune &cd : cands) {
+      C.bin_tune.assign(nb, cd);
+      run(best);
+      std::vector<double> ms = C.last_bin_xdrop_ms;
+      run(best);
+      for (int b = 0; b < nb && b < (int)ms.size() && b < (int)C.last_bin_xdrop_ms.size(); ++b) {
+        const double m = std::min(ms[b], C.last_bin_xdrop_ms[b]);
+        if (m < best_ms[b]) best_ms[b] = m, choice[b] = cd;
+      }
+    }
+    C.bin_tune = choice;
+  }
+  // the scan's tiling target (tiles per resident thread before reference rows are split into chunks; it matters
+  // for batches of few long pairs) and, on the 2-gap path, the 2-piece kernel's warps per DP: by whole-call time
+  {
+    int best_t = C.scan_tiles_per_thread;
+    double best_t_ms = 1e300;
+    for (int t : {4, 8, 16}) {
+      C.scan_tiles_per_thread = t;
+      const double ms = std::min(run(best), run(best));
+      if (ms < best_t_ms) best_t_ms = ms, best_t = t;
+    }
+    C.scan_tiles_per_thread = best_t;
+  }
+  if (mode == DCNS_MODE_TWO_GAP) {
+    int best_w = 0;
+    double best_w_ms = 1e300;
+    for (int nw : {0, 2, 4, kSgNW}) {
+      C.sg_warps = nw;
+      const double ms = std::min(run(best), run(best));
+      if (ms < best_w_ms) best_w_ms = ms, best_w = nw;
+    }
+    C.sg_warps = best_w;
+  }
 }
 
 void add_stats(dcns_stats &a, const dcns_stats &b) {
@@ -1902,6 +2020,9 @@ void add_stats(dcns_stats &a, const dcns_stats &b) {
   a.kernel_launches += b.kernel_launches, a.scan_rounds += b.scan_rounds, a.xdrop_rounds += b.xdrop_rounds;
   a.ms_xdrop_kernel += b.ms_xdrop_kernel;
   a.bytes_h2d += b.bytes_h2d;
+  a.ms_xdrop_tb_kernel += b.ms_xdrop_tb_kernel, a.ms_sg_kernel += b.ms_sg_kernel;
+  a.ms_sg_tb_kernel += b.ms_sg_tb_kernel;
+  a.bytes_codes_xdrop += b.bytes_codes_xdrop, a.bytes_codes_sg += b.bytes_codes_sg;
 }
 
 // Batches large enough to fill the GPU several times over are split into bins of similar work (pairs dealt
@@ -1961,6 +2082,7 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
   std::vector<std::string> errs(nl);
   std::vector<int> codes(nl, 0);
   std::vector<dcns_stats> st(nl, dcns_stats{});
+  std::vector<double> bin_xdrop_ms(kBins, 0.0);
   auto worker = [&](int l) {
     Context &L = *C.lanes[l];
     try {
@@ -1986,6 +2108,13 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
                                 cudaMemcpyHostToDevice, L.st));
         L.seqbase_dev = L.d_seqbase.as<int64_t>();
         L.stats = dcns_stats{};
+        // the bin's kernel shapes: the autotuner's per-bin choice, else the parent context's
+        const Context::BinTune bt = b < (int)C.bin_tune.size()
+                                        ? C.bin_tune[b]
+                                        : Context::BinTune{C.xdrop_warp_from, C.xdrop_wave_max_w, C.xdrop_flat};
+        L.xdrop_warp_from = bt.xdrop_warp_from, L.xdrop_wave_max_w = bt.xdrop_wave_max_w, L.xdrop_flat = bt.xdrop_flat;
+        L.sg_warps = C.sg_warps;
+        L.scan_tiles_per_thread = C.scan_tiles_per_thread;
         L.call_t0 = C.call_t0;
         L.lane_id = l;
         L.trace = C.trace;
@@ -1997,6 +2126,7 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
         align_single(L, sub, P, mode, so);
         pass.failed = false;
         for (size_t k = 0; k < ids.size(); ++k) out[ids[k]] = std::move(so[k]);
+        bin_xdrop_ms[b] = L.stats.ms_xdrop_kernel;
         add_stats(st[l], L.stats);
       }
     } catch (const Error &e) {
@@ -2015,6 +2145,7 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
   for (int l = 0; l < nl; ++l)
     if (codes[l]) throw Error(codes[l], errs[l]);
   for (int l = 0; l < nl; ++l) add_stats(C.stats, st[l]);
+  C.last_bin_xdrop_ms = std::move(bin_xdrop_ms);
 }
 
 void align_single(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,

@@ -100,7 +100,7 @@ struct Context {
   int nsm = 0, scan_blocks_per_sm = 1;
   std::string err;
   dcns_stats stats{};
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
 
   // device buffers
   DevBuf d_codes, d_srcoff, d_dstbase, d_len, d_pk, d_nm, d_seqbase, d_flag;
@@ -125,6 +125,20 @@ struct Context {
   int xdrop_warp_from = 20;  // x-drop bands wider than this run one warp per pass (DCNS_XDROP_WARP_FROM)
   // x-drop bands wider than xdrop_warp_from and up to this run as one-warp wavefronts (DCNS_XDROP_WAVE; 0 = off)
   int xdrop_wave_max_w = 256;
+  // register-band levels (w <= 20) as the row-interleaved kernel (DCNS_XDROP_FLAT=0: one pass per thread)
+  bool xdrop_flat = true;
+  // warps per DP of the unweighted semi-global kernel: 2, 4 or 8 (DCNS_SG_WARPS; 0 = by the number of DPs)
+  int sg_warps = 0;
+  // seed-scan tiling target: reference rows are split into chunks while a launch has fewer tiles than this many per
+  // resident thread (DCNS_SCAN_TILES)
+  int scan_tiles_per_thread = 8;
+  // per-bin x-drop pass forms chosen by the autotuner (empty: the values above for every bin)
+  struct BinTune {
+    int xdrop_warp_from, xdrop_wave_max_w;
+    bool xdrop_flat;
+  };
+  std::vector<BinTune> bin_tune;
+  std::vector<double> last_bin_xdrop_ms;  // x-drop kernel time of each bin of the last binned call
   // Level-0 turnstile of one binned call: the bins enqueue their level-0 scans on the parent's bulk stream in bin
   // order, so the scans run one after another and the first bins' host work overlaps the later bins' scans.
   struct Turnstile {
@@ -147,6 +161,8 @@ struct Context {
 };
 
 void init_context(Context &C, int device, size_t budget);
+// Frees the context's grow-only device buffers (after its stream is idle), so the next call sizes them afresh.
+void release_device_buffers(Context &C);
 
 Params to_params(const dcns_params *p);
 void validate(const Params &P);
@@ -170,6 +186,9 @@ void align_weighted(Context &C, const std::vector<PairIn> &pairs, const std::vec
                     std::vector<std::vector<FragOut>> &out);
 // The seeded 2-gap overload (cut2Gaps2) over many pairs; seeds[p] in the caller's order.
 void align_seeded(Context &C, const std::vector<PairIn> &pairs, const std::vector<std::vector<Seed4>> &seeds,
+                  const Params &P, std::vector<std::vector<FragOut>> &out);
+// The 2-piece stage over caller-given x-seeds (the x-seed overload without maximumAlignLength).
+void align_xseeds(Context &C, const std::vector<PairIn> &pairs, const std::vector<std::vector<Seed4>> &seeds,
                   const Params &P, std::vector<std::vector<FragOut>> &out);
 // Times the resident batch under candidate (lanes, bins, bin_ratio) shapes and keeps the fastest on C.
 void autotune(Context &C, Batch &B, const Params &P, int mode);

@@ -136,7 +136,7 @@ extern "C" int dcns_semiglobal_noalloc(const int8_t *d_seq1, int32_t len1, const
     std::lock_guard<std::mutex> lk(g_na_mu);
     if (!g_na_ptr[dev]) {
       // the kernel's boundary scratch for one CTA must fit the fixed array (checked once, with the kernel's own sizing)
-      if (sg_bnd_bytes(1, kNaMaxLen) > (int64_t)sizeof(NaScratch::bnd)) return DCNS_ERR_DEVICE;
+      if (sg_bnd_bytes(1, kNaMaxLen, kSgNW) > (int64_t)sizeof(NaScratch::bnd)) return DCNS_ERR_DEVICE;
       void *p = nullptr;
       if (cudaGetSymbolAddress(&p, g_na_scratch) != cudaSuccess || !p) {
         (void)cudaGetLastError();  // the failed lookup's own error
@@ -149,7 +149,7 @@ extern "C" int dcns_semiglobal_noalloc(const int8_t *d_seq1, int32_t len1, const
   cudaStream_t st = (cudaStream_t)stream;
   na_prepare_kernel<<<1, 256, 0, st>>>(S, d_seq1, len1, d_seq2, len2);
   Arena ar{S->pk, S->nm};
-  launch_semiglobal(&S->task, &S->idx, 1, ar, P, nullptr, S->bnd, kNaMaxLen, &S->counter, 1, st);
+  launch_semiglobal(&S->task, &S->idx, 1, ar, P, nullptr, S->bnd, kNaMaxLen, &S->counter, 1, kSgNW, st);
   na_finish_kernel<<<1, 32, 0, st>>>(S, d_out);
   return cudaGetLastError() == cudaSuccess ? DCNS_OK : DCNS_ERR_DEVICE;
 }

@@ -41,42 +41,44 @@ int64_t sg_tb_bytes(int n1, int n2, int w) {
   return (int64_t)((n1 + kSgRows - 1) / kSgRows) * sg_stride_steps(n2, w) * 32 * kSgR;
 }
 
-// Super-step length K (wavefront steps between CTA barriers) for a DP whose stripes take at most smax steps:
-//  * a warp finishes stripe s before stripe s+8 starts:   kSgD * kSgNW * K >= smax
+// Super-step length K (wavefront steps between CTA barriers) for a DP whose stripes take at most smax steps, on a CTA
+// of nw warps:
+//  * a warp finishes stripe s before stripe s+nw starts:   kSgD * nw * K >= smax
 //  * every boundary cell is written at least one barrier before the consumer stages it 32-63 steps ahead of use.
 //    Stripe s writes column j at its step j - jstart_s + 31; stripe s+1, which starts kSgD super-steps later, stages
 //    it at step j - jstart_{s+1} - 63 or later, and jstart_{s+1} - jstart_s <= kSgRows; so the producer is at most
 //    kSgRows + 94 steps ahead of that read, which must be at most (kSgD - 1) * K:  K >= kSgRows + 96
-__host__ __device__ inline int sg_superstep(int n2, int w) {
+__host__ __device__ inline int sg_superstep(int n2, int w, int nw) {
   const int64_t span = 2 * (int64_t)w + kSgRows;
   const int smax = (int)(n2 < span ? (int64_t)n2 : span) + 31;
-  const int k = (smax + kSgD * kSgNW - 1) / (kSgD * kSgNW);
+  const int k = (smax + kSgD * nw - 1) / (kSgD * nw);
   static_assert(kSgD == 2, "the lower bound below assumes two super-steps between stripe starts");
   return k > kSgRows + 96 ? k : kSgRows + 96;
 }
 
-// One CTA per DP, on a fixed schedule: stripe s runs steps [(g - 2s) K, (g - 2s + 1) K) in super-step g, and all
-// warps meet at a barrier after every super-step, so every cross-warp dependency (the row above a stripe, the row
+// One CTA of NW warps per DP (stripe s on warp s mod NW), on a fixed schedule: stripe s runs steps
+// [(g - 2s) K, (g - 2s + 1) K) in super-step g, and all warps meet at a barrier after every super-step, so every cross-warp dependency (the row above a stripe, the row
 // evaluation order, the stop decision) crosses at least one __syncthreads.  There are no flag waits.
 //   bnd   global scratch of this CTA: per stripe slot (s mod 8), the stripe's last row (M, F1, F2) by column
-__global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tasks, const int *__restrict__ idx,
-                                                         int n, Arena ar, Params P, uint8_t *__restrict__ tb,
-                                                         SgRec *__restrict__ bnd_all, int64_t bnd_stride,
-                                                         int *__restrict__ counter) {
-  __shared__ SgRec stage[kSgNW][2][32];  // per warp: boundary cells of the next two 32-column chunks
-  __shared__ int stage_c[kSgNW][2][32];  // and the query codes of those columns
-  __shared__ int row_best[kSgNW][kSgRows], row_bestj[kSgNW][kSgRows];
-  __shared__ int done_stripe[kSgNW];
+template <int NW>
+__global__ void __launch_bounds__(32 * NW) sg_kernel(SgTask *__restrict__ tasks, const int *__restrict__ idx, int n,
+                                                      Arena ar, Params P, uint8_t *__restrict__ tb,
+                                                      SgRec *__restrict__ bnd_all, int64_t bnd_stride,
+                                                      int *__restrict__ counter) {
+  __shared__ SgRec stage[NW][2][32];  // per warp: boundary cells of the next two 32-column chunks
+  __shared__ int stage_c[NW][2][32];  // and the query codes of those columns
+  __shared__ int row_best[NW][kSgRows], row_bestj[NW][kSgRows];
+  __shared__ int done_stripe[NW];
   __shared__ int s_max, s_end1, s_end2, s_rows, s_next_eval, s_stop, s_stale_last, s_stale_prev, s_task;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int o1 = P.open1, x1 = P.ext1, o2 = P.open2, x2 = P.ext2, w = P.bandwidth;
-  SgRec *bnd = bnd_all + (int64_t)blockIdx.x * kSgNW * bnd_stride;
+  SgRec *bnd = bnd_all + (int64_t)blockIdx.x * NW * bnd_stride;
   for (;;) {
     if (threadIdx.x == 0) s_task = atomicAdd(counter, 1);
     __syncthreads();
     const int q = s_task;
     if (q >= n) break;
-    if (threadIdx.x < kSgNW) done_stripe[threadIdx.x] = -1;
+    if (threadIdx.x < NW) done_stripe[threadIdx.x] = -1;
     if (threadIdx.x == 0) {
       // ends are 1-based rows/columns and stay -1 while no cell is positive: the reference then reports -2 (0-based)
       s_max = 0, s_end1 = -1, s_end2 = -1, s_rows = 0, s_next_eval = 0, s_stop = 0;
@@ -91,7 +93,7 @@ __global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tas
     const int n1_eff = (n1 <= 0 || n2 <= 0) ? 0 : min(n1, n2 + w);  // rows with a non-empty band
     const int nstripes = (n1_eff + kSgRows - 1) / kSgRows;
     const int64_t stride = sg_stride_steps(n2, w);
-    const int K = sg_superstep(n2, w);
+    const int K = sg_superstep(n2, w, NW);
     // per-warp stripe state (registers persist across super-steps)
     int cs = warp;  // this warp's current stripe
     int i0 = 0, jstart = 0, nsteps = 0, upB = 0, tdone = 0;
@@ -127,8 +129,8 @@ __global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tas
       upB = min(kSgRows * s + w, n2);  // the row above (128s) holds columns [max(128s - w, 1), upB]
       produce = s + 1 < nstripes;
       trow = reinterpret_cast<uint32_t *>(tb + T.tb_off) + (int64_t)s * stride * 32;
-      bup = bnd + (int64_t)((s + kSgNW - 1) % kSgNW) * bnd_stride;
-      bdown = bnd + (int64_t)(s % kSgNW) * bnd_stride;
+      bup = bnd + (int64_t)((s + NW - 1) % NW) * bnd_stride;
+      bdown = bnd + (int64_t)(s % NW) * bnd_stride;
       diag = (lane == 0 && s > 0 && jstart > 1) ? bup[jstart - 1].m : kOut;
       outM = kOut, outF1 = kOut, outF2 = kOut, outC = 0;
       tdone = 0;
@@ -216,12 +218,12 @@ __global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tas
         if (tdone == nsteps) {  // stripe complete: publish its rows for the in-order evaluation
 #pragma unroll
           for (int k = 0; k < kSgR; ++k) {
-            row_best[cs % kSgNW][kSgR * lane + k] = best[k];
-            row_bestj[cs % kSgNW][kSgR * lane + k] = bestj[k];
+            row_best[cs % NW][kSgR * lane + k] = best[k];
+            row_bestj[cs % NW][kSgR * lane + k] = bestj[k];
           }
           __syncwarp();
-          if (lane == 0) done_stripe[cs % kSgNW] = cs;
-          cs += kSgNW;
+          if (lane == 0) done_stripe[cs % NW] = cs;
+          cs += NW;
           started = false;
         }
       }
@@ -230,11 +232,11 @@ __global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tas
       if (threadIdx.x == 0 && !s_stop) {
         int mx = s_max, e1r = s_end1, e2r = s_end2, rows = s_rows, ne = s_next_eval;
         bool stop = false;
-        while (!stop && ne < nstripes && done_stripe[ne % kSgNW] == ne) {
+        while (!stop && ne < nstripes && done_stripe[ne % NW] == ne) {
           for (int r = 0; r < kSgRows && !stop; ++r) {
             const int ii = kSgRows * ne + 1 + r;
             if (ii > n1_eff) break;
-            const int tm = row_best[ne % kSgNW][r], tj = row_bestj[ne % kSgNW][r];
+            const int tm = row_best[ne % NW][r], tj = row_bestj[ne % NW][r];
             if (tm > mx) mx = tm, e1r = ii, e2r = tj;
             int l = (ii - e1r) - (tj - e2r);
             l = l > 0 ? l : -l;
@@ -284,21 +286,33 @@ __global__ void __launch_bounds__(32 * kSgNW) sg_kernel(SgTask *__restrict__ tas
   }
 }
 
-int sg_ctas_per_sm() {
+// Resident CTAs per SM of the NW-warp kernel.
+int sg_ctas_per_sm(int nw) {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sg_kernel, 32 * kSgNW, 0) != cudaSuccess) {
+  cudaError_t e = nw == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sg_kernel<2>, 64, 0)
+                  : nw == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sg_kernel<4>, 128, 0)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sg_kernel<kSgNW>, 32 * kSgNW, 0);
+  if (e != cudaSuccess) {
     (void)cudaGetLastError();
     nb = 1;
   }
   return nb > 0 ? nb : 1;
 }
 
-int64_t sg_bnd_bytes(int grid, int max_n2) { return (int64_t)grid * kSgNW * ((int64_t)max_n2 + 2) * sizeof(SgRec); }
+int64_t sg_bnd_bytes(int grid, int max_n2, int nw) {
+  return (int64_t)grid * nw * ((int64_t)max_n2 + 2) * sizeof(SgRec);
+}
 
 void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p, uint8_t *tb, void *bnd,
-                       int max_n2, int *work_counter, int grid, cudaStream_t st) {
+                       int max_n2, int *work_counter, int grid, int nw, cudaStream_t st) {
   if (n <= 0) return;
-  sg_kernel<<<grid, 32 * kSgNW, 0, st>>>(tasks, idx, n, ar, p, tb, (SgRec *)bnd, (int64_t)max_n2 + 2, work_counter);
+  const int64_t stride = (int64_t)max_n2 + 2;
+  if (nw == 2)
+    sg_kernel<2><<<grid, 64, 0, st>>>(tasks, idx, n, ar, p, tb, (SgRec *)bnd, stride, work_counter);
+  else if (nw == 4)
+    sg_kernel<4><<<grid, 128, 0, st>>>(tasks, idx, n, ar, p, tb, (SgRec *)bnd, stride, work_counter);
+  else
+    sg_kernel<kSgNW><<<grid, 32 * kSgNW, 0, st>>>(tasks, idx, n, ar, p, tb, (SgRec *)bnd, stride, work_counter);
 }
 
 // ------------------------------------------------------------------ traceback (:869-914)

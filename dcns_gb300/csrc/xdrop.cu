@@ -153,6 +153,82 @@ __device__ __forceinline__ int xd_row(XPassScalars &x, int32_t (&M)[XBand<WC>::N
   return -1;
 }
 
+// Row x.i as one left-to-right loop: the same cells, comparisons and tie rules as xd_row, with A (the diagonal /
+// vertical choice) and the incoming horizontal gap e of each cell kept in registers for that cell only, so the band
+// arrays are the only per-cell state (a third of xd_row's registers: more warps per SM).  Returns as xd_row.
+template <int WC>
+__device__ __forceinline__ int xd_row_fused(XPassScalars &x, int32_t (&M)[XBand<WC>::NA], int32_t (&F)[XBand<WC>::NA],
+                                            uint64_t (&qw)[XBand<WC>::NQ], const Arena &ar, const Params &P,
+                                            uint32_t *__restrict__ tb) {
+  constexpr int NK = XBand<WC>::NK, NQ = XBand<WC>::NQ;
+  const int i = x.i, w = x.w, nk = x.nk, n2 = x.n2;
+  if (i > x.n1) return 0;
+  const int c0 = max(i - w, 1), c1 = min(i + w, n2);
+  if (x.codes && (int64_t)i * x.wpr > x.tb_cap) return 2;
+  const int open = P.open1, ext = P.ext1, g = ext > open ? ext : open;
+  const int ci = x.s1.at(ar, i - 1);
+  int best = 0, bestj = -1;
+  int32_t ec = kOut;  // e entering the cell: the reference starts each row with e = OUT
+  uint32_t cw = 0;
+  int kw = 0;
+  uint32_t *row_codes = tb + x.tb_off + (int64_t)(i - 1) * x.wpr;
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int j = i - w + k;
+    uint32_t nib = 0xFu;
+    if (k < nk && j >= c0 && j <= c1) {
+      // M[k] and F[k + 1] still hold the row above: F[k + 1] is rewritten at the next cell
+      const int cj = (int)((qw[k >> 4] >> (4 * (k & 15))) & 15u);
+      const int32_t diag = (j == 1) ? (i == 1 ? 0 : kOut) : M[k];
+      const int32_t fin = (j == c1) ? kOut : F[k + 1];
+      const int32_t sd = score_of(ci, cj, P.match, P.mismatch) + diag;
+      const int32_t A = sd > fin ? sd : fin;
+      const bool ge = !(A > ec);  // the horizontal gap wins ties
+      const int32_t v = ge ? ec : A;
+      uint32_t d = ge ? 2u : (sd > fin ? 0u : 1u);
+      M[k] = v;
+      if (v > best) {
+        best = v;
+        bestj = j;
+      }
+      const int32_t h = v + open;
+      const int32_t f = fin + ext;
+      if (f >= h) d |= 4u;
+      F[k] = f >= h ? f : h;
+      if (ec + ext >= h) d |= 8u;
+      ec = max(ec + g, A + open);  // = max(e + ext, max(A, e) + open), the reference's e update
+      nib = d;
+    }
+    if (x.codes && k < nk) {
+      cw |= nib << (4 * (k & 7));
+      if ((k & 7) == 7 || k == nk - 1) {
+        row_codes[kw++] = cw;
+        cw = 0;
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < NQ; ++u) qw[u] = (qw[u] >> 4) | (u + 1 < NQ ? qw[u + 1] << 60 : 0ull);
+  const int jn = i + 1 + w;
+  if (jn <= n2) {
+    const int kl = nk - 1;
+#pragma unroll
+    for (int u = 0; u < NQ; ++u)
+      if (u == (kl >> 4)) qw[u] |= (uint64_t)x.s2.at(ar, jn - 1) << (4 * (kl & 15));
+  }
+  x.rows = i;
+  if (bestj != n2 && bestj != 1 && (bestj == c0 || bestj == c1)) return 1;
+  if (best > x.score) {
+    x.score = best;
+    x.e1 = i;
+    x.e2 = bestj;
+  }
+  if (x.score - best > P.xdrop) return 0;
+  if (best <= 0) return 0;
+  x.i = i + 1;
+  return -1;
+}
+
 __device__ __forceinline__ void xd_finish(const XPassScalars &x, XTask &T, int status) {
   T.status = status;
   T.rows = x.rows;
@@ -438,6 +514,7 @@ struct XLevelArgs {
   int *retry, *retry_count;
   unsigned long long *tb_cursor;
   int64_t tb_words;
+  int *fetch;  // passes of the level handed out so far (the row-interleaved kernel)
 };
 
 __device__ __forceinline__ bool xd_take_slot(XTask &T, const XLevelArgs &L) {
@@ -472,6 +549,47 @@ __global__ void __launch_bounds__(128) xdrop_level_kernel(XLevelArgs L, Arena ar
     }
     xdrop_pass<WC>(T, ar, P, tb, nullptr, nullptr);
     xd_route(T, id, L);
+  }
+}
+
+// The register-band level as a row-interleaved loop: every lane of a warp advances its own pass one row per
+// iteration and, when that pass ends, takes the level's next pass (warp-aggregated atomic on L.fetch), so the warp
+// keeps issuing full rows until the level's list runs out instead of idling until its longest pass ends.
+template <int WC>
+__global__ void __launch_bounds__(128) xdrop_level_flat_kernel(XLevelArgs L, Arena ar, Params P,
+                                                               uint32_t *__restrict__ tb) {
+  const int n = *L.count_in;
+  const int lane = threadIdx.x & 31;
+  XPassScalars x;
+  int32_t Mr[XBand<WC>::NA], Fr[XBand<WC>::NA];
+  uint64_t qw[XBand<WC>::NQ];
+  int id = -1;
+  for (;;) {
+    if (id < 0) {
+      const unsigned m = __activemask();
+      const int leader = __ffs(m) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(L.fetch, __popc(m));
+      base = __shfl_sync(m, base, leader);
+      const int q = base + __popc(m & ((1u << lane) - 1u));
+      if (q >= n) break;
+      id = L.list_in[q];
+      XTask &T = L.tasks[id];
+      if (T.want_codes && !xd_take_slot(T, L)) {
+        T.status = 2;
+        L.retry[atomicAdd(L.retry_count, 1)] = id;
+        id = -1;
+        continue;
+      }
+      xd_begin<WC>(x, Mr, Fr, qw, T, ar);
+    }
+    const int st = xd_row_fused<WC>(x, Mr, Fr, qw, ar, P, tb);
+    if (st >= 0) {
+      XTask &T = L.tasks[id];
+      xd_finish(x, T, st);
+      xd_route(T, id, L);
+      id = -1;
+    }
   }
 }
 
@@ -688,13 +806,36 @@ void launch_xdrop_iota(int *list, int n, int *count, cudaStream_t st) {
   xdrop_iota_kernel<<<(n + 255) / 256, 256, 0, st>>>(list, n, count);
 }
 
+template <int WC>
+int flat_blocks_per_sm() {
+  static int nb = 0;
+  if (nb == 0) {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, xdrop_level_flat_kernel<WC>, 128, 0) != cudaSuccess) {
+      (void)cudaGetLastError();
+      v = 1;
+    }
+    nb = v > 0 ? v : 1;
+  }
+  return nb;
+}
+
 void launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
-                        int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, Arena ar,
-                        Params p, uint32_t *tb, int w, int n_bound, int nsm, int32_t *scratch, int64_t per_warp,
-                        int warps, int warp_from, int wave_max_w, cudaStream_t st) {
+                        int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int *fetch,
+                        Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm, int32_t *scratch,
+                        int64_t per_warp, int warps, int warp_from, int wave_max_w, bool flat, cudaStream_t st) {
   if (n_bound <= 0) return;
-  const XLevelArgs L{tasks, list_in, count_in, list_out, count_out, retry, retry_count, tb_cursor, tb_words};
+  const XLevelArgs L{tasks, list_in, count_in, list_out, count_out, retry, retry_count, tb_cursor, tb_words, fetch};
   const int g = (int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * 16);
+  if (flat && w <= warp_from && w <= 20) {  // register band, row-interleaved: one resident wave of blocks
+    if (w <= 10)
+      xdrop_level_flat_kernel<10><<<(int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * flat_blocks_per_sm<10>()),
+                                    128, 0, st>>>(L, ar, p, tb);
+    else
+      xdrop_level_flat_kernel<20><<<(int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * flat_blocks_per_sm<20>()),
+                                    128, 0, st>>>(L, ar, p, tb);
+    return;
+  }
   if (w > warp_from && w <= wave_max_w && w <= kXwMaxW)  // wide bands up to 256: the wavefront
     xdrop_level_wave_kernel<<<(int)std::min<int64_t>((n_bound + 3) / 4, (int64_t)nsm * 16), 128, 0, st>>>(L, ar, p,
                                                                                                          tb);

@@ -16,6 +16,11 @@
  *   dcns_xextend_batch                         SemiGlobal_xextend (both overloads)  impl/sequenceAlignment.h:72-81
  *   dcns_semiglobal_batch                      SemiGlobal (2-piece affine)          impl/sequenceAlignment.h:52-56
  *   dcns_sliding_window                        slidingWindowAlignment    impl/slidingWindowAlignment.h:21-24
+ *   dcns_align_weighted                        findSimilarFragmentsForPairedSequence_wighted / _wighted_1gap
+ *                                              impl/findSimilarFragmentsForPairedSequence.h:45-61
+ *   dcns_align_xseeds                          the x-seed overload, impl/findSimilarFragmentsForPairedSequence.h:70-77
+ *   dcns_align_seeded                          the x-seed overload with maximumAlignLength (cut2Gaps2)
+ *                                              impl/findSimilarFragmentsForPairedSequence.h:79-86
  *
  * Sequences cross the boundary as dCNS integer codes (int8: A=0 C=1 N=2 G=3 T=4, the output of
  * SequenceCharToUInt8::seq_to_int8, with lower-case 'n' already removed as the reference's drivers do); reverse
@@ -83,6 +88,11 @@ typedef struct {
   int32_t xdrop_rounds;    /* x-drop launch rounds (band restarts), summed over lanes */
   double ms_xdrop_kernel;  /* device: x-drop pass kernels, CUDA events */
   int64_t bytes_h2d;       /* host-to-device bytes of the sequence upload (codes and per-sequence offsets) */
+  double ms_xdrop_tb_kernel;  /* device: x-drop traceback and CIGAR packing kernels, CUDA events */
+  double ms_sg_kernel;        /* device: semi-global DP kernels, CUDA events */
+  double ms_sg_tb_kernel;     /* device: semi-global traceback kernels, CUDA events */
+  int64_t bytes_codes_xdrop;  /* direction codes of the final-width x-drop passes that kept them: 4 bits per band cell */
+  int64_t bytes_codes_sg;     /* direction codes of the semi-global DPs that kept them: 1 byte per band cell */
 } dcns_stats;
 
 /* Results of one dcns_align_pairs call; owned by the library until dcns_results_free. */
@@ -128,6 +138,13 @@ int dcns_align_weighted(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, 
 int dcns_align_seeded(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, const int32_t *seeds,
                       const int64_t *seed_offset, const dcns_params *params, dcns_results **out);
 
+/* The x-seed overload without maximumAlignLength (impl/findSimilarFragmentsForPairedSequence.h:70-77,
+ * impl/findSimilarFragmentsForPairedSequence4.cpp:532-616; the 2-gap overload runs it on its own x-seeds) for many
+ * pairs: per x-seed a reverse 2-piece DP from its end, the StartAlignment gate, a forward 2-piece DP with CIGAR and
+ * the dedupe by end; no p-value filter, no length cap.  Seeds and offsets as for dcns_align_seeded. */
+int dcns_align_xseeds(dcns_ctx *ctx, const dcns_pair *pairs, int64_t n_pairs, const int32_t *seeds,
+                      const int64_t *seed_offset, const dcns_params *params, dcns_results **out);
+
 /* x-seeds of cut2Gaps2 from SAM text (samFileToSeeds, impl/samFileToSeeds.cpp:19-141): the reference and query
  * genomes are given by name with their texts (still holding lower-case 'n' runs).  *seeds receives a malloc'ed array
  * (free with dcns_free_seeds) of *n_seeds records of 7 int32 in line order: reference index, query index (-1 when the
@@ -157,11 +174,25 @@ int dcns_measure_scan_roofline(dcns_ctx *ctx, double *gcups);
 int dcns_ctx_set_lanes(dcns_ctx *ctx, int lanes, int bins);
 
 /* Autotuner (no counterpart in the reference): aligns the resident batch once per candidate pipeline shape (lanes,
- * bins, and the geometric ratio of bin sizes), times each call, and keeps the fastest on the context.  The chosen
- * values are returned (any pointer may be NULL).  Results do not depend on the shape; this only tunes throughput for
- * batches like this one. */
+ * bins, and the geometric ratio of bin sizes), times each call, and keeps the fastest on the context; then, per bin,
+ * the x-drop pass forms by that bin's x-drop kernel time, and by whole-call time the seed scan's tiling target and
+ * (2-gap mode) the 2-piece kernel's warps per DP (dcns_get_tuning reports them).  The pipeline shape is returned (any
+ * pointer may be NULL).  Results do not depend on any of these; this only tunes throughput for batches like this. */
 int dcns_autotune(dcns_ctx *ctx, dcns_batch *batch, const dcns_params *params, int mode, int *lanes, int *bins,
                   double *bin_ratio);
+
+/* The context's kernel shapes (no counterpart in the reference): what dcns_autotune chose, or the defaults and the
+ * DCNS_* environment settings.  Per bin (at most 16 reported): the x-drop band from which passes run one warp each,
+ * the widest band of the one-warp wavefront form, and whether the register-band levels run row-interleaved. */
+typedef struct {
+  int32_t lanes, bins;
+  double bin_ratio;
+  int32_t scan_tiles_per_thread;  /* seed-scan tiling target: rows split into chunks below this many tiles per thread */
+  int32_t sg_warps;               /* warps per 2-piece DP (0: two for launches of many DPs, else eight) */
+  int32_t n_bins_tuned;           /* bins with their own x-drop forms below (0: every bin uses bin 0's values) */
+  int32_t xdrop_warp_from[16], xdrop_wave_max_w[16], xdrop_flat[16];
+} dcns_tuning;
+int dcns_get_tuning(const dcns_ctx *ctx, dcns_tuning *out);
 
 /* Stats of the context's last dcns_align_pairs call. */
 int dcns_last_stats(const dcns_ctx *ctx, dcns_stats *out);
@@ -193,22 +224,52 @@ int dcns_sliding_window(dcns_ctx *ctx, const int8_t *const *seqs, const int32_t 
  * processes whose device memory belongs to another allocator or budget, and latency-bound threads that cannot afford
  * the device-wide synchronisation of cudaMalloc/cudaFree.  The caller passes device buffers: the two code sequences
  * (at most 16384 bases each; longer inputs return DCNS_ERR_INVALID) and d_out (4 int32: maxScore, endPosition1,
- * endPosition2 (0-based), status 0 ok / 1 a code outside 0..4).  Work is queued on `stream` (a cudaStream_t; NULL =
- * the legacy default stream); read d_out after synchronising it.  All scratch is one fixed device array of about
- * 1.6 MB per GPU that holds the library, shared by every call: calls that overlap on the GPU race, calls ordered on
- * one stream do not.  The first call on each device resolves the array's address (cudaGetSymbolAddress, with that
- * device current); make it before any stream capture. */
+ * endPosition2 (0-based), status 0 ok / 1 a code outside 0..4).  Parameters are checked as dcns_semiglobal_batch
+ * checks them (DCNS_ERR_INVALID for the same values).  Work is queued on `stream` (a cudaStream_t; NULL = the legacy
+ * default stream); read d_out after synchronising it.  All scratch is one fixed device array of about 1.6 MB per GPU
+ * that holds the library, shared by every call: calls that overlap on the GPU race, calls ordered on one stream do
+ * not.  The first call on each device resolves the array's address (cudaGetSymbolAddress, with that device current);
+ * make it before any stream capture.  A CUDA error still pending in the calling thread from earlier work makes the
+ * call return DCNS_ERR_DEVICE without queueing anything, and leaves that error in place for its owner. */
 int dcns_semiglobal_noalloc(const int8_t *d_seq1, int32_t len1, const int8_t *d_seq2, int32_t len2,
                             const dcns_params *params, int32_t *d_out, void *stream);
 
-/* Serving loop: continuous batching.  dcns_submit copies the pair and returns a ticket at once; requests are
- * admitted to the device as memory allows and overlap with work already running.  dcns_poll returns DCNS_OK with
- * the result when done, DCNS_ERR_BUSY while pending.  dcns_serve_wait blocks up to timeout_ms. */
+/* Serving loop (no counterpart in the reference, whose drivers align one pair per call): continuous batching.
+ * dcns_submit checks and copies the pair and returns a ticket at once (DCNS_ERR_INVALID for codes outside 0..4).
+ * Workers, each with its own stream and device buffers, admit queued requests in arrival order into a batch while
+ * the batch's predicted device memory (sequence arena, scan records, x-drop traceback and CIGAR slots, 2-piece
+ * direction codes) fits the worker's share of the context budget and its predicted seed-scan cells stay under the
+ * batch cap (at most max_inflight_pairs requests); a worker admits new requests as soon as it finishes its batch,
+ * while the other workers' batches run.  A batch the device budget rejects is halved; a batch that fails otherwise is
+ * retried one request at a time, so a failing request fails only itself (its status is returned by poll / wait).
+ * dcns_poll returns DCNS_OK with the result when done, DCNS_ERR_BUSY while pending, DCNS_ERR_NOTFOUND for unknown,
+ * collected or cancelled tickets.  dcns_serve_wait blocks up to timeout_ms (DCNS_ERR_TIMEOUT).  dcns_cancel removes a
+ * queued request, or drops the result of one being aligned.  dcns_serve_stop aligns what is queued, ends the workers
+ * and wakes every waiter; it may overlap submit / poll / wait / cancel calls on other threads (those return
+ * DCNS_ERR_INVALID, or what is known of their ticket, once it has run).  Serving calls are thread-safe with one
+ * another; dcns_ctx_destroy must not overlap any call on the context. */
 int dcns_serve_start(dcns_ctx *ctx, const dcns_params *params, int mode, int max_inflight_pairs);
 int dcns_submit(dcns_ctx *ctx, const dcns_pair *pair, uint64_t *ticket);
 int dcns_poll(dcns_ctx *ctx, uint64_t ticket, dcns_results **out);
 int dcns_serve_wait(dcns_ctx *ctx, uint64_t ticket, int64_t timeout_ms, dcns_results **out);
+int dcns_cancel(dcns_ctx *ctx, uint64_t ticket);
 int dcns_serve_stop(dcns_ctx *ctx);
+/* Shape of the next dcns_serve_start: workers (1..8, default 3; DCNS_SERVE_WORKERS overrides), the batch cap in
+ * predicted level-0 seed-scan cells (0 = the default, 1e11, about 25 ms of scan) and in predicted device bytes
+ * (0 = the worker's share of the context budget; larger values let the device budget's own check split batches).
+ * Results do not depend on any of them. */
+int dcns_serve_set_shape(dcns_ctx *ctx, int workers, int64_t batch_cells, int64_t admit_bytes);
+
+/* Counters of the serving loop since dcns_serve_start. */
+typedef struct {
+  int64_t submitted, completed, failed, cancelled;
+  int64_t batches, max_batch;
+  int64_t nomem_splits;     /* batches the device budget rejected, halved */
+  int64_t solo_retries;     /* requests retried alone after their batch failed for another reason */
+  int64_t queued, pending;  /* now: waiting for admission; queued or being aligned */
+  int32_t workers, pad;
+} dcns_serving_stats;
+int dcns_serve_stats(dcns_ctx *ctx, dcns_serving_stats *out);
 
 /* SAM and "o" text of one reference/query pair, as cut1Gap writes them (outputMasking,
  * controlLayer4.cpp:835-1358; cut1Gap's per-query "#done" trailer, :1430-1432, is left to the caller).  Host only.

@@ -7,7 +7,13 @@
 #                      shipped x86 binary runs; on a non-x86 host the scalar SmithWaterman_non_avx is selected by the
 #                      reference's own #ifdef, which needs an x86 <immintrin.h>, so the build is skipped there.
 set -euo pipefail
+#
+#   build_ref.sh --where   prints the checkout's location (nothing where there is none) and builds nothing
 REF="${DCNS_REFERENCE:-/root/reference}"
+if [ "${1:-}" = "--where" ]; then
+  if [ -d "$REF/impl" ]; then echo "$REF"; fi
+  exit 0
+fi
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/impl" ]; then echo "build_ref: reference checkout not found at $REF; skipped"; exit 0; fi
@@ -25,6 +31,14 @@ g++ -O2 -mavx2 -std=gnu++14 -include cstdint -fPIC -w -I"$REF" -c "$HERE/ref_har
 wait
 g++ -shared -o "$OUT/libdcns_ref.so" $OBJS "$OUT/ref_harness.o"
 echo "build_ref: $OUT/libdcns_ref.so"
+
+# The same reference objects with the dense traceback matrix (model/Matrix.cpp) replaced by oracle/lazy_matrix.cpp,
+# which keeps its get/set/reset semantics but stores only the touched cells: pairs of 50-200 kb, whose dense
+# (L1+1)(L2+1)-byte matrix does not fit in memory, then run through the unmodified alignment code.
+g++ -O2 -std=gnu++14 -include cstdint -fPIC -w -I"$REF" -c "$HERE/lazy_matrix.cpp" -o "$OUT/lazy_matrix.o"
+LOBJS="$(echo $OBJS | tr ' ' '\n' | grep -v model_Matrix.cpp.o | tr '\n' ' ')"
+g++ -shared -o "$OUT/libdcns_ref_lazy.so" $LOBJS "$OUT/lazy_matrix.o" "$OUT/ref_harness.o"
+echo "build_ref: $OUT/libdcns_ref_lazy.so"
 
 # The reference's record writer (outputMasking, controlLayer4.cpp) links against most of the command-line program:
 # every non-test source of its CMakeLists target except main.cpp, compiled directly.

@@ -948,6 +948,45 @@ int or_xextend(const int8_t *s1, int32_t n1, const int8_t *s2, int32_t n2, int o
   return 0;
 }
 
+// x_extend_seed's two DP passes (impl/findSimilarFragmentsForPairedSequence4.cpp:245-285 calls SemiGlobal_xextend
+// forward without, then again with the traceback) over n independent tasks on `threads` threads, tasks taken in
+// order from a shared counter.  out[k] = score of the traceback pass; cells_o[0] = the algorithmic band cells of both
+// passes; the checksum folds every task's integer outputs and CIGAR words.
+int or_xextend_batch(int n, const int8_t *const *s1, const int32_t *n1, const int8_t *const *s2, const int32_t *n2,
+                     int open, int ext, int match, int mismatch, int xdrop, int w, int threads, int32_t *out,
+                     uint64_t *checksum_out, int64_t *cells_o) {
+  Score sc{match, mismatch};
+  std::atomic<int> next(0);
+  const int nt = std::max(threads, 1);
+  std::vector<int64_t> cells(nt, 0);
+  std::vector<uint64_t> sums(nt, 0);
+  auto work = [&](int t) {
+    for (int k; (k = next.fetch_add(1)) < n;) {
+      uint64_t h = 1469598103934665603ull;
+      for (int pass = 0; pass < 2; ++pass) {
+        XOut o;
+        xextend(s1[k], n1[k], s2[k], n2[k], open, ext, sc, xdrop, w, pass == 1, o);
+        cells[t] += o.cells;
+        for (int64_t v : {(int64_t)o.score, (int64_t)o.end1, (int64_t)o.end2, (int64_t)o.iii, (int64_t)o.jjj})
+          h = (h ^ (uint64_t)v) * 1099511628211ull;
+        for (uint32_t c : o.cigar) h = (h ^ c) * 1099511628211ull;
+        if (pass == 1) out[k] = o.score;
+      }
+      sums[t] += h;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto &th : pool) th.join();
+  int64_t tot = 0;
+  uint64_t sum = 0;
+  for (int t = 0; t < nt; ++t) tot += cells[t], sum += sums[t];
+  cells_o[0] = tot;
+  *checksum_out = sum;
+  return 0;
+}
+
 int or_semiglobal(const int8_t *s1, int32_t n1, const int8_t *s2, int32_t n2, const int32_t *ip, const double *dp,
                   int want_cigar, uint32_t *cigar, int cigar_cap, int32_t *out) {
   Params P = params_from(ip, dp);
@@ -1012,6 +1051,21 @@ int or_find_seeded_2gap(const int8_t *s1, int32_t n1, const int8_t *s2, int32_t 
   for (int32_t k = 0; k < n_seeds; ++k) sd[k] = Seed4{seeds[4 * k], seeds[4 * k + 1], seeds[4 * k + 2], seeds[4 * k + 3]};
   Cells cells;
   std::vector<Frag> fr = seeded_two_piece(pr, P, max_align, sd, cells);
+  cells_out(cells, cells_o);
+  return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
+}
+
+// The x-seed overload without maximumAlignLength (two_piece_stage) on caller-given x-seeds, 0-based, in order.
+int or_find_xseeds_2gap(const int8_t *s1, int32_t n1, const int8_t *s2, int32_t n2, const int32_t *seeds,
+                        int32_t n_seeds, const int32_t *ip, const double *dp, int64_t *frag, double *pe,
+                        uint32_t *cigar, int frag_cap, int cigar_cap, int *n_cigar, int64_t *cells_o) {
+  Params P = params_from(ip, dp);
+  Pair pr{s1, s2, n1, n2, {}, {}};
+  pr.init();
+  std::vector<Seed4> sd(n_seeds);
+  for (int32_t k = 0; k < n_seeds; ++k) sd[k] = Seed4{seeds[4 * k], seeds[4 * k + 1], seeds[4 * k + 2], seeds[4 * k + 3]};
+  Cells cells;
+  std::vector<Frag> fr = two_piece_stage(pr, P, sd, cells);
   cells_out(cells, cells_o);
   return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
 }

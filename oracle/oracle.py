@@ -37,8 +37,17 @@ U64P = C.POINTER(C.c_uint64)
 F64P = C.POINTER(C.c_double)
 
 
-# The reference checkout the parity checker is built from (absent on hosts that only run the built files).
-REFERENCE_DIR = os.environ.get("DCNS_REFERENCE", "/root/reference")
+REF_LAZY_SO = os.path.join(HERE, "_ref", "libdcns_ref_lazy.so")
+_ref_dir = []
+
+
+def reference_dir():
+    """The reference checkout the parity checker is built from, as oracle/build_ref.sh locates it (the environment
+    variable DCNS_REFERENCE overrides the recipe's default); None on hosts without one, which only run built files."""
+    if not _ref_dir:
+        out = subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), "--where"], capture_output=True, text=True)
+        _ref_dir.append(out.stdout.strip() or None)
+    return _ref_dir[0]
 
 
 def build(force: bool = False) -> None:
@@ -47,9 +56,10 @@ def build(force: bool = False) -> None:
     src = os.path.join(HERE, "dcns_oracle.cpp")
     if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src):
         subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", src, "-o", ORACLE_SO])
-    if os.path.isdir(REFERENCE_DIR):
-        harness = os.path.join(HERE, "ref_harness.cpp")
-        if force or not os.path.exists(REF_SO) or os.path.getmtime(REF_SO) < os.path.getmtime(harness):
+    if reference_dir():
+        newest = max(os.path.getmtime(os.path.join(HERE, f))
+                     for f in ("ref_harness.cpp", "lazy_matrix.cpp", "build_ref.sh"))
+        if force or any(not os.path.exists(p) or os.path.getmtime(p) < newest for p in (REF_SO, REF_LAZY_SO)):
             subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")], stdout=subprocess.DEVNULL)
 
 
@@ -122,10 +132,14 @@ class Oracle(_Lib):
                                     I32P, U64P, I64P]
         L.or_sliding.argtypes = [I8P, C.c_int32, I8P, C.c_int32, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                  F64P, I32P, C.c_int]
+        L.or_xextend_batch.argtypes = [C.c_int, C.POINTER(I8P), I32P, C.POINTER(I8P), I32P] + [C.c_int] * 7 + \
+            [I32P, U64P, I64P]
         L.or_find_weighted.argtypes = [C.c_int, I8P, C.c_int32, I8P, C.c_int32, C.POINTER(C.c_int16), I32P, C.c_int32,
                                        I32P, F64P, I64P, F64P, U32P, C.c_int, C.c_int, I32P, I64P]
         L.or_find_seeded_2gap.argtypes = [I8P, C.c_int32, I8P, C.c_int32, I32P, C.c_int32, C.c_int32, I32P, F64P, I64P,
                                           F64P, U32P, C.c_int, C.c_int, I32P, I64P]
+        L.or_find_xseeds_2gap.argtypes = [I8P, C.c_int32, I8P, C.c_int32, I32P, C.c_int32, I32P, F64P, I64P, F64P,
+                                          U32P, C.c_int, C.c_int, I32P, I64P]
 
     def sw(self, ref, read, open=-4, ext=-2, match=2, mismatch=-3, mode=0):
         """mode 0: the reference's own dispatch; 1: striped (AVX2) semantics; 2: scalar semantics."""
@@ -219,6 +233,24 @@ class Oracle(_Lib):
         assert n >= 0, "fragment buffer too small"
         return _unflatten(n, frag, pe, cg)
 
+    def find_xseeds(self, s1, s2, seeds, **kw):
+        """The x-seed overload without maximumAlignLength (findSimilar...4.cpp:532): seeds = [(start1, end1, start2,
+        end2)] 0-based, in order."""
+        _, ip, dp = params(**kw)
+        s1, s2 = _i8(s1), _i8(s2)
+        sd = np.asarray(seeds, np.int32).reshape(-1, 4)
+        fcap, ccap = 4096, 1 << 20
+        frag = np.zeros((fcap, 8), np.int64)
+        pe = np.zeros((fcap, 2), np.float64)
+        cg = np.zeros(ccap, np.uint32)
+        nc = np.zeros(1, np.int32)
+        cells = np.zeros(4, np.int64)
+        n = self.lib.or_find_xseeds_2gap(_p(s1, I8P), len(s1), _p(s2, I8P), len(s2), _p(sd, I32P), len(sd),
+                                         _p(ip, I32P), _p(dp, F64P), _p(frag, I64P), _p(pe, F64P), _p(cg, U32P), fcap,
+                                         ccap, _p(nc, I32P), _p(cells, I64P))
+        assert n >= 0, "fragment buffer too small"
+        return _unflatten(n, frag, pe, cg)
+
     def find_batch(self, pairs, two_gap=False, threads=1, **kw):
         """pairs: list of (seq1 codes, seq2 codes).  Returns (n_fragments per pair, checksum, cells)."""
         _, ip, dp = params(**kw)
@@ -235,6 +267,22 @@ class Oracle(_Lib):
                                int(threads), _p(nf, I32P), _p(ck, U64P), _p(cells, I64P))
         return nf, int(ck[0]), dict(zip(("scan", "scan_rev", "xdrop", "semiglobal"), map(int, cells)))
 
+    def xextend_batch(self, tasks, threads=1, open=-4, ext=-2, match=2, mismatch=-3, xdrop=20, w=10):
+        """x_extend_seed's two passes (forward, then with traceback) per (seq1, seq2) task on `threads` threads.
+        Returns (traceback-pass scores, checksum, algorithmic cells of both passes)."""
+        keep = [(_i8(a), _i8(b)) for a, b in tasks]
+        n = len(keep)
+        p1 = (I8P * max(n, 1))(*[_p(a, I8P) for a, _ in keep])
+        p2 = (I8P * max(n, 1))(*[_p(b, I8P) for _, b in keep])
+        n1 = np.array([len(a) for a, _ in keep] or [0], np.int32)
+        n2 = np.array([len(b) for _, b in keep] or [0], np.int32)
+        out = np.zeros(max(n, 1), np.int32)
+        ck = np.zeros(1, np.uint64)
+        cells = np.zeros(1, np.int64)
+        self.lib.or_xextend_batch(n, p1, _p(n1, I32P), p2, _p(n2, I32P), open, ext, match, mismatch, xdrop, w,
+                                  int(threads), _p(out, I32P), _p(ck, U64P), _p(cells, I64P))
+        return out[:n], int(ck[0]), int(cells[0])
+
     def sliding(self, ref, other, window=38, step=8, open=-4, ext=-2, match=2, mismatch=-3):
         ref, other = _i8(ref), _i8(other)
         cap = len(ref) // max(step, 1) + 2
@@ -246,10 +294,12 @@ class Oracle(_Lib):
 
 
 class Reference(_Lib):
-    """The unmodified reference behind oracle/ref_harness.cpp (libdcns_ref.so)."""
+    """The unmodified reference behind oracle/ref_harness.cpp (libdcns_ref.so).  lazy=True loads the same code with
+    oracle/lazy_matrix.cpp in place of its dense traceback matrix (libdcns_ref_lazy.so), for pairs whose dense matrix
+    would not fit in memory."""
 
-    def __init__(self):
-        super().__init__(REF_SO)
+    def __init__(self, lazy: bool = False):
+        super().__init__(REF_LAZY_SO if lazy else REF_SO)
         L = self.lib
         L.ref_sw.argtypes = [I8P, C.c_int32, I8P, C.c_int32, C.c_int, C.c_int, C.c_int, C.c_int, I32P]
         L.ref_sw_scalar.argtypes = L.ref_sw.argtypes
@@ -257,6 +307,8 @@ class Reference(_Lib):
                                         C.c_int32, C.c_char_p] + [C.c_int] * 7 + [C.c_double] * 3 + \
             [C.c_int] * 4 + [I64P, F64P, U32P, C.c_int, C.c_int, I32P]
         L.ref_find_seeded_2gap.argtypes = [I8P, C.c_int32, I8P, C.c_int32, I32P, C.c_int32, C.c_int32] + \
+            [C.c_int] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int, I64P, F64P, U32P, C.c_int, C.c_int, I32P]
+        L.ref_find_xseeds_2gap.argtypes = [I8P, C.c_int32, I8P, C.c_int32, I32P, C.c_int32] + \
             [C.c_int] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int, I64P, F64P, U32P, C.c_int, C.c_int, I32P]
         L.ref_xextend.argtypes = [I8P, C.c_int32, I8P, C.c_int32, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                   C.c_int, I32P]
@@ -379,6 +431,22 @@ class Reference(_Lib):
                                           d["mismatch"], d["pvalue"], d["lambda_"], d["kvalue"], d["zdrop"],
                                           d["bandwidth"], _p(frag, I64P), _p(pe, F64P), _p(cg, U32P), fcap, ccap,
                                           _p(nc, I32P))
+        assert n >= 0, "fragment buffer too small"
+        return _unflatten(n, frag, pe, cg)
+
+    def find_xseeds(self, s1, s2, seeds, **kw):
+        d, _, _ = params(**kw)
+        s1, s2 = _i8(s1), _i8(s2)
+        sd = np.asarray(seeds, np.int32).reshape(-1, 4)
+        fcap, ccap = 4096, 1 << 20
+        frag = np.zeros((fcap, 8), np.int64)
+        pe = np.zeros((fcap, 2), np.float64)
+        cg = np.zeros(ccap, np.uint32)
+        nc = np.zeros(1, np.int32)
+        n = self.lib.ref_find_xseeds_2gap(_p(s1, I8P), len(s1), _p(s2, I8P), len(s2), _p(sd, I32P), len(sd),
+                                          d["open1"], d["ext1"], d["open2"], d["ext2"], d["match"], d["mismatch"],
+                                          d["pvalue"], d["lambda_"], d["kvalue"], d["zdrop"], d["bandwidth"],
+                                          _p(frag, I64P), _p(pe, F64P), _p(cg, U32P), fcap, ccap, _p(nc, I32P))
         assert n >= 0, "fragment buffer too small"
         return _unflatten(n, frag, pe, cg)
 

@@ -284,6 +284,33 @@ int ref_find_seeded_2gap(const int8_t *s1, int32_t L1, const int8_t *s2, int32_t
   return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
 }
 
+// The x-seed overload without maximumAlignLength, impl/findSimilarFragmentsForPairedSequence4.cpp:532-616, with the
+// traceback matrix its caller (the 2-gap overload, :769) allocates: (L1 + 1) x (L2 + 1).
+int ref_find_xseeds_2gap(const int8_t *s1, int32_t L1, const int8_t *s2, int32_t L2, const int32_t *seeds,
+                         int32_t n_seeds, int open1, int ext1, int open2, int ext2, int match, int mismatch,
+                         double pvalue, double lambda, double kvalue, int zdrop, int bandwidth, int64_t *frag,
+                         double *pe, uint32_t *cigar, int frag_cap, int cigar_cap, int *n_cigar) {
+  Scorei m((int8_t)match, (int8_t)mismatch);
+  std::vector<int8_t> a = copyseq(s1, L1), b = copyseq(s2, L2);
+  std::vector<int8_t> ar = revcomp(s1, L1), br = revcomp(s2, L2);
+  int32_t l1 = L1, l2 = L2, win = 38;
+  std::string str1, str2;
+  std::vector<Seed> sd;
+  for (int32_t k = 0; k < n_seeds; ++k) {
+    int32_t a1 = seeds[4 * k], e1 = seeds[4 * k + 1], a2 = seeds[4 * k + 2], e2 = seeds[4 * k + 3];
+    sd.emplace_back(a1, e1, a2, e2);
+  }
+  Matrix T(L1 + 1, L2 + 1);
+  std::vector<PairedSimilarFragment> fr;
+  {
+    Silence quiet;
+    fr = findSimilarFragmentsForPairedSequence(a.data(), ar.data(), b.data(), br.data(), l1, l2, win, open1, ext1,
+                                               open2, ext2, match, mismatch, m, str1, str2, pvalue, lambda, kvalue,
+                                               zdrop, bandwidth, sd, T);
+  }
+  return flatten(fr, frag, pe, cigar, frag_cap, cigar_cap, n_cigar);
+}
+
 // The weighted drivers, impl/findSimilarFragmentsForPairedSequence4.cpp:784 (pieces 1) and :883 (pieces 2).  The
 // categories are written as a Score folder (matrixList + one 7-line file per category, model/Score.cpp:3) under
 // score_dir.  The weight arrays get one extra entry on each side repeating the end categories, so the reference's

@@ -213,6 +213,6 @@ def main(refdir):
 
 
 if __name__ == "__main__":
-    refdir = sys.argv[1] if len(sys.argv) > 1 else O.REFERENCE_DIR
+    refdir = sys.argv[1] if len(sys.argv) > 1 else O.reference_dir()
     O.build()
     main(refdir)

@@ -328,9 +328,10 @@ def test_long_pairs_200kb_full_size_alone_equals_in_batch(eng):
     assert [f.cigar for f in alone] == [f.cigar for f in mixed]
 
 
-def test_one_reference_many_queries_shared_upload(eng):
-    """The multi-species pattern (one reference x N queries, p-value filter off as that caller sets it): one batched
-    call with the reference packed once gives the per-pair results."""
+def test_one_reference_many_queries_shared_upload(eng, oracle):
+    """The multi-species pattern (one reference x N queries, p-value filter off as that caller sets it,
+    getCnsForMultipleSpecies.cpp:126-135): one batched call with the reference packed once gives the oracle's
+    per-pair results."""
     rng = np.random.default_rng(515)
     ref_txt = W.planted_pair(rng, 6000, 10, 0, 30, 60, 0.9, 0.9, 0.0, 0.1)[0]
     ref = W.prepare(ref_txt)
@@ -342,8 +343,7 @@ def test_one_reference_many_queries_shared_upload(eng):
         queries.append(W.prepare(seg.decode()))
     got = eng.align_one_to_many(ref, queries, pvalue=1.0)
     for k, q in enumerate(queries):
-        exp = eng.align_pairs([(ref.copy(), q)], 1, pvalue=1.0)[0]
-        assert frag_keys(got[k]) == frag_keys(exp), k
+        assert_same_fragments(got[k], oracle.find(ref, q, pvalue=1.0)[0], k)
 
 
 @pytest.mark.parametrize("max_align", [0, 400])
@@ -357,6 +357,17 @@ def test_seeded_two_gap_vs_oracle(eng, oracle, max_align):
     for k, (A, B, seeds) in enumerate(cases):
         exp = oracle.find_seeded(A, B, seeds, max_align if max_align > 0 else 1 << 30)
         assert_same_fragments(got[k], exp, k)
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(bandwidth=40, zdrop=20, open2=-30, ext2=-1)])
+def test_xseed_overload_vs_oracle(eng, oracle, kw):
+    """The x-seed overload without maximumAlignLength (the 2-gap overload's 2-piece stage) on caller-given seeds."""
+    from test_oracle_pin import _seeded_cases
+
+    cases = _seeded_cases(oracle, n=4, seed=9)
+    got = eng.align_xseeds([(A, B) for A, B, _ in cases], [s for _, _, s in cases], **kw)
+    for k, (A, B, seeds) in enumerate(cases):
+        assert_same_fragments(got[k], oracle.find_xseeds(A, B, seeds, **kw), k)
 
 
 @pytest.mark.parametrize("pieces,bandwidth", [(1, 20000), (2, 20000), (2, 30), (1, 30)])

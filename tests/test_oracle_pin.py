@@ -163,6 +163,23 @@ def test_seeded_two_gap_matches_reference(oracle, reference):
     assert n > 20
 
 
+def test_xseed_overload_matches_reference(oracle, reference):
+    """The x-seed overload without maximumAlignLength (findSimilarFragmentsForPairedSequence4.cpp:532-616), on the
+    same seed sets, both default and narrow-band / low z-drop 2-piece parameters."""
+    if reference is None:
+        pytest.skip("reference not built on this host")
+    n = 0
+    for A, B, seeds in _seeded_cases(oracle, n=4, seed=5):
+        for kw in (dict(), dict(bandwidth=40, zdrop=20, open2=-30, ext2=-1)):
+            got = oracle.find_xseeds(A, B, seeds, **kw)
+            exp = reference.find_xseeds(A, B, seeds, **kw)
+            assert [f.key() for f in got] == [f.key() for f in exp], kw
+            for x, y in zip(got, exp):
+                assert abs(x.pvalue - y.pvalue) <= 1e-12 * max(1.0, abs(y.pvalue))
+            n += len(got)
+    assert n > 20
+
+
 WEIGHT_CATS = [(2, -3, -4, -2, -45, 0, 100), (3, -4, -6, -2, -60, -1, 50), (1, -2, -3, -1, -30, 0, 200)]
 
 
