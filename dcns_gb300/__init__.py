@@ -121,7 +121,7 @@ class Stats(C.Structure):
                [("scan_launches", C.c_int32), ("kernel_launches", C.c_int32), ("scan_rounds", C.c_int32),
                 ("xdrop_rounds", C.c_int32), ("ms_xdrop_kernel", C.c_double), ("bytes_h2d", C.c_int64),
                 ("ms_xdrop_tb_kernel", C.c_double), ("ms_sg_kernel", C.c_double), ("ms_sg_tb_kernel", C.c_double),
-                ("bytes_codes_xdrop", C.c_int64), ("bytes_codes_sg", C.c_int64)]
+                ("bytes_codes_xdrop", C.c_int64), ("bytes_codes_sg", C.c_int64), ("bytes_device", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -139,14 +139,16 @@ class ServingStats(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("lanes", C.c_int32), ("bins", C.c_int32), ("bin_ratio", C.c_double),
                 ("scan_tiles_per_thread", C.c_int32), ("sg_warps", C.c_int32), ("n_bins_tuned", C.c_int32),
-                ("xdrop_warp_from", C.c_int32 * 16), ("xdrop_wave_max_w", C.c_int32 * 16), ("xdrop_flat", C.c_int32 * 16)]
+                ("xdrop_warp_from", C.c_int32 * 16), ("xdrop_wave_max_w", C.c_int32 * 16), ("xdrop_flat", C.c_int32 * 16),
+                ("xdrop_handoff", C.c_int32 * 16)]
 
     def as_dict(self):
         n = max(self.n_bins_tuned, 1)
         return {"lanes": self.lanes, "bins": self.bins, "bin_ratio": self.bin_ratio,
                 "scan_tiles_per_thread": self.scan_tiles_per_thread, "sg_warps": self.sg_warps,
                 "xdrop_per_bin": [{"warp_from": self.xdrop_warp_from[b], "wave_max_w": self.xdrop_wave_max_w[b],
-                                   "row_interleaved": bool(self.xdrop_flat[b])} for b in range(n)]}
+                                   "row_interleaved": bool(self.xdrop_flat[b]),
+                                   "handoff_rows": self.xdrop_handoff[b]} for b in range(n)]}
 
 
 class Results(C.Structure):

@@ -489,6 +489,7 @@ int dcns_get_tuning(const dcns_ctx *ctx, dcns_tuning *out) {
     out->xdrop_warp_from[b] = own ? C.bin_tune[b].xdrop_warp_from : C.xdrop_warp_from;
     out->xdrop_wave_max_w[b] = own ? C.bin_tune[b].xdrop_wave_max_w : C.xdrop_wave_max_w;
     out->xdrop_flat[b] = (own ? C.bin_tune[b].xdrop_flat : C.xdrop_flat) ? 1 : 0;
+    out->xdrop_handoff[b] = own ? C.bin_tune[b].xdrop_handoff : C.xdrop_handoff;
   }
   return DCNS_OK;
 }

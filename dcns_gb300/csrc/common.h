@@ -143,6 +143,27 @@ struct SgRec {
   int m, f1, f2;
 };
 
+// The stripe-flow form of the unweighted semi-global kernel (semiglobal.cu, sg_flow_kernel): per DP, its boundary
+// row and the state of its in-order row evaluation; per launch, the DPs in queue order and their stripes as units.
+struct SgFlowDP {
+  int64_t bnd_off;                  // the DP's boundary row: n2 + 2 records of SgFlow::bnd
+  int evaluated, stop;              // stripes evaluated in row order; 1 once the DP ended
+  int mx, e1r, e2r, rows;           // running evaluation after `evaluated` stripes (initially 0, -1, -1, 0)
+  int stale_last, stale_prev;       // column n2 - 1 of rows n2 - 1 + w and n2 - 2 + w (initially kOut)
+};
+struct SgFlow {
+  SgTask *tasks;
+  const int *idx;                   // queue order: DP q is tasks[idx[q]]
+  const int64_t *unit_begin;        // [n]: first unit (stripe) of DP q; DP q has max(1, stripes) units
+  SgFlowDP *dps;                    // [n], queue order
+  SgRec *bnd;
+  int *prog;                        // [total_units]: columns of the unit's last row published (zero before launch)
+  unsigned long long *unit_counter; // zero before launch
+  int *err;                         // set to 1 when a wait ran out of iterations (zero before launch)
+  int64_t total_units;
+  int n, pad;
+};
+
 // ---- kernel launchers (defined in the .cu files)
 void launch_pack(const int8_t *codes, const int64_t *src_off, const int64_t *dst_base, const int32_t *len, int nseq,
                  uint32_t *pk, uint32_t *nm, cudaStream_t st);
@@ -159,16 +180,29 @@ void launch_scan_generic(const ScanTask *tasks, const int *idx, int n, const int
                          unsigned long long *keys, int32_t *scratch, int64_t scratch_per_thread, cudaStream_t st);
 void launch_reverse(ScanTask *tasks, int first, int n, const unsigned long long *keys, const int64_t *pair_base,
                     const int32_t *pair_len, Arena ar, Params p, cudaStream_t st);
+// wcap: 10 or 20 (one thread per pass, band in registers), 0 (one warp per pass, band in scratch), -1 (one warp per
+// pass as a wavefront, w <= 256: for long passes)
 void launch_xdrop(XTask *tasks, const int *idx, int n, Arena ar, Params p, uint32_t *tb, int wcap, int32_t *scratch,
                   int64_t scratch_per_thread, cudaStream_t st);
 void launch_xdrop_traceback(XTask *tasks, const int *idx, int n, const uint32_t *tb, uint32_t *cig, cudaStream_t st);
 // Chained x-drop levels (one launch per band width, work lists and counts in device memory).
 void launch_xdrop_iota(int *list, int n, int *count, cudaStream_t st);
+// Hand-off of long register-band passes to the wavefront form: a pass of a row-interleaved level still running after
+// `rows` rows moves its band state to one of `cap` spill slots (2 x (2 x 20 + 2) ints each) and its id to list;
+// *count (zero before the level) counts the slots taken.  rows = 0 or cap = 0: off.
+struct XHandoff {
+  int *list, *count;
+  int32_t *spill;
+  int cap, rows;
+};
+constexpr int kXdropSpillInts = 2 * (2 * 20 + 2);
 // fetch: the level's pass counter, zero before the launch (the row-interleaved register-band kernel, flat = true).
-void launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
-                        int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int *fetch,
-                        Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm, int32_t *scratch,
-                        int64_t per_warp, int warps, int warp_from, int wave_max_w, bool flat, cudaStream_t st);
+// Returns the number of kernels launched.
+int launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
+                       int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int *fetch,
+                       const XHandoff &H, Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm,
+                       int32_t *scratch, int64_t per_warp, int warps, int warp_from, int wave_max_w, bool flat,
+                       cudaStream_t st);
 void launch_xdrop_traceback_all(XTask *tasks, int n, const uint32_t *tb, uint32_t *cig,
                                 unsigned long long *cig_cursor, cudaStream_t st);
 // Packs the CIGARs of every finished task in task order into dense (cig_dense offsets); *total = their words.
@@ -178,6 +212,8 @@ void launch_xdrop_cigar_pack(XTask *tasks, int n, const uint32_t *cig, uint32_t 
 void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p, uint8_t *tb, void *bnd,
                        int max_n2, int *work_counter, int grid, int nw, cudaStream_t st);
 int sg_ctas_per_sm(int nw);
+void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, int nsm, cudaStream_t st);
+int64_t sg_flow_units(int n1, int n2, int w);  // stripe units of one DP in the flow form (at least 1)
 int64_t sg_bnd_bytes(int grid, int max_n2, int nw);
 void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, uint32_t *cig,
                          cudaStream_t st, bool weighted_layout = false);

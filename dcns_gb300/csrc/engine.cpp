@@ -148,10 +148,14 @@ void init_context(Context &C, int device, size_t budget) {
   if (const char *e = std::getenv("DCNS_XDROP_WARP_FROM")) C.xdrop_warp_from = std::max(0, std::atoi(e));
   if (const char *e = std::getenv("DCNS_XDROP_WAVE")) C.xdrop_wave_max_w = std::max(0, std::atoi(e));
   if (const char *e = std::getenv("DCNS_XDROP_FLAT")) C.xdrop_flat = std::atoi(e) != 0;
+  if (const char *e = std::getenv("DCNS_XDROP_HANDOFF")) C.xdrop_handoff = std::max(0, std::atoi(e));
   if (const char *e = std::getenv("DCNS_SCAN_TILES")) C.scan_tiles_per_thread = std::max(1, std::min(64, std::atoi(e)));
   if (const char *e = std::getenv("DCNS_SG_WARPS")) {
     const int v = std::atoi(e);
     C.sg_warps = (v == 2 || v == 4 || v == kSgNW) ? v : 0;
+  }
+  if (const char *e = std::getenv("DCNS_SG_FLOW")) {
+    C.sg_flow = std::atoi(e) != 0;
   }
   if (const char *e = std::getenv("DCNS_BIN_RATIO")) C.bin_ratio = std::max(0.1, std::min(1.0, std::atof(e)));
 }
@@ -1003,6 +1007,15 @@ int64_t band_cells(int rows, int w, int n2) {
 
 int wpr_of(int w) { return (2 * w + 1 + 7) / 8; }
 
+// Device bytes the context's buffers hold, its lanes' included (buffers only grow, so after a call this is at least
+// what the call used).
+int64_t device_bytes(const Context &C) {
+  int64_t b = (int64_t)C.used;
+  for (const auto &L : C.lanes)
+    if (L) b += (int64_t)L->used;
+  return b;
+}
+
 // Runs the passes `subset` of X to completion in host-driven rounds (band restarts, traceback-slot growth), then
 // their tracebacks when want_codes; X lives on the host between launches.  Traceback slots start at the whole pass
 // (full_slots) or at min(n1, 1024) rows.  With want_codes, every finished pass's CIGAR is appended to *flat and
@@ -1039,11 +1052,14 @@ void run_xdrop_rounds(Context &C, std::vector<XTask> &X, const Params &P, bool w
       for (int64_t q = b * 4096, e = std::min(m, q + 4096); q < e; ++q) Xc[q] = X[pend[q]];
     });
     h2d(C, C.d_x, Xc, (size_t)m);
-    std::vector<int32_t> g10, g20, gw;
+    // passes known to be long (they outgrew their slot in the levels: full_slots) run as wavefronts up to w = 256
+    std::vector<int32_t> g10, g20, gw, gwave;
     int maxw = 0;
     for (int64_t q = 0; q < m; ++q) {
       const int w = Xc[q].w;
-      if (w <= 10)
+      if (full_slots && w <= 256)
+        gwave.push_back((int32_t)q);
+      else if (w <= 10)
         g10.push_back((int32_t)q);
       else if (w <= 20)
         g20.push_back((int32_t)q);
@@ -1070,6 +1086,7 @@ void run_xdrop_rounds(Context &C, std::vector<XTask> &X, const Params &P, bool w
     };
     tp = phase(C, "xd_prep", tp);
     DCNS_CK(cudaEventRecord(C.ev0, C.st));
+    launch_group(gwave, -1);
     launch_group(g10, 10);
     launch_group(g20, 20);
     launch_group(gw, 0);
@@ -1197,8 +1214,13 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
       warps[L] = (int)(std::min<int64_t>({n, cap, (int64_t)C.nsm * 64}) + 3) / 4 * 4;  // whole blocks of 4 warps
       scratch_ints = std::max(scratch_ints, warps[L] * per_warp[L]);
     }
+    // hand-off slots of the register-band levels (one level at a time: the resume kernel empties them before the
+    // next level starts)
+    const bool any_flat = C.xdrop_flat && C.xdrop_handoff > 0 && std::min(C.xdrop_warp_from, 20) >= w0;
+    const int spill_cap = any_flat ? (int)std::min<int64_t>(n, 1 << 16) : 0;
     C.d_x.ensure(C, sizeof(XTask) * n);
-    C.d_idx.ensure(C, sizeof(int32_t) * (3 * n + 4 + nlev + 64));
+    C.d_idx.ensure(C, sizeof(int32_t) * (3 * n + spill_cap + 4 + 2 * nlev + 64));
+    if (spill_cap > 0) C.d_spill.ensure(C, sizeof(int32_t) * (size_t)spill_cap * kXdropSpillInts);
     C.d_counter.ensure(C, 64);
     if (want_codes) {
       C.d_tb.ensure(C, sizeof(uint32_t) * tb_words);
@@ -1206,21 +1228,25 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
     }
     if (scratch_ints > 1) C.d_scratch.ensure(C, sizeof(int32_t) * scratch_ints);
     int *lists = C.d_idx.as<int>();
-    int *cnt = lists + 3 * n;  // [0], [1]: the two work-list counts, [2]: retry count, [4 + L]: level L's fetch
+    // [0], [1]: the two work-list counts, [2]: retry count, [4 + L]: level L's fetch, [4 + nlev + L]: its hand-offs
+    int *cnt = lists + 3 * n;
+    int *long_list = cnt + 4 + 2 * nlev + 64;
     unsigned long long *cur = C.d_counter.as<unsigned long long>();  // [0]: traceback arena, [1]: CIGAR arena
     h2d(C, C.d_x, X.data(), (size_t)n);
-    DCNS_CK(cudaMemsetAsync(cnt, 0, sizeof(int) * (4 + nlev), C.st));
+    DCNS_CK(cudaMemsetAsync(cnt, 0, sizeof(int) * (4 + 2 * nlev), C.st));
     DCNS_CK(cudaMemsetAsync(cur, 0, sizeof(unsigned long long) * 2, C.st));
     launch_xdrop_iota(lists, (int)n, cnt, C.st);
     DCNS_CK(cudaEventRecord(C.ev0, C.st));
-    int in = 0;
+    int in = 0, launched = 0;
     for (int L = 0; L < nlev; ++L) {
       const int out = 1 - in;
       DCNS_CK(cudaMemsetAsync(cnt + out, 0, sizeof(int), C.st));
-      launch_xdrop_level(C.d_x.as<XTask>(), lists + in * n, cnt + in, lists + out * n, cnt + out, lists + 2 * n,
-                         cnt + 2, cur, want_codes ? tb_words : 0, cnt + 4 + L, C.arena, P, C.d_tb.as<uint32_t>(),
-                         w0 << L, (int)n, C.nsm, C.d_scratch.as<int32_t>(), per_warp[L], warps[L], C.xdrop_warp_from,
-                         C.xdrop_wave_max_w, C.xdrop_flat, C.st);
+      const XHandoff H{long_list, cnt + 4 + nlev + L, C.d_spill.as<int32_t>(), spill_cap, C.xdrop_handoff};
+      launched += launch_xdrop_level(C.d_x.as<XTask>(), lists + in * n, cnt + in, lists + out * n, cnt + out,
+                                     lists + 2 * n, cnt + 2, cur, want_codes ? tb_words : 0, cnt + 4 + L, H, C.arena, P,
+                                     C.d_tb.as<uint32_t>(), w0 << L, (int)n, C.nsm, C.d_scratch.as<int32_t>(),
+                                     per_warp[L], warps[L], C.xdrop_warp_from, C.xdrop_wave_max_w, C.xdrop_flat,
+                                     C.st);
       in = out;
     }
     DCNS_CK(cudaEventRecord(C.ev1, C.st));
@@ -1231,7 +1257,7 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
                               cur + 1, C.st);
       DCNS_CK(cudaEventRecord(C.ev2, C.st));
     }
-    C.stats.kernel_launches += nlev + 1 + (want_codes ? 3 : 0);
+    C.stats.kernel_launches += launched + 1 + (want_codes ? 3 : 0);
     C.stats.xdrop_rounds += 1;
     C.h_misc.ensure(sizeof(int32_t) * (n + 8) + 64);
     int32_t *hret = C.h_misc.as<int32_t>();  // [0]: leftover count, [1]: retry count, [8..]: retry list
@@ -1403,16 +1429,25 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
   const int64_t cap_bytes = std::max<int64_t>((int64_t)(free_budget / 2), (int64_t)64 << 20);
   int64_t k0 = 0;
   C.d_sg.ensure(C, sizeof(SgTask) * n);
+  // the stripe-flow form (unweighted DPs): per DP also its boundary row and flow state, per stripe a progress flag
+  const bool flow = W == nullptr && C.sg_flow;
+  auto flow_bytes = [&](const SgTask &g) -> int64_t {
+    return flow ? (int64_t)sizeof(SgRec) * (std::max(g.n2, 0) + 2) + (int64_t)sizeof(SgFlowDP) + 8 +
+                      4 * sg_flow_units(g.n1, g.n2, P.bandwidth)
+                : 0;
+  };
   while (k0 < n) {
-    int64_t bytes = 0, k1 = k0;
+    int64_t bytes = 0, extra = 0, k1 = k0;
     while (k1 < n) {
       const int64_t b =
           !want_codes ? 0 : W ? sgw_tb_bytes(G[k1].n1, G[k1].n2, P.bandwidth) : sg_tb_bytes(G[k1].n1, G[k1].n2, P.bandwidth);
-      if (k1 > k0 && bytes + b > cap_bytes) break;
+      const int64_t e = flow_bytes(G[k1]);
+      if (k1 > k0 && bytes + extra + b + e > cap_bytes) break;
       G[k1].tb_off = bytes;
       G[k1].tb_bytes = b;
       G[k1].want_codes = want_codes ? 1 : 0;
       bytes += b;
+      extra += e;
       ++k1;
     }
     const int64_t m = k1 - k0;
@@ -1425,10 +1460,9 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
     const int grid = (int)std::min<int64_t>(m, W ? (int64_t)C.nsm * 16 : (int64_t)C.nsm * sg_ctas_per_sm(nw));
     int maxn2 = 1;
     for (int64_t q = k0; q < k1; ++q) maxn2 = std::max(maxn2, G[q].n2);
-    C.d_bnd.ensure(C, (size_t)(W ? sgw_bnd_bytes((grid + 3) / 4 * 4, maxn2) : sg_bnd_bytes(grid, maxn2, nw)));
     C.d_counter.ensure(C, 64);
     DCNS_CK(cudaMemsetAsync(C.d_counter.p, 0, sizeof(int), C.st));
-    // largest DPs first: the CTA work queue then finishes with the small ones
+    // largest DPs first: the work queue then finishes with the small ones
     std::vector<int32_t> idx(m);
     for (int64_t q = 0; q < m; ++q) idx[q] = (int32_t)(k0 + q);
     std::sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) {
@@ -1439,14 +1473,53 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
     C.d_idx.ensure(C, sizeof(int32_t) * m);
     h2d(C, C.d_idx, idx.data(), (size_t)m);
     h2d(C, C.d_sg, G.data(), (size_t)n);
+    SgFlow F{};
+    if (flow) {
+      // units (stripes) and boundary rows in queue order; flow state in one buffer: unit_begin | dps | prog | counters
+      std::vector<int64_t> ub((size_t)m);
+      std::vector<SgFlowDP> dps((size_t)m);
+      int64_t units = 0, brows = 0;
+      for (int64_t q = 0; q < m; ++q) {
+        const SgTask &g = G[idx[q]];
+        ub[q] = units;
+        units += sg_flow_units(g.n1, g.n2, P.bandwidth);
+        dps[q] = SgFlowDP{brows, 0, 0, 0, -1, -1, 0, kOut, kOut};
+        brows += std::max(g.n2, 0) + 2;
+      }
+      auto al = [](int64_t b) { return (b + 255) / 256 * 256; };
+      const int64_t o_dps = al(8 * m), o_prog = o_dps + al((int64_t)sizeof(SgFlowDP) * m);
+      const int64_t o_cnt = o_prog + al(4 * units), total = o_cnt + 256;
+      C.d_flow.ensure(C, (size_t)total);
+      C.d_bnd.ensure(C, (size_t)(sizeof(SgRec) * brows));
+      char *base = static_cast<char *>(C.d_flow.p);
+      DCNS_CK(cudaMemcpyAsync(base, ub.data(), 8 * m, cudaMemcpyHostToDevice, C.st));
+      DCNS_CK(cudaMemcpyAsync(base + o_dps, dps.data(), sizeof(SgFlowDP) * m, cudaMemcpyHostToDevice, C.st));
+      DCNS_CK(cudaMemsetAsync(base + o_prog, 0, (size_t)(total - o_prog), C.st));
+      F.tasks = C.d_sg.as<SgTask>();
+      F.idx = C.d_idx.as<int>();
+      F.unit_begin = reinterpret_cast<const int64_t *>(base);
+      F.dps = reinterpret_cast<SgFlowDP *>(base + o_dps);
+      F.bnd = C.d_bnd.as<SgRec>();
+      F.prog = reinterpret_cast<int *>(base + o_prog);
+      F.unit_counter = reinterpret_cast<unsigned long long *>(base + o_cnt);
+      F.err = reinterpret_cast<int *>(base + o_cnt + 8);
+      F.total_units = units;
+      F.n = (int)m;
+    } else {
+      C.d_bnd.ensure(C, (size_t)(W ? sgw_bnd_bytes((grid + 3) / 4 * 4, maxn2) : sg_bnd_bytes(grid, maxn2, nw)));
+    }
     DCNS_CK(cudaEventRecord(C.ev0, C.st));
     if (W)
       launch_semiglobal_weighted(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, *W,
                                  C.d_sgtb.as<uint8_t>(), C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, C.st);
+    else if (flow)
+      launch_semiglobal_flow(F, C.arena, P, C.d_sgtb.as<uint8_t>(), C.nsm, C.st);
     else
       launch_semiglobal(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, C.d_sgtb.as<uint8_t>(),
                         C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, nw, C.st);
     DCNS_CK(cudaEventRecord(C.ev1, C.st));
+    int flow_err = 0;
+    if (flow) DCNS_CK(cudaMemcpyAsync(&flow_err, F.err, sizeof(int), cudaMemcpyDeviceToHost, C.st));
     C.stats.kernel_launches += 1;
     C.stats.semiglobal_dps += m;
     auto kernel_ms = [&](cudaEvent_t a, cudaEvent_t b) {
@@ -1454,9 +1527,13 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
       DCNS_CK(cudaEventElapsedTime(&ms, a, b));
       return (double)ms;
     };
+    auto check_flow = [&]() {
+      if (flow_err != 0) throw Error(DCNS_ERR_DEVICE, "semi-global stripe flow: a wait ran out of iterations");
+    };
     if (want_codes) {
       d2h(C, G.data(), C.d_sg, (size_t)n);
       sync(C);
+      check_flow();
       C.stats.ms_sg_kernel += kernel_ms(C.ev0, C.ev1);
       int64_t cw = 0;
       for (int64_t q = k0; q < k1; ++q) {
@@ -1484,6 +1561,7 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
     } else {
       d2h(C, G.data(), C.d_sg, (size_t)n);
       sync(C);
+      check_flow();
       C.stats.ms_sg_kernel += kernel_ms(C.ev0, C.ev1);
     }
     k0 = k1;
@@ -1787,6 +1865,7 @@ void align_seeded(Context &C, const std::vector<PairIn> &pairs, const std::vecto
   upload(C, pairs);
   seeded_two_gap(C, pairs, seeds, P, out);
   C.stats.ms_total = ms_since(t0);
+  C.stats.bytes_device = device_bytes(C);
 }
 
 void align_xseeds(Context &C, const std::vector<PairIn> &pairs, const std::vector<std::vector<Seed4>> &seeds,
@@ -1801,6 +1880,7 @@ void align_xseeds(Context &C, const std::vector<PairIn> &pairs, const std::vecto
   upload(C, pairs);
   two_gap_stage(C, pairs, P, seeds, out);
   C.stats.ms_total = ms_since(t0);
+  C.stats.bytes_device = device_bytes(C);
 }
 
 // getAllExtendSeed's p-value filter and x-seed merge (findSimilarFragmentsForPairedSequence4.cpp:395-427).
@@ -1882,6 +1962,7 @@ void align_weighted(Context &C, const std::vector<PairIn> &pairs, const std::vec
   }
   C.weights = nullptr;
   C.stats.ms_total = ms_since(t0);
+  C.stats.bytes_device = device_bytes(C);
 }
 
 // ------------------------------------------------------------------ entry points
@@ -1909,6 +1990,7 @@ void align_pairs(Context &C, const std::vector<PairIn> &pairs, const Params &P, 
   print_phases(C, "upload");
   align_core(C, pairs, P, mode, out);
   C.stats.ms_total = ms_since(t0);
+  C.stats.bytes_device = device_bytes(C);
 }
 
 void batch_upload(Context &C, const std::vector<PairIn> &pairs, Batch &B) {
@@ -1933,6 +2015,7 @@ void align_batch(Context &C, Batch &B, const Params &P, int mode, std::vector<st
   C.seqbase_dev = B.sb.as<int64_t>();
   align_core(C, B.lens, P, mode, out);
   C.stats.ms_total = ms_since(t0);
+  C.stats.bytes_device = device_bytes(C);
 }
 
 void autotune(Context &C, Batch &B, const Params &P, int mode) {
@@ -1964,12 +2047,15 @@ void autotune(Context &C, Batch &B, const Params &P, int mode) {
   C.max_lanes = best.lanes, C.bins = best.bins, C.bin_ratio = best.ratio;
 
   // Per bin: the x-drop pass forms (register-band levels row-interleaved or one pass per thread, the band where one
-  // warp per pass takes over, the widest band of the wavefront form), chosen by that bin's x-drop kernel time with
+  // warp per pass takes over, the widest band of the wavefront form, the rows after which a register-band pass moves
+  // to the wavefront form), chosen by that bin's x-drop kernel time with
   // each candidate applied to every bin; the bins differ in how many long and wide-band passes they hold.
   C.bin_tune.clear();
   if (C.max_lanes > 1 && (int64_t)B.lens.size() >= 4096) {
-    const Context::BinTune cands[] = {{20, 256, true}, {20, 256, false}, {10, 256, true}, {20, 128, true},
-                                      {20, 512, true}};
+    const int h = C.xdrop_handoff;
+    const Context::BinTune cands[] = {{20, 256, true, h},  {20, 256, false, 0}, {10, 256, true, h},
+                                      {20, 256, true, 0},  {20, 256, true, 48}, {20, 256, true, 192},
+                                      {20, 128, true, h}};
     const int nb = std::max(C.bins, C.max_lanes);
     std::vector<double> best_ms(nb, 1e300);
     std::vector<Context::BinTune> choice(nb, cands[0]);
@@ -2111,8 +2197,10 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
         // the bin's kernel shapes: the autotuner's per-bin choice, else the parent context's
         const Context::BinTune bt = b < (int)C.bin_tune.size()
                                         ? C.bin_tune[b]
-                                        : Context::BinTune{C.xdrop_warp_from, C.xdrop_wave_max_w, C.xdrop_flat};
+                                        : Context::BinTune{C.xdrop_warp_from, C.xdrop_wave_max_w, C.xdrop_flat,
+                                                           C.xdrop_handoff};
         L.xdrop_warp_from = bt.xdrop_warp_from, L.xdrop_wave_max_w = bt.xdrop_wave_max_w, L.xdrop_flat = bt.xdrop_flat;
+        L.xdrop_handoff = bt.xdrop_handoff;
         L.sg_warps = C.sg_warps;
         L.scan_tiles_per_thread = C.scan_tiles_per_thread;
         L.call_t0 = C.call_t0;

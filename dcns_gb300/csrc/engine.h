@@ -105,7 +105,7 @@ struct Context {
   // device buffers
   DevBuf d_codes, d_srcoff, d_dstbase, d_len, d_pk, d_nm, d_seqbase, d_flag;
   DevBuf d_tasks, d_keys, d_tiles, d_counter, d_idx, d_scratch;
-  DevBuf d_x, d_tb, d_cig, d_sg, d_sgtb, d_bnd, d_wts, d_cats;
+  DevBuf d_x, d_tb, d_cig, d_sg, d_sgtb, d_bnd, d_wts, d_cats, d_spill, d_flow;
   const WeightSet *weights = nullptr;  // set during a weighted call
   // pinned staging
   HostBuf h_codes, h_misc, h_out, h_tasks, h_tiles;
@@ -127,8 +127,13 @@ struct Context {
   int xdrop_wave_max_w = 256;
   // register-band levels (w <= 20) as the row-interleaved kernel (DCNS_XDROP_FLAT=0: one pass per thread)
   bool xdrop_flat = true;
+  // a pass of a row-interleaved level still running after this many rows moves to the wavefront form
+  // (DCNS_XDROP_HANDOFF; 0 = off)
+  int xdrop_handoff = 96;
   // warps per DP of the unweighted semi-global kernel: 2, 4 or 8 (DCNS_SG_WARPS; 0 = by the number of DPs)
   int sg_warps = 0;
+  // unweighted semi-global DPs as a flow of stripe units over one persistent grid (DCNS_SG_FLOW=0: one CTA per DP)
+  bool sg_flow = true;
   // seed-scan tiling target: reference rows are split into chunks while a launch has fewer tiles than this many per
   // resident thread (DCNS_SCAN_TILES)
   int scan_tiles_per_thread = 8;
@@ -136,6 +141,7 @@ struct Context {
   struct BinTune {
     int xdrop_warp_from, xdrop_wave_max_w;
     bool xdrop_flat;
+    int xdrop_handoff;
   };
   std::vector<BinTune> bin_tune;
   std::vector<double> last_bin_xdrop_ms;  // x-drop kernel time of each bin of the last binned call

@@ -21,6 +21,9 @@
 // first and its 128 rows are then evaluated in order; rows after a stop are discarded.  Rows past n2 + w have an empty
 // band: the reference then scores only the last column from a stale cell of column n2-1, which is replayed exactly
 // from the two values the DP left there.
+#include <algorithm>
+#include <climits>
+
 #include "device_common.cuh"
 
 namespace dcns {
@@ -313,6 +316,314 @@ void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p,
     sg_kernel<4><<<grid, 128, 0, st>>>(tasks, idx, n, ar, p, tb, (SgRec *)bnd, stride, work_counter);
   else
     sg_kernel<kSgNW><<<grid, 32 * kSgNW, 0, st>>>(tasks, idx, n, ar, p, tb, (SgRec *)bnd, stride, work_counter);
+}
+
+// ------------------------------------------------------------------ stripes as a flow of independent warp units
+// The DPs of a launch are cut into their 128-row stripes, numbered DP after DP (queue order: largest DPs first) and
+// handed out by one atomic counter; every warp of a persistent grid takes the next stripe, computes it with the
+// per-cell code of sg_kernel (same wavefront, same code layout), and takes the next.  Stripe s of a DP depends only
+// on stripe s - 1: the last row of s - 1 reaches s through the DP's boundary row in global memory (one row per DP:
+// stripe s reads a column before it overwrites it with its own last row, and s + 1 reads it only after s published
+// it), and s - 1 publishes how many columns of that row it has written (release / acquire per 32-column chunk).  So
+// a long DP runs on as many warps as it has stripes, each one chunk pair behind the stripe above it, instead of on
+// one CTA.  Stripes are handed out in increasing order and a stripe waits only on lower stripes of its own DP, which
+// are held by running warps, so the waits always end; each still has an iteration limit, after which the warp flags
+// a device error (SgFlow::err) and abandons the DP.
+//
+// Row-level decisions (running maximum, z-drop, non-positive row maximum) are taken in row order: after computing
+// stripe s, its warp waits until s - 1 is evaluated, evaluates its 128 rows from the DP's running state and
+// publishes it; the stripe whose rows stop the DP, or its last stripe, writes the DP's result.  Stripes computed past
+// the stop are abandoned at their next chunk (their codes lie past the DP's last row and are never read).
+// Iteration limit of every wait: each iteration is an L2 load and a ~200 ns sleep, so a wait gives up after about a
+// second or more; the longest legitimate wait (a stripe of 200,000 columns while its SM is shared) is some tens of ms.
+constexpr int kSgSpin = 1 << 22;
+
+__device__ __forceinline__ int sg_ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void sg_st_release(int *p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int sg_ld_relaxed(const int *p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Waits until *flag >= need, or until *stop_flag != 0; every lane polls (one broadcast load).  Returns 1 when the
+// flag is reached, 0 when the DP stopped, -1 when the iteration limit ran out or another warp already flagged an
+// error (*err), so that after one failed wait the whole grid winds down instead of timing out wait after wait.
+__device__ __forceinline__ int sg_wait_at_least(const int *flag, int need, const int *stop_flag, const int *err) {
+  for (int it = 0; it < kSgSpin; ++it) {
+    const bool ok = sg_ld_acquire(flag) >= need;
+    if (__all_sync(0xFFFFFFFFu, ok)) return 1;
+    if (__any_sync(0xFFFFFFFFu, sg_ld_relaxed(stop_flag) != 0)) return 0;
+    if ((it & 63) == 63 && __any_sync(0xFFFFFFFFu, sg_ld_relaxed(err) != 0)) return -1;
+    __nanosleep(200);
+  }
+  return -1;
+}
+
+constexpr int kSgFlowWarps = 4;  // warps per block of the flow kernel
+
+__global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Arena ar, Params P,
+                                                                   uint8_t *__restrict__ tb) {
+  __shared__ SgRec stage[kSgFlowWarps][2][32];
+  __shared__ int stage_c[kSgFlowWarps][2][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int o1 = P.open1, x1 = P.ext1, o2 = P.open2, x2 = P.ext2, w = P.bandwidth;
+  for (;;) {
+    long long u = 0;
+    if (lane == 0) u = (long long)atomicAdd(F.unit_counter, 1ull);
+    u = __shfl_sync(0xFFFFFFFFu, u, 0);
+    if (u >= F.total_units) break;
+    if (__any_sync(0xFFFFFFFFu, sg_ld_relaxed(F.err) != 0)) break;  // a wait ran out: the launch fails as a whole
+    // the DP of unit u: the last q with unit_begin[q] <= u
+    int lo = 0, hi = F.n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (F.unit_begin[mid] <= u) lo = mid; else hi = mid - 1;
+    }
+    const int q = lo, s = (int)(u - F.unit_begin[q]);
+    SgTask &T = F.tasks[F.idx[q]];
+    SgFlowDP &D = F.dps[q];
+    int *const prog_self = F.prog + u;
+    const int n1 = T.n1, n2 = T.n2;
+    const int n1_eff = (n1 <= 0 || n2 <= 0) ? 0 : min(n1, n2 + w);
+    const int nstripes = (n1_eff + kSgRows - 1) / kSgRows;
+    if (nstripes == 0) {  // nothing to align: the reference reports score 0 and ends -2 (0-based)
+      if (lane == 0) T.score = 0, T.end1 = -1, T.end2 = -1, T.rows = 0, T.status = 0;
+      continue;
+    }
+    if (__any_sync(0xFFFFFFFFu, sg_ld_relaxed(&D.stop) != 0)) {
+      if (lane == 31) sg_st_release(prog_self, INT_MAX);
+      continue;
+    }
+    const SeqView s1{T.base1, T.a1, T.dir}, s2{T.base2, T.a2, T.dir};
+    const bool codes = T.want_codes != 0;
+    const int r_last = n2 - 1 + w;
+    const int64_t stride = sg_stride_steps(n2, w);
+    SgRec *const brow = F.bnd + D.bnd_off;  // the DP's boundary row, by column
+    const int *const prog_up = s > 0 ? F.prog + (u - 1) : nullptr;
+    const int i0 = kSgRows * s + 1 + kSgR * lane;
+    const bool live = i0 <= n1_eff;
+    int ci[kSgR], c0[kSgR], c1[kSgR], e1[kSgR], e2[kSgR], best[kSgR], bestj[kSgR], prevM[kSgR];
+    bool liver[kSgR];
+#pragma unroll
+    for (int k = 0; k < kSgR; ++k) {
+      const int i = i0 + k;
+      liver[k] = i <= n1_eff;
+      c0[k] = max(i - w, 1);
+      c1[k] = min(i + w, n2);
+      ci[k] = liver[k] ? s1.at(ar, i - 1) : 0;
+      e1[k] = kOut, e2[k] = kOut, best[k] = 0, bestj[k] = 0, prevM[k] = kOut;
+    }
+    const int r0 = kSgRows * s + 1, rl = min(kSgRows * s + kSgRows, n1_eff);
+    const int jstart = max(r0 - w, 1);
+    const int nsteps = min(rl + w, n2) - jstart + 1 + 31;
+    const int upB = min(kSgRows * s + w, n2);  // the row above (128s) holds columns [max(128s - w, 1), upB]
+    const bool produce = s + 1 < nstripes;
+    uint32_t *const trow = reinterpret_cast<uint32_t *>(tb + T.tb_off) + (int64_t)s * stride * 32;
+    int abandon = 0;  // 0 computing, 1 the DP stopped, -1 a wait ran out
+    // columns jstart + 32 * chunk + lane of the row above, into stage[warp][chunk & 1]; the producer must have
+    // published them first
+    auto stage_chunk = [&](int chunk) {
+      if (s > 0 && abandon == 0) {
+        const int need = min(jstart + 32 * chunk + 31, upB);
+        const int r = sg_wait_at_least(prog_up, need, &D.stop, F.err);
+        if (r <= 0) abandon = r == 0 ? 1 : -1;
+      }
+      const int j = jstart + 32 * chunk + lane;
+      SgRec rec{kOut, kOut, kOut};
+      if (s > 0 && abandon == 0 && j >= 1 && j <= upB) {
+        rec.m = __ldcg(&brow[j].m);
+        rec.f1 = __ldcg(&brow[j].f1);
+        rec.f2 = __ldcg(&brow[j].f2);
+      }
+      stage[warp][chunk & 1][lane] = rec;
+      stage_c[warp][chunk & 1][lane] = (j >= 1 && j <= n2) ? s2.at(ar, j - 1) : 0;
+    };
+    stage_chunk(0);  // waits for columns up to jstart + 31, which include the diagonal column jstart - 1
+    int diag = (lane == 0 && s > 0 && jstart > 1 && abandon == 0) ? __ldcg(&brow[jstart - 1].m) : kOut;
+    stage_chunk(1);
+    __syncwarp();
+    int outM = kOut, outF1 = kOut, outF2 = kOut, outC = 0;
+    for (int t = 0; t < nsteps && abandon == 0; ++t) {
+      int upM = __shfl_up_sync(0xFFFFFFFFu, outM, 1);
+      int upF1 = __shfl_up_sync(0xFFFFFFFFu, outF1, 1);
+      int upF2 = __shfl_up_sync(0xFFFFFFFFu, outF2, 1);
+      int cj = __shfl_up_sync(0xFFFFFFFFu, outC, 1);
+      if ((t & 31) == 0 && t > 0) {
+        // chunk boundary: publish the columns of this stripe's last row written so far, stop early if the DP
+        // ended, stage the chunk two ahead of lane 0's reads
+        if (lane == 31 && produce) sg_st_release(prog_self, jstart + t - 32);
+        if (__any_sync(0xFFFFFFFFu, sg_ld_relaxed(&D.stop) != 0)) {
+          abandon = 1;
+          break;
+        }
+        __syncwarp();
+        stage_chunk((t >> 5) + 1);
+        if (abandon != 0) break;
+      }
+      const int j = jstart + t - lane;
+      if (lane == 0) {
+        const SgRec r = stage[warp][(t >> 5) & 1][t & 31];
+        upM = r.m, upF1 = r.f1, upF2 = r.f2;
+        cj = stage_c[warp][(t >> 5) & 1][t & 31];
+      }
+      int aF1 = upF1, aF2 = upF2, dg = diag;
+      uint32_t word = 0xFFFFFFFFu;
+#pragma unroll
+      for (int k = 0; k < kSgR; ++k) {
+        const int i = i0 + k;
+        int cM = kOut, cF1 = kOut, cF2 = kOut;
+        if (liver[k] && j >= c0[k] && j <= c1[k]) {
+          const int dgv = (j == 1) ? (i == 1 ? 0 : kOut) : dg;
+          const bool last = (j == c1[k]);
+          const int fin1 = last ? kOut : aF1, fin2 = last ? kOut : aF2;
+          int v = score_of(ci[k], cj, P.match, P.mismatch) + dgv;
+          int d = 0;
+          bool pr;
+          v = __vibmax_s32(fin1, v, &pr);  // pr: !(v > fin1)
+          d = pr ? 1 : d;
+          v = __vibmax_s32(e1[k], v, &pr);
+          d = pr ? 2 : d;
+          v = __vibmax_s32(fin2, v, &pr);
+          d = pr ? 3 : d;
+          v = __vibmax_s32(e2[k], v, &pr);
+          d = pr ? 4 : d;
+          cM = v;
+          if (v > best[k]) best[k] = v, bestj[k] = j;
+          if (j == n2 - 1) {
+            if (i == r_last) D.stale_last = v;
+            if (i == r_last - 1) D.stale_prev = v;
+          }
+          if (!last) {
+            const int h = v + o1, h2 = v + o2;
+            cF1 = __vibmax_s32(fin1 + x1, h, &pr);
+            d |= pr ? 8 : 0;
+            e1[k] = __vibmax_s32(e1[k] + x1, h, &pr);
+            d |= pr ? 16 : 0;
+            cF2 = __vibmax_s32(fin2 + x2, h2, &pr);
+            d |= pr ? 32 : 0;
+            e2[k] = __vibmax_s32(e2[k] + x2, h2, &pr);
+            d |= pr ? 64 : 0;
+            word = (word & ~(0xFFu << (8 * k))) | ((uint32_t)d << (8 * k));
+          }
+          if (k == kSgR - 1 && lane == 31 && produce) brow[j] = SgRec{cM, cF1, cF2};
+        }
+        dg = prevM[k];  // row k at column j - 1: the diagonal of row k + 1
+        prevM[k] = cM;
+        aF1 = cF1, aF2 = cF2;
+        if (k == kSgR - 1) outM = cM;
+      }
+      if (codes && live) trow[(int64_t)t * 32 + lane] = word;
+      diag = upM;
+      outF1 = aF1, outF2 = aF2, outC = cj;
+    }
+    __syncwarp();
+    if (lane == 31) sg_st_release(prog_self, INT_MAX);  // every column written (or abandoned): release the consumer
+    if (abandon < 0 && lane == 0) {
+      atomicExch(F.err, 1);
+      atomicExch(&D.stop, 1);
+      T.status = 4;
+    }
+    if (abandon != 0) continue;
+    // ---- the stripe's rows in order, from the DP's running state after stripe s - 1
+    if (s > 0) {
+      const int r = sg_wait_at_least(&D.evaluated, s, &D.stop, F.err);
+      if (r <= 0) {
+        if (r < 0 && lane == 0) {
+          atomicExch(F.err, 1);
+          atomicExch(&D.stop, 1);
+          T.status = 4;
+        }
+        continue;
+      }
+      if (__any_sync(0xFFFFFFFFu, sg_ld_relaxed(&D.stop) != 0)) continue;  // an earlier stripe ended the DP
+    }
+    int mx = 0, e1r = -1, e2r = -1, rows = 0;  // ends are 1-based and stay -1 while no cell is positive
+    if (s > 0) mx = sg_ld_relaxed(&D.mx), e1r = sg_ld_relaxed(&D.e1r), e2r = sg_ld_relaxed(&D.e2r),
+               rows = sg_ld_relaxed(&D.rows);
+    bool stop = false;
+    for (int ol = 0; ol < 32; ++ol) {  // row 128s + 1 + 4 ol + k is lane ol's row k
+#pragma unroll
+      for (int k = 0; k < kSgR; ++k) {
+        const int tm = __shfl_sync(0xFFFFFFFFu, best[k], ol), tj = __shfl_sync(0xFFFFFFFFu, bestj[k], ol);
+        const int ii = r0 + kSgR * ol + k;
+        if (!stop && ii <= n1_eff) {
+          if (tm > mx) mx = tm, e1r = ii, e2r = tj;
+          int l = (ii - e1r) - (tj - e2r);
+          l = l > 0 ? l : -l;
+          rows = ii;
+          if (mx - tm > P.zdrop + l * x2)
+            stop = true;
+          else if (tj <= 0)
+            stop = true;
+        }
+      }
+    }
+    if (lane == 0) {
+      if (!stop && s == nstripes - 1 && n1 > n1_eff && n2 >= 1) {
+        // empty-band rows: only the last column, from the stale column n2-1 of the row with the same parity
+        const int c2 = s2.at(ar, n2 - 1);
+        const int st_last = sg_ld_relaxed(&D.stale_last), st_prev = sg_ld_relaxed(&D.stale_prev);
+        for (int ii = n1_eff + 1; ii <= n1 && !stop; ++ii) {
+          const int dg = (n2 == 1) ? (int)kOut : (((ii - 1 - r_last) % 2 == 0) ? st_last : st_prev);
+          int v = score_of(s1.at(ar, ii - 1), c2, P.match, P.mismatch) + dg;
+          if (!(v > kOut)) v = kOut;
+          const int tm = v > 0 ? v : 0, tj = v > 0 ? n2 : 0;
+          if (tm > mx) mx = tm, e1r = ii, e2r = tj;
+          int l = (ii - e1r) - (tj - e2r);
+          l = l > 0 ? l : -l;
+          rows = ii;
+          if (mx - tm > P.zdrop + l * x2)
+            stop = true;
+          else if (tj <= 0)
+            stop = true;
+        }
+      }
+      if (stop || s == nstripes - 1) {
+        T.score = mx;
+        T.end1 = e1r;
+        T.end2 = e2r;
+        T.rows = rows;
+        T.status = 0;
+        if (stop) atomicExch(&D.stop, 1);
+      } else {
+        D.mx = mx, D.e1r = e1r, D.e2r = e2r, D.rows = rows;
+      }
+      __threadfence();
+      sg_st_release(&D.evaluated, s + 1);
+    }
+    __syncwarp();
+  }
+}
+
+int64_t sg_flow_units(int n1, int n2, int w) {
+  const int64_t n1_eff = (n1 <= 0 || n2 <= 0) ? 0 : std::min<int64_t>(n1, (int64_t)n2 + w);
+  return std::max<int64_t>(1, (n1_eff + kSgRows - 1) / kSgRows);
+}
+
+int sg_flow_blocks_per_sm() {
+  static int nb = 0;
+  if (nb == 0) {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, sg_flow_kernel, 32 * kSgFlowWarps, 0) != cudaSuccess) {
+      (void)cudaGetLastError();
+      v = 1;
+    }
+    nb = v > 0 ? v : 1;
+  }
+  return nb;
+}
+
+void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, int nsm, cudaStream_t st) {
+  if (f.total_units <= 0) return;
+  const int64_t warps = std::min<int64_t>(f.total_units, (int64_t)nsm * sg_flow_blocks_per_sm() * kSgFlowWarps);
+  sg_flow_kernel<<<(int)((warps + kSgFlowWarps - 1) / kSgFlowWarps), 32 * kSgFlowWarps, 0, st>>>(f, ar, p, tb);
 }
 
 // ------------------------------------------------------------------ traceback (:869-914)

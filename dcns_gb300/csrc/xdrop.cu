@@ -515,6 +515,11 @@ struct XLevelArgs {
   unsigned long long *tb_cursor;
   int64_t tb_words;
   int *fetch;  // passes of the level handed out so far (the row-interleaved kernel)
+  // hand-off of long register-band passes to the wavefront form (handoff_rows = 0: off): a pass still running after
+  // handoff_rows rows stores its band (M then F, spill_half ints each) in spill slot s and its id in long_list[s]
+  int *long_list, *long_count;
+  int32_t *spill;
+  int spill_cap, spill_half, handoff_rows;
 };
 
 __device__ __forceinline__ bool xd_take_slot(XTask &T, const XLevelArgs &L) {
@@ -554,41 +559,79 @@ __global__ void __launch_bounds__(128) xdrop_level_kernel(XLevelArgs L, Arena ar
 
 // The register-band level as a row-interleaved loop: every lane of a warp advances its own pass one row per
 // iteration and, when that pass ends, takes the level's next pass (warp-aggregated atomic on L.fetch), so the warp
-// keeps issuing full rows until the level's list runs out instead of idling until its longest pass ends.
+// keeps issuing full rows until the level's list runs out instead of idling until its longest pass ends.  The loop
+// is warp-uniform (every lane iterates until no lane has a pass or can take one), so the lanes with a pass run each
+// row together.  With L.handoff_rows > 0, a pass still running after that many rows (and more than a stripe from
+// the end of seq1) leaves its band state in a spill slot for the wavefront form (xdrop_level_resume_kernel), which
+// runs the rest of the pass 32 rows at a time: the level then no longer lasts as long as its longest pass on one
+// thread.  A pass that finds the spill slots full stays on its thread.
 template <int WC>
 __global__ void __launch_bounds__(128) xdrop_level_flat_kernel(XLevelArgs L, Arena ar, Params P,
                                                                uint32_t *__restrict__ tb) {
+  constexpr int NA = XBand<WC>::NA;
   const int n = *L.count_in;
   const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
   XPassScalars x;
-  int32_t Mr[XBand<WC>::NA], Fr[XBand<WC>::NA];
+  int32_t Mr[NA], Fr[NA];
   uint64_t qw[XBand<WC>::NQ];
   int id = -1;
+  bool more = true;                        // the level's list may still hold a pass for this lane
+  bool can_spill = L.handoff_rows > 0;
   for (;;) {
-    if (id < 0) {
-      const unsigned m = __activemask();
+    const bool need = id < 0 && more;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, need);
+    if (m != 0) {
       const int leader = __ffs(m) - 1;
       int base = 0;
       if (lane == leader) base = atomicAdd(L.fetch, __popc(m));
-      base = __shfl_sync(m, base, leader);
-      const int q = base + __popc(m & ((1u << lane) - 1u));
-      if (q >= n) break;
-      id = L.list_in[q];
-      XTask &T = L.tasks[id];
-      if (T.want_codes && !xd_take_slot(T, L)) {
-        T.status = 2;
-        L.retry[atomicAdd(L.retry_count, 1)] = id;
-        id = -1;
-        continue;
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (need) {
+        const int q = base + __popc(m & below);
+        if (q >= n) {
+          more = false;
+        } else {
+          id = L.list_in[q];
+          XTask &T = L.tasks[id];
+          if (T.want_codes && !xd_take_slot(T, L)) {
+            T.status = 2;
+            L.retry[atomicAdd(L.retry_count, 1)] = id;
+            id = -1;
+          } else {
+            xd_begin<WC>(x, Mr, Fr, qw, T, ar);
+          }
+        }
       }
-      xd_begin<WC>(x, Mr, Fr, qw, T, ar);
     }
-    const int st = xd_row_fused<WC>(x, Mr, Fr, qw, ar, P, tb);
-    if (st >= 0) {
-      XTask &T = L.tasks[id];
-      xd_finish(x, T, st);
-      xd_route(T, id, L);
-      id = -1;
+    if (!__any_sync(0xFFFFFFFFu, id >= 0 || more)) break;
+    if (id >= 0) {
+      const int st = xd_row_fused<WC>(x, Mr, Fr, qw, ar, P, tb);
+      if (st >= 0) {
+        XTask &T = L.tasks[id];
+        xd_finish(x, T, st);
+        xd_route(T, id, L);
+        id = -1;
+      } else if (can_spill && x.rows >= L.handoff_rows && x.n1 - x.rows > 32) {
+        const int s = atomicAdd(L.long_count, 1);
+        if (s < L.spill_cap) {
+          int32_t *sp = L.spill + (int64_t)s * 2 * L.spill_half;
+#pragma unroll
+          for (int k = 0; k < NA; ++k)
+            if (k <= x.nk) {
+              sp[k] = Mr[k];
+              sp[L.spill_half + k] = Fr[k];
+            }
+          XTask &T = L.tasks[id];
+          T.score = x.score;
+          T.end1 = x.e1;
+          T.end2 = x.e2;
+          T.rows = x.rows;
+          L.long_list[s] = id;
+          id = -1;
+        } else {
+          can_spill = false;
+        }
+      }
     }
   }
 }
@@ -635,18 +678,19 @@ __global__ void __launch_bounds__(128) xdrop_level_warp_kernel(XLevelArgs L, Are
 // A row costs (2w + 63) / 32 steps of one cell per lane: a long pass runs several times faster than on one thread.
 constexpr int kXwMaxW = 256;
 
+// The pass resumes at row r_begin: bM / bF hold row r_begin - 1 by band index (row 0: every cell kOut), and the
+// running maximum, its cell and the rows evaluated so far are (score, e1, e2, rows).
 __device__ void xdrop_wave_pass(XTask &T, const Arena &ar, const Params &P, uint32_t *__restrict__ tb,
                                 int32_t *__restrict__ bM, int32_t *__restrict__ bF, int64_t tb_off, int32_t tb_cap,
-                                int lane) {
+                                int lane, int r_begin, int score, int e1, int e2, int rows) {
   const int w = T.w, n1 = T.n1, n2 = T.n2, nk = 2 * w + 1, wpr = xd_words_per_row(w);
   const bool codes = T.want_codes != 0;
   const SeqView s1{T.base1, T.a1, T.dir}, s2{T.base2, T.a2, T.dir};
   const int open = P.open1, ext = P.ext1;
-  for (int k = lane; k <= nk; k += 32) bM[k] = kOut, bF[k] = kOut;  // row 0
   __syncwarp();
-  int score = 0, e1 = 0, e2 = 0, rows = 0, status = 0;
+  int status = 0;
   bool stop = false;
-  for (int r0 = 1; r0 <= n1 && !stop; r0 += 32) {
+  for (int r0 = r_begin; r0 <= n1 && !stop; r0 += 32) {
     const int i = r0 + lane;
     const bool live = i <= n1;
     const int c0 = max(i - w, 1), c1 = min(i + w, n2);
@@ -777,7 +821,33 @@ __global__ void __launch_bounds__(128) xdrop_level_wave_kernel(XLevelArgs L, Are
       }
       continue;
     }
-    xdrop_wave_pass(T, ar, P, tb, sM[wb], sF[wb], off, cap, lane);
+    for (int k = lane; k <= 2 * T.w + 1; k += 32) sM[wb][k] = kOut, sF[wb][k] = kOut;  // row 0
+    xdrop_wave_pass(T, ar, P, tb, sM[wb], sF[wb], off, cap, lane, 1, 0, 0, 0, 0);
+    __syncwarp();
+    if (lane == 0) xd_route(T, id, L);
+    __syncwarp();
+  }
+}
+
+// The passes the register-band level handed off (L.long_list), one warp per pass, resumed from their spilled band
+// and running state at the row after the last one their thread evaluated; routed like every other pass of the level.
+constexpr int kXrMaxW = 20;
+__global__ void __launch_bounds__(128) xdrop_level_resume_kernel(XLevelArgs L, Arena ar, Params P,
+                                                                 uint32_t *__restrict__ tb) {
+  __shared__ int32_t sM[4][2 * kXrMaxW + 2], sF[4][2 * kXrMaxW + 2];
+  const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  const int n = min(*L.long_count, L.spill_cap);
+  for (int q = gw; q < n; q += nw) {
+    const int id = L.long_list[q];
+    XTask &T = L.tasks[id];
+    const int32_t *sp = L.spill + (int64_t)q * 2 * L.spill_half;
+    const int nk = 2 * T.w + 1;
+    for (int k = lane; k <= nk; k += 32) sM[wb][k] = sp[k], sF[wb][k] = sp[L.spill_half + k];
+    const int64_t off = T.tb_off;
+    const int cap = T.tb_cap, score = T.score, e1 = T.end1, e2 = T.end2, rows = T.rows;
+    __syncwarp();
+    xdrop_wave_pass(T, ar, P, tb, sM[wb], sF[wb], off, cap, lane, rows + 1, score, e1, e2, rows);
     __syncwarp();
     if (lane == 0) xd_route(T, id, L);
     __syncwarp();
@@ -790,11 +860,28 @@ __global__ void xdrop_iota_kernel(int *list, int n, int *count) {
   if (k == 0) *count = n;
 }
 
+// Whole passes on the wavefront form, one warp per pass (w <= 256), with the traceback slot the host assigned
+// (T.tb_off, T.tb_cap): the form for passes known to be long, such as those that outgrew their slot in the levels.
+__global__ void __launch_bounds__(128) xdrop_wave_kernel(XTask *__restrict__ tasks, const int *__restrict__ idx, int n,
+                                                         Arena ar, Params P, uint32_t *__restrict__ tb) {
+  __shared__ int32_t sM[4][2 * kXwMaxW + 2], sF[4][2 * kXwMaxW + 2];
+  const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (gw >= n) return;  // whole warp
+  XTask &T = tasks[idx[gw]];
+  const int64_t off = T.tb_off;
+  const int cap = T.tb_cap;
+  for (int k = lane; k <= 2 * T.w + 1; k += 32) sM[wb][k] = kOut, sF[wb][k] = kOut;  // row 0
+  xdrop_wave_pass(T, ar, P, tb, sM[wb], sF[wb], off, cap, lane, 1, 0, 0, 0, 0);
+}
+
 void launch_xdrop(XTask *tasks, const int *idx, int n, Arena ar, Params p, uint32_t *tb, int wcap, int32_t *scratch,
                   int64_t scratch_per_thread, cudaStream_t st) {
   if (n <= 0) return;
   const int g = (n + 127) / 128;
-  if (wcap == 10)
+  if (wcap < 0)  // long passes: wavefront, one warp each
+    xdrop_wave_kernel<<<(n + 3) / 4, 128, 0, st>>>(tasks, idx, n, ar, p, tb);
+  else if (wcap == 10)
     xdrop_kernel<10><<<g, 128, 0, st>>>(tasks, idx, n, ar, p, tb, scratch, 0);
   else if (wcap == 20)
     xdrop_kernel<20><<<g, 128, 0, st>>>(tasks, idx, n, ar, p, tb, scratch, 0);
@@ -820,21 +907,29 @@ int flat_blocks_per_sm() {
   return nb;
 }
 
-void launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
-                        int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int *fetch,
-                        Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm, int32_t *scratch,
-                        int64_t per_warp, int warps, int warp_from, int wave_max_w, bool flat, cudaStream_t st) {
-  if (n_bound <= 0) return;
-  const XLevelArgs L{tasks, list_in, count_in, list_out, count_out, retry, retry_count, tb_cursor, tb_words, fetch};
+int launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
+                       int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int *fetch,
+                       const XHandoff &H, Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm,
+                       int32_t *scratch, int64_t per_warp, int warps, int warp_from, int wave_max_w, bool flat,
+                       cudaStream_t st) {
+  if (n_bound <= 0) return 0;
+  const bool flat_level = flat && w <= warp_from && w <= kXrMaxW;
+  const bool handoff = flat_level && H.rows > 0 && H.cap > 0;
+  XLevelArgs L{tasks, list_in, count_in, list_out, count_out, retry, retry_count, tb_cursor, tb_words, fetch,
+               H.list, H.count, H.spill, handoff ? H.cap : 0, w <= 10 ? XBand<10>::NA : XBand<20>::NA,
+               handoff ? H.rows : 0};
   const int g = (int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * 16);
-  if (flat && w <= warp_from && w <= 20) {  // register band, row-interleaved: one resident wave of blocks
+  if (flat_level) {  // register band, row-interleaved: one resident wave of blocks, then the handed-off passes
     if (w <= 10)
       xdrop_level_flat_kernel<10><<<(int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * flat_blocks_per_sm<10>()),
                                     128, 0, st>>>(L, ar, p, tb);
     else
       xdrop_level_flat_kernel<20><<<(int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * flat_blocks_per_sm<20>()),
                                     128, 0, st>>>(L, ar, p, tb);
-    return;
+    if (!handoff) return 1;
+    xdrop_level_resume_kernel<<<(int)std::min<int64_t>((H.cap + 3) / 4, (int64_t)nsm * 16), 128, 0, st>>>(L, ar, p,
+                                                                                                         tb);
+    return 2;
   }
   if (w > warp_from && w <= wave_max_w && w <= kXwMaxW)  // wide bands up to 256: the wavefront
     xdrop_level_wave_kernel<<<(int)std::min<int64_t>((n_bound + 3) / 4, (int64_t)nsm * 16), 128, 0, st>>>(L, ar, p,
@@ -847,6 +942,7 @@ void launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, i
     xdrop_level_kernel<20><<<g, 128, 0, st>>>(L, ar, p, tb);
   else
     xdrop_level_warp_kernel<<<(warps + 3) / 4, 128, 0, st>>>(L, ar, p, tb, scratch, per_warp);
+  return 1;
 }
 
 // ------------------------------------------------------------------ traceback of the reverse pass

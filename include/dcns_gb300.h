@@ -93,6 +93,7 @@ typedef struct {
   double ms_sg_tb_kernel;     /* device: semi-global traceback kernels, CUDA events */
   int64_t bytes_codes_xdrop;  /* direction codes of the final-width x-drop passes that kept them: 4 bits per band cell */
   int64_t bytes_codes_sg;     /* direction codes of the semi-global DPs that kept them: 1 byte per band cell */
+  int64_t bytes_device;       /* device memory the context's buffers hold after the call (they are kept for reuse) */
 } dcns_stats;
 
 /* Results of one dcns_align_pairs call; owned by the library until dcns_results_free. */
@@ -183,14 +184,15 @@ int dcns_autotune(dcns_ctx *ctx, dcns_batch *batch, const dcns_params *params, i
 
 /* The context's kernel shapes (no counterpart in the reference): what dcns_autotune chose, or the defaults and the
  * DCNS_* environment settings.  Per bin (at most 16 reported): the x-drop band from which passes run one warp each,
- * the widest band of the one-warp wavefront form, and whether the register-band levels run row-interleaved. */
+ * the widest band of the one-warp wavefront form, whether the register-band levels run row-interleaved, and the rows
+ * after which a register-band pass moves to the wavefront form (0: never). */
 typedef struct {
   int32_t lanes, bins;
   double bin_ratio;
   int32_t scan_tiles_per_thread;  /* seed-scan tiling target: rows split into chunks below this many tiles per thread */
   int32_t sg_warps;               /* warps per 2-piece DP (0: two for launches of many DPs, else eight) */
   int32_t n_bins_tuned;           /* bins with their own x-drop forms below (0: every bin uses bin 0's values) */
-  int32_t xdrop_warp_from[16], xdrop_wave_max_w[16], xdrop_flat[16];
+  int32_t xdrop_warp_from[16], xdrop_wave_max_w[16], xdrop_flat[16], xdrop_handoff[16];
 } dcns_tuning;
 int dcns_get_tuning(const dcns_ctx *ctx, dcns_tuning *out);
 
