@@ -13,8 +13,9 @@ Reported (one JSON line, rank 0):
   cpu_baseline  the oracle restatement of the reference over all host cores on a fixed sample of the workload (every
           k-th pair, 64 per thread)
   per_pair_launch, serving  the one-pair-per-call form and the continuous-batching loop (p50/p99) for comparison
-  two_gap, long_pairs, extension_seeds  the other benchmark configurations (the cut2Gaps path, whole 200 kb pairs,
-          1,000,000 extension seeds), each with its kernel figures, its own CPU baseline and clock record
+  two_gap, long_pairs, seeded_chromosome, extension_seeds  the other benchmark configurations (the cut2Gaps path,
+          whole 200 kb pairs, cut2Gaps2's seeded overload on a whole 200 kb pair with no length cap, 1,000,000
+          extension seeds), each with its kernel figures, its own CPU baseline and clock record
 
 `--impl reference` times the reference's CPU implementation of the path instead (the oracle restatement, since the
 reference sources are not present on the GPU host), with every host core, each step one pass over the same fixed
@@ -280,6 +281,62 @@ def line_long_pairs(eng, timed, threads, gpu, scan_peak, n=8, steps=2, cpu_query
             "clocks": clk.summary()}
 
 
+def line_seeded_chromosome(eng, timed, threads, gpu, steps=3, n_seeds=16, cpu_seeds=None, cpu_len=20000):
+    """cut2Gaps2's seeded 2-gap overload at chromosome scale: one whole 200 kb x ~234 kb pair of the long-pair workload
+    with maximumAlignLength unlimited (the reference's driver caps it at 140 kb for its dense traceback matrix).  The
+    x-seeds are the pair's first n_seeds cut1Gap fragments (as cut2Gaps2 reads them from a SAM file of earlier
+    alignments).  C ABI call on host buffers (upload and result download in every step); the 2-piece kernels'
+    GCUPS, and the device memory the call's buffers hold.  The CPU baseline runs the oracle port on a sample of the
+    pair's leading part (a whole-pair seed takes minutes on one core), one seed per thread."""
+    from concurrent.futures import ThreadPoolExecutor
+    from dcns_gb300 import workloads as W
+    a, b = W.long_pairs_200kb(n_pairs=1)[0]
+    frs = eng.align_pairs([(a, b)], 1)[0][:n_seeds]
+    seeds = [(f.start1 - 1, f.end1 - 1, f.start2 - 1, f.end2 - 1) for f in frs]
+    eng.align_seeded([(a, b)], [seeds], max_align_len=0)
+    tot_ms, cells, sg_ms, tb_ms, nfrag, dev = 0.0, 0, 0.0, 0.0, 0, 0
+    with ClockSampler(gpu) as clk:
+        for _ in range(steps):
+            res, t = timed(lambda: eng.align_seeded([(a, b)], [seeds], max_align_len=0))
+            st = eng.last_stats()
+            tot_ms += t
+            cells += st["cells_semiglobal"]
+            sg_ms += st["ms_sg_kernel"]
+            tb_ms += st["ms_sg_tb_kernel"]
+            nfrag = len(res[0])
+            dev = max(dev, st["bytes_device"])
+    # CPU: the same kind of call on the pair's first cpu_len bases of each sequence (a whole-pair seed takes about two
+    # minutes of one core), one x-seed per thread, cells counted by the oracle
+    from oracle import oracle as O
+    O.build()
+    ca, cb = a[:cpu_len], b[:int(cpu_len * len(b) / len(a))]
+    sample = [s for s in seeds if s[1] < len(ca) - 1 and s[3] < len(cb) - 1][:cpu_seeds or threads]
+    orc = O.Oracle()
+
+    def one(sd):
+        return orc.find_seeded(ca, cb, [sd], 1 << 30, with_cells=True)[1]["semiglobal"]
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max(1, len(sample))) as ex:
+        cpu_cells = sum(ex.map(one, sample))
+    dt = time.perf_counter() - t0
+    return {"workload": f"cut2Gaps2 seeded overload: one whole 200 kb x {len(b) // 1000} kb pair, {len(seeds)} x-seeds "
+                        f"(its first cut1Gap fragments), maximumAlignLength unlimited",
+            "value": round(cells / (tot_ms * 1e-3) / 1e9, 3), "unit": "GCUPS", "steps": steps,
+            "ms_per_step": round(tot_ms / steps, 2), "fragments": nfrag,
+            "sg_kernel": {"ms_per_step": round(sg_ms / steps, 2), "gcups": round(cells / (sg_ms * 1e-3) / 1e9, 2),
+                          "traceback_ms_per_step": round(tb_ms / steps, 2)},
+            "device_bytes": int(dev),
+            "device_memory_note": "device buffers the call holds (sequences, DP codes of one DP per seed at 1 byte "
+                                  "per band cell, boundary rows); the reference's dense traceback matrix for this "
+                                  f"pair would be {(len(a) + 1) * (len(b) + 1) / 1e9:.0f} GB",
+            "cpu_baseline": {"value": cpu_cells / dt / 1e9, "unit": "GCUPS", "cores": len(sample), "kind": "port",
+                             "seconds": dt,
+                             "sample": f"the same call on the pair's first {len(ca):,} x {len(cb):,} bases, its first "
+                                       f"{len(sample)} x-seeds there, one per thread"},
+            "clocks": clk.summary()}
+
+
 def _seed_chunk(c):
     from dcns_gb300 import workloads as W
     return W.extension_seeds(n_seeds=10000, seed=20261207 + c)
@@ -525,6 +582,7 @@ def main():
         threads = host_threads()
         extras["two_gap"] = line_two_gap(eng, timed, pairs, threads, local)
         extras["long_pairs"] = line_long_pairs(eng, timed, threads, local, peak)
+        extras["seeded_chromosome"] = line_seeded_chromosome(eng, timed, threads, local)
         extras["extension_seeds"] = line_extension_seeds(eng, args.ext_seeds, threads, local)
 
     threads = host_threads()

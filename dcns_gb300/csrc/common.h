@@ -184,7 +184,9 @@ void launch_reverse(ScanTask *tasks, int first, int n, const unsigned long long 
 // pass as a wavefront, w <= 256: for long passes)
 void launch_xdrop(XTask *tasks, const int *idx, int n, Arena ar, Params p, uint32_t *tb, int wcap, int32_t *scratch,
                   int64_t scratch_per_thread, cudaStream_t st);
-void launch_xdrop_traceback(XTask *tasks, const int *idx, int n, const uint32_t *tb, uint32_t *cig, cudaStream_t st);
+// tb_words: size of the band store tb (the traceback reads nothing past it)
+void launch_xdrop_traceback(XTask *tasks, const int *idx, int n, const uint32_t *tb, int64_t tb_words, uint32_t *cig,
+                            cudaStream_t st);
 // Chained x-drop levels (one launch per band width, work lists and counts in device memory).
 void launch_xdrop_iota(int *list, int n, int *count, cudaStream_t st);
 // Hand-off of long register-band passes to the wavefront form: a pass of a row-interleaved level still running after
@@ -203,7 +205,7 @@ int launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, in
                        const XHandoff &H, Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm,
                        int32_t *scratch, int64_t per_warp, int warps, int warp_from, int wave_max_w, bool flat,
                        cudaStream_t st);
-void launch_xdrop_traceback_all(XTask *tasks, int n, const uint32_t *tb, uint32_t *cig,
+void launch_xdrop_traceback_all(XTask *tasks, int n, const uint32_t *tb, int64_t tb_words, uint32_t *cig,
                                 unsigned long long *cig_cursor, cudaStream_t st);
 // Packs the CIGARs of every finished task in task order into dense (cig_dense offsets); *total = their words.
 void launch_xdrop_cigar_pack(XTask *tasks, int n, const uint32_t *cig, uint32_t *dense, unsigned long long *total,
@@ -212,11 +214,13 @@ void launch_xdrop_cigar_pack(XTask *tasks, int n, const uint32_t *cig, uint32_t 
 void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p, uint8_t *tb, void *bnd,
                        int max_n2, int *work_counter, int grid, int nw, cudaStream_t st);
 int sg_ctas_per_sm(int nw);
-void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, int nsm, cudaStream_t st);
+// codes: the DPs keep direction codes (every DP of a launch alike)
+void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, bool codes, int nsm, cudaStream_t st);
 int64_t sg_flow_units(int n1, int n2, int w);  // stripe units of one DP in the flow form (at least 1)
 int64_t sg_bnd_bytes(int grid, int max_n2, int nw);
-void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, uint32_t *cig,
-                         cudaStream_t st, bool weighted_layout = false);
+// tb_bytes: size of the code store tb (the traceback reads nothing past it)
+void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, int64_t tb_bytes,
+                         uint32_t *cig, cudaStream_t st, bool weighted_layout = false);
 int64_t sg_tb_bytes(int n1, int n2, int w);
 int64_t sgw_tb_bytes(int n1, int n2, int w);
 int64_t sgw_bnd_bytes(int warps, int max_n2);

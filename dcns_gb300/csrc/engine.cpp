@@ -1128,7 +1128,7 @@ void run_xdrop_rounds(Context &C, std::vector<XTask> &X, const Params &P, bool w
       h2d(C, C.d_x, Xc, (size_t)m);
       h2d(C, C.d_idx, fin_c.data(), fin_c.size());
       DCNS_CK(cudaEventRecord(C.ev1, C.st));
-      launch_xdrop_traceback(C.d_x.as<XTask>(), C.d_idx.as<int>(), (int)fin_c.size(), C.d_tb.as<uint32_t>(),
+      launch_xdrop_traceback(C.d_x.as<XTask>(), C.d_idx.as<int>(), (int)fin_c.size(), C.d_tb.as<uint32_t>(), words,
                              C.d_cig.as<uint32_t>(), C.st);
       DCNS_CK(cudaEventRecord(C.ev2, C.st));
       C.stats.kernel_launches += 1;
@@ -1251,8 +1251,8 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
     }
     DCNS_CK(cudaEventRecord(C.ev1, C.st));
     if (want_codes) {
-      launch_xdrop_traceback_all(C.d_x.as<XTask>(), (int)n, C.d_tb.as<uint32_t>(), C.d_cig.as<uint32_t>(), cur + 1,
-                                 C.st);
+      launch_xdrop_traceback_all(C.d_x.as<XTask>(), (int)n, C.d_tb.as<uint32_t>(), tb_words, C.d_cig.as<uint32_t>(),
+                                 cur + 1, C.st);
       launch_xdrop_cigar_pack(C.d_x.as<XTask>(), (int)n, C.d_cig.as<uint32_t>(), C.d_cig.as<uint32_t>() + cig_words,
                               cur + 1, C.st);
       DCNS_CK(cudaEventRecord(C.ev2, C.st));
@@ -1452,10 +1452,9 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
     }
     const int64_t m = k1 - k0;
     if (want_codes) C.d_sgtb.ensure(C, (size_t)std::max<int64_t>(bytes, 1));
-    // unweighted: one 8-warp CTA per DP; weighted: one warp per DP, 16 warps per SM.  (One warp per DP measured
-    // 8.6x slower than the CTA pipeline on the unweighted 2-gap DPs of 2,000 log-normal pairs: 2819 vs 328 ms.)
-    // CTA shape of the unweighted kernel: many DPs run two warps each (short DPs stop within a few stripes, and more
-    // of them run at once); few DPs keep eight warps each for the stripes of long DPs
+    // unweighted: the stripe flow (or, with sg_flow off, one CTA per DP); weighted: one warp per DP, 16 warps per SM.
+    // CTA shape of the unweighted CTA kernel: many DPs run two warps each (short DPs stop within a few stripes, and
+    // more of them run at once); few DPs keep eight warps each for the stripes of long DPs
     const int nw = C.sg_warps > 0 ? C.sg_warps : (m >= (int64_t)C.nsm * 8 ? 2 : kSgNW);
     const int grid = (int)std::min<int64_t>(m, W ? (int64_t)C.nsm * 16 : (int64_t)C.nsm * sg_ctas_per_sm(nw));
     int maxn2 = 1;
@@ -1513,7 +1512,7 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
       launch_semiglobal_weighted(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, *W,
                                  C.d_sgtb.as<uint8_t>(), C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, C.st);
     else if (flow)
-      launch_semiglobal_flow(F, C.arena, P, C.d_sgtb.as<uint8_t>(), C.nsm, C.st);
+      launch_semiglobal_flow(F, C.arena, P, C.d_sgtb.as<uint8_t>(), want_codes, C.nsm, C.st);
     else
       launch_semiglobal(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, C.d_sgtb.as<uint8_t>(),
                         C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, nw, C.st);
@@ -1544,7 +1543,7 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
       C.d_cig.ensure(C, sizeof(uint32_t) * std::max<int64_t>(cw, 1));
       h2d(C, C.d_sg, G.data(), (size_t)n);
       DCNS_CK(cudaEventRecord(C.ev0, C.st));
-      launch_sg_traceback(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, P.bandwidth, C.d_sgtb.as<uint8_t>(),
+      launch_sg_traceback(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, P.bandwidth, C.d_sgtb.as<uint8_t>(), bytes,
                           C.d_cig.as<uint32_t>(), C.st, W != nullptr);
       DCNS_CK(cudaEventRecord(C.ev1, C.st));
       C.stats.kernel_launches += 1;
@@ -2084,14 +2083,17 @@ void autotune(Context &C, Batch &B, const Params &P, int mode) {
     C.scan_tiles_per_thread = best_t;
   }
   if (mode == DCNS_MODE_TWO_GAP) {
-    int best_w = 0;
+    // the stripe flow (-1 below), or one CTA per DP with 2, 4 or 8 warps (0: by the number of DPs)
+    int best_w = -1;
     double best_w_ms = 1e300;
-    for (int nw : {0, 2, 4, kSgNW}) {
-      C.sg_warps = nw;
+    for (int nw : {-1, 0, 2, 4, kSgNW}) {
+      C.sg_flow = nw < 0;
+      C.sg_warps = std::max(nw, 0);
       const double ms = std::min(run(best), run(best));
       if (ms < best_w_ms) best_w_ms = ms, best_w = nw;
     }
-    C.sg_warps = best_w;
+    C.sg_flow = best_w < 0;
+    C.sg_warps = std::max(best_w, 0);
   }
 }
 
@@ -2202,6 +2204,7 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
         L.xdrop_warp_from = bt.xdrop_warp_from, L.xdrop_wave_max_w = bt.xdrop_wave_max_w, L.xdrop_flat = bt.xdrop_flat;
         L.xdrop_handoff = bt.xdrop_handoff;
         L.sg_warps = C.sg_warps;
+        L.sg_flow = C.sg_flow;
         L.scan_tiles_per_thread = C.scan_tiles_per_thread;
         L.call_t0 = C.call_t0;
         L.lane_id = l;

@@ -1,15 +1,19 @@
 // Two-piece affine semi-global DP with z-drop and band (SemiGlobal_no_avx, impl/sequenceAlignment3.cpp:681-928)
 // and its traceback.
 //
-// One CTA of 8 warps runs one DP.  Rows are processed in stripes of 128: lane l owns the four consecutive rows
-// 128s+1+4l .. 128s+4+4l, stripe s on warp s mod 8, each as an anti-diagonal wavefront: at step t lane l computes
-// column j = jstart + t - l for its four rows top to bottom, receiving the cell above its first row (M, both
-// vertical-gap states, and the query code) from lane l-1 through __shfl_up_sync; rows inside a lane pass the cell
-// above in registers.  Lane 0 takes the row above the stripe from the previous stripe, written to global scratch at
-// least one CTA barrier earlier and staged into shared memory (with the query codes) 32-63 steps ahead of use, so
-// consecutive stripes run concurrently on different warps.  The horizontal gap states stay in registers of the lane
-// that owns the row.  Each cell's priority chain (diag > F1 > E1 > F2 > E2, strict) and gap updates use the DPX
-// max-with-predicate instruction, which yields the maximum and the reference's comparison bit at once.
+// Rows are processed in stripes of 128: lane l owns the four consecutive rows 128s+1+4l .. 128s+4+4l of stripe s as
+// an anti-diagonal wavefront: at step t lane l computes column j = jstart + t - l for its four rows top to bottom,
+// receiving the cell above its first row (M, both vertical-gap states, and the query code) from lane l-1 through
+// __shfl_up_sync; rows inside a lane pass the cell above in registers.  Lane 0 takes the row above the stripe from
+// the stripe before, through a boundary row in global memory staged into shared memory (with the query codes) 32-63
+// steps ahead of use.  The horizontal gap states stay in registers of the lane that owns the row.  Each cell's
+// priority chain (diag > F1 > E1 > F2 > E2) and gap updates use the DPX max-with-predicate instruction, which yields
+// the maximum and the reference's comparison bit at once.
+//
+// Two schedules of the stripes.  The batched path runs every stripe of every DP as an independent unit of one
+// persistent grid (sg_flow_kernel: a long DP spreads over as many warps as it has stripes).  The one-pair entry point
+// without allocation keeps a whole DP on one CTA whose warps take its stripes in turn on a barrier schedule
+// (sg_kernel), which needs only one CTA's boundary rows.
 //
 // Direction codes are one byte per cell (state 0..4 in bits 0-2, gap-continuation flags in bits 3-6): the reference's
 // traceback needs all seven bits to stay bit-exact.  Layout: stripe-major, then step, then lane, one 32-bit word per
@@ -368,6 +372,51 @@ __device__ __forceinline__ int sg_wait_at_least(const int *flag, int need, const
 
 constexpr int kSgFlowWarps = 4;  // warps per block of the flow kernel
 
+// One cell of a flow stripe, branch-free: (aF1, aF2) = the vertical gap states of the cell above (kOut at the row's
+// last band column, which no row above has in its band or updates), dg = the diagonal cell.  Cells outside the band
+// leave kOut in M and both F, and reset the row's horizontal states to kOut (the reference starts a row with them
+// OUT); the band's last column takes the cell's maximum but leaves kOut in both F (its gap states are not updated,
+// and the row's horizontal states are not read again).  With CODES, *d gets the cell's direction code: the winning
+// state (priority order diag, F1, E1, F2, E2, a later state winning ties) and the four gap-continuation flags;
+// codes of cells outside the band or on its last column are never read by the traceback.
+template <bool CODES>
+__device__ __forceinline__ int sg_cell(int sc, int dg, int aF1, int aF2, int &e1, int &e2, bool valid, bool last,
+                                       int o1, int x1, int o2, int x2, int &cF1, int &cF2, uint32_t *d) {
+  int v = sc + dg, nF1, nF2, nE1, nE2;
+  if (CODES) {
+    bool pr;
+    uint32_t c = 0;
+    v = __vibmax_s32(aF1, v, &pr);  // pr: !(v > F1)
+    c = pr ? 1u : c;
+    v = __vibmax_s32(e1, v, &pr);
+    c = pr ? 2u : c;
+    v = __vibmax_s32(aF2, v, &pr);
+    c = pr ? 3u : c;
+    v = __vibmax_s32(e2, v, &pr);
+    c = pr ? 4u : c;
+    const int h = v + o1, h2 = v + o2;
+    bool p1, p2, p3, p4;
+    nF1 = __vibmax_s32(aF1 + x1, h, &p1);
+    nE1 = __vibmax_s32(e1 + x1, h, &p2);
+    nF2 = __vibmax_s32(aF2 + x2, h2, &p3);
+    nE2 = __vibmax_s32(e2 + x2, h2, &p4);
+    *d = c | (p1 ? 8u : 0u) | (p2 ? 16u : 0u) | (p3 ? 32u : 0u) | (p4 ? 64u : 0u);
+  } else {
+    v = __vimax3_s32(__vimax3_s32(v, aF1, e1), aF2, e2);
+    nF1 = __viaddmax_s32(aF1, x1, v + o1);
+    nE1 = __viaddmax_s32(e1, x1, v + o1);
+    nF2 = __viaddmax_s32(aF2, x2, v + o2);
+    nE2 = __viaddmax_s32(e2, x2, v + o2);
+  }
+  const bool upd = valid && !last;
+  cF1 = upd ? nF1 : kOut;
+  cF2 = upd ? nF2 : kOut;
+  e1 = valid ? nE1 : kOut;
+  e2 = valid ? nE2 : kOut;
+  return valid ? v : kOut;
+}
+
+template <bool CODES>
 __global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Arena ar, Params P,
                                                                    uint8_t *__restrict__ tb) {
   __shared__ SgRec stage[kSgFlowWarps][2][32];
@@ -402,22 +451,25 @@ __global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Ar
       continue;
     }
     const SeqView s1{T.base1, T.a1, T.dir}, s2{T.base2, T.a2, T.dir};
-    const bool codes = T.want_codes != 0;
     const int r_last = n2 - 1 + w;
     const int64_t stride = sg_stride_steps(n2, w);
     SgRec *const brow = F.bnd + D.bnd_off;  // the DP's boundary row, by column
     const int *const prog_up = s > 0 ? F.prog + (u - 1) : nullptr;
     const int i0 = kSgRows * s + 1 + kSgR * lane;
     const bool live = i0 <= n1_eff;
-    int ci[kSgR], c0[kSgR], c1[kSgR], e1[kSgR], e2[kSgR], best[kSgR], bestj[kSgR], prevM[kSgR];
-    bool liver[kSgR];
+    // per row of the lane: band [c0, c0 + span] (rows past the DP: an empty band), its base, the stale-column role,
+    // running states
+    int ci[kSgR], c0[kSgR], span[kSgR], e1[kSgR], e2[kSgR], best[kSgR], bestj[kSgR], prevM[kSgR];
+    int stale_rows = 0;  // bit k: row k is row r_last (bit 4 + k: row r_last - 1)
 #pragma unroll
     for (int k = 0; k < kSgR; ++k) {
       const int i = i0 + k;
-      liver[k] = i <= n1_eff;
-      c0[k] = max(i - w, 1);
-      c1[k] = min(i + w, n2);
-      ci[k] = liver[k] ? s1.at(ar, i - 1) : 0;
+      const bool lv = i <= n1_eff;
+      c0[k] = lv ? max(i - w, 1) : INT_MAX / 2;
+      span[k] = lv ? min(i + w, n2) - c0[k] : 0;
+      ci[k] = lv ? s1.at(ar, i - 1) : 0;
+      if (lv && i == r_last) stale_rows |= 1 << k;
+      if (lv && i == r_last - 1) stale_rows |= 16 << k;
       e1[k] = kOut, e2[k] = kOut, best[k] = 0, bestj[k] = 0, prevM[k] = kOut;
     }
     const int r0 = kSgRows * s + 1, rl = min(kSgRows * s + kSgRows, n1_eff);
@@ -425,7 +477,7 @@ __global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Ar
     const int nsteps = min(rl + w, n2) - jstart + 1 + 31;
     const int upB = min(kSgRows * s + w, n2);  // the row above (128s) holds columns [max(128s - w, 1), upB]
     const bool produce = s + 1 < nstripes;
-    uint32_t *const trow = reinterpret_cast<uint32_t *>(tb + T.tb_off) + (int64_t)s * stride * 32;
+    uint32_t *const trow = CODES ? reinterpret_cast<uint32_t *>(tb + T.tb_off) + (int64_t)s * stride * 32 : nullptr;
     int abandon = 0;  // 0 computing, 1 the DP stopped, -1 a wait ran out
     // columns jstart + 32 * chunk + lane of the row above, into stage[warp][chunk & 1]; the producer must have
     // published them first
@@ -446,7 +498,10 @@ __global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Ar
       stage_c[warp][chunk & 1][lane] = (j >= 1 && j <= n2) ? s2.at(ar, j - 1) : 0;
     };
     stage_chunk(0);  // waits for columns up to jstart + 31, which include the diagonal column jstart - 1
-    int diag = (lane == 0 && s > 0 && jstart > 1 && abandon == 0) ? __ldcg(&brow[jstart - 1].m) : kOut;
+    // the diagonal of the stripe's first row at column jstart: cell (0, 0) = 0 for the DP's first row, else the
+    // row above at jstart - 1 (kOut at column 0)
+    int diag = kOut;
+    if (lane == 0) diag = s == 0 ? 0 : (jstart > 1 && abandon == 0) ? __ldcg(&brow[jstart - 1].m) : kOut;
     stage_chunk(1);
     __syncwarp();
     int outM = kOut, outF1 = kOut, outF2 = kOut, outC = 0;
@@ -474,52 +529,32 @@ __global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Ar
         cj = stage_c[warp][(t >> 5) & 1][t & 31];
       }
       int aF1 = upF1, aF2 = upF2, dg = diag;
-      uint32_t word = 0xFFFFFFFFu;
+      uint32_t word = 0;
+      const int mt = cj == 2 ? 0 : P.match, mm = cj == 2 ? 0 : P.mismatch;  // Scorei: N scores 0
 #pragma unroll
       for (int k = 0; k < kSgR; ++k) {
-        const int i = i0 + k;
-        int cM = kOut, cF1 = kOut, cF2 = kOut;
-        if (liver[k] && j >= c0[k] && j <= c1[k]) {
-          const int dgv = (j == 1) ? (i == 1 ? 0 : kOut) : dg;
-          const bool last = (j == c1[k]);
-          const int fin1 = last ? kOut : aF1, fin2 = last ? kOut : aF2;
-          int v = score_of(ci[k], cj, P.match, P.mismatch) + dgv;
-          int d = 0;
-          bool pr;
-          v = __vibmax_s32(fin1, v, &pr);  // pr: !(v > fin1)
-          d = pr ? 1 : d;
-          v = __vibmax_s32(e1[k], v, &pr);
-          d = pr ? 2 : d;
-          v = __vibmax_s32(fin2, v, &pr);
-          d = pr ? 3 : d;
-          v = __vibmax_s32(e2[k], v, &pr);
-          d = pr ? 4 : d;
-          cM = v;
-          if (v > best[k]) best[k] = v, bestj[k] = j;
-          if (j == n2 - 1) {
-            if (i == r_last) D.stale_last = v;
-            if (i == r_last - 1) D.stale_prev = v;
-          }
-          if (!last) {
-            const int h = v + o1, h2 = v + o2;
-            cF1 = __vibmax_s32(fin1 + x1, h, &pr);
-            d |= pr ? 8 : 0;
-            e1[k] = __vibmax_s32(e1[k] + x1, h, &pr);
-            d |= pr ? 16 : 0;
-            cF2 = __vibmax_s32(fin2 + x2, h2, &pr);
-            d |= pr ? 32 : 0;
-            e2[k] = __vibmax_s32(e2[k] + x2, h2, &pr);
-            d |= pr ? 64 : 0;
-            word = (word & ~(0xFFu << (8 * k))) | ((uint32_t)d << (8 * k));
-          }
-          if (k == kSgR - 1 && lane == 31 && produce) brow[j] = SgRec{cM, cF1, cF2};
+        const int dj = j - c0[k];
+        const bool valid = (unsigned)dj <= (unsigned)span[k];
+        const bool last = dj == span[k];
+        const int sc = ci[k] == 2 ? 0 : (ci[k] == cj ? mt : mm);
+        int cF1, cF2;
+        uint32_t d = 0;
+        const int cM = sg_cell<CODES>(sc, dg, aF1, aF2, e1[k], e2[k], valid, last, o1, x1, o2, x2, cF1, cF2, &d);
+        if (CODES) word |= d << (8 * k);
+        bool keep;
+        best[k] = __vibmax_s32(best[k], cM, &keep);  // keep: !(cM > best), the first maximum of the row stays
+        bestj[k] = keep ? bestj[k] : j;
+        if (stale_rows && j == n2 - 1 && valid) {
+          if ((stale_rows >> k) & 1) D.stale_last = cM;
+          if ((stale_rows >> (4 + k)) & 1) D.stale_prev = cM;
         }
+        if (k == kSgR - 1 && lane == 31 && produce && valid) brow[j] = SgRec{cM, cF1, cF2};
         dg = prevM[k];  // row k at column j - 1: the diagonal of row k + 1
         prevM[k] = cM;
         aF1 = cF1, aF2 = cF2;
         if (k == kSgR - 1) outM = cM;
       }
-      if (codes && live) trow[(int64_t)t * 32 + lane] = word;
+      if (CODES && live) trow[(int64_t)t * 32 + lane] = word;
       diag = upM;
       outF1 = aF1, outF2 = aF2, outC = cj;
     }
@@ -611,7 +646,7 @@ int sg_flow_blocks_per_sm() {
   static int nb = 0;
   if (nb == 0) {
     int v = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, sg_flow_kernel, 32 * kSgFlowWarps, 0) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, sg_flow_kernel<true>, 32 * kSgFlowWarps, 0) != cudaSuccess) {
       (void)cudaGetLastError();
       v = 1;
     }
@@ -620,27 +655,48 @@ int sg_flow_blocks_per_sm() {
   return nb;
 }
 
-void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, int nsm, cudaStream_t st) {
+void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, bool codes, int nsm, cudaStream_t st) {
   if (f.total_units <= 0) return;
   const int64_t warps = std::min<int64_t>(f.total_units, (int64_t)nsm * sg_flow_blocks_per_sm() * kSgFlowWarps);
-  sg_flow_kernel<<<(int)((warps + kSgFlowWarps - 1) / kSgFlowWarps), 32 * kSgFlowWarps, 0, st>>>(f, ar, p, tb);
+  const int blocks = (int)((warps + kSgFlowWarps - 1) / kSgFlowWarps);
+  if (codes)
+    sg_flow_kernel<true><<<blocks, 32 * kSgFlowWarps, 0, st>>>(f, ar, p, tb);
+  else
+    sg_flow_kernel<false><<<blocks, 32 * kSgFlowWarps, 0, st>>>(f, ar, p, tb);
 }
 
 // ------------------------------------------------------------------ traceback (:869-914)
-// R: rows per lane of the layout that wrote the codes (kSgR for sg_kernel, 1 for the weighted kernel).
+// State machine of impl/sequenceAlignment3.cpp:869-914: start in the state that produced the cell; a gap state persists
+// while the cell's continuation flag is set; unwritten cells (outside the band, and the unweighted DP's last band
+// column) read 255; the remaining rows and columns pad the walk as D and I, and the CIGAR is reversed.  R: rows per
+// lane of the layout that wrote the codes (kSgR for the unweighted kernels, 1 for the weighted kernel).
+//
+// One warp per DP walks through shared-memory windows of the code store.  In the stripe / step / lane
+// layout every move of the walk (diagonal, up, left) goes to a lower address, at most 2 x 32 x R + R bytes lower,
+// so the warp stages the kSgTbWin bytes that end at the current cell with coalesced 16-byte loads and lane 0 walks
+// them until the path leaves the window below; one memory round trip then serves about kSgTbWin / (32 R) moves
+// instead of one.  The CIGAR is built and reversed as in sg_traceback_kernel.  tb_bytes: size of the code store
+// (no load goes past it).
+constexpr int kSgTbWin = 4096;
+
 template <int R>
-__global__ void sg_traceback_kernel(SgTask *__restrict__ tasks, const int *__restrict__ idx, int n, int w,
-                                    const uint8_t *__restrict__ tb, uint32_t *__restrict__ cig) {
+__global__ void __launch_bounds__(128) sg_traceback_warp_kernel(SgTask *__restrict__ tasks, const int *__restrict__ idx,
+                                                                int n, int w, const uint8_t *__restrict__ tb,
+                                                                int64_t tb_bytes, uint32_t *__restrict__ cig) {
   constexpr int kRows = 32 * R;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  SgTask &T = tasks[idx[k]];
+  __shared__ __align__(16) uint8_t win[4][kSgTbWin];
+  const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (gw >= n) return;  // whole warp
+  SgTask &T = tasks[idx[gw]];
   const int n2 = T.n2;
   const int64_t span = 2 * (int64_t)w + kRows;
   const int64_t stride = (n2 < span ? (int64_t)n2 : span) + 32;
   int ii = T.end1, jj = T.end2, state = 0, nc = 0;
   uint32_t *out = cig + T.cig_off;
   uint32_t last = 0xFFFFFFFFu;
+  int64_t base = -1;  // window [base, base + kSgTbWin) of the code store; -1: none yet
+  bool full = false;
   auto push = [&](uint32_t op) {
     if (nc > 0 && (last & 0xFu) == op) {
       last += 1u << 4;
@@ -649,53 +705,81 @@ __global__ void sg_traceback_kernel(SgTask *__restrict__ tasks, const int *__res
       last = (1u << 4) | op;
       out[nc++] = last;
     } else {
-      T.status = 3;
+      full = true;
     }
   };
-  while (ii > 0 && jj > 0) {
-    int code = 255;
-    const int c0 = max(ii - w, 1), c1 = min(ii + w, n2);
-    // the unweighted DP writes no code for the band's last column (it reads 255); the weighted DP does
-    if (ii <= T.rows && jj >= c0 && (jj < c1 || (R == 1 && jj == c1))) {
-      const int s = (ii - 1) / kRows, rr = (ii - 1) % kRows, l = rr / R, kk = rr % R;
-      const int jstart = max(kRows * s + 1 - w, 1);
-      const int64_t t = jj - jstart + l;
-      code = tb[T.tb_off + (((int64_t)s * stride + t) * 32 + l) * R + kk];
+  for (;;) {
+    // lane 0 walks while the next cell is outside the band (no read) or inside the window; the warp refills the
+    // window when the walk needs a cell below it
+    int64_t need = -1;
+    if (lane == 0) {
+      while (ii > 0 && jj > 0) {
+        int code = 255;
+        const int c0 = max(ii - w, 1), c1 = min(ii + w, n2);
+        if (ii <= T.rows && jj >= c0 && (jj < c1 || (R == 1 && jj == c1))) {
+          const int s = (ii - 1) / kRows, rr = (ii - 1) % kRows, l = rr / R, kk = rr % R;
+          const int jstart = max(kRows * s + 1 - w, 1);
+          const int64_t t = jj - jstart + l;
+          const int64_t a = T.tb_off + (((int64_t)s * stride + t) * 32 + l) * R + kk;
+          if (base < 0 || a < base || a >= base + kSgTbWin) {
+            need = a;
+            break;
+          }
+          code = win[wb][a - base];
+        }
+        if (state == 0)
+          state = code & 7;
+        else if (!((code >> (state + 2)) & 1))
+          state = 0;
+        if (state == 0) state = code & 7;
+        if (state == 0) {
+          push(0);
+          --ii;
+          --jj;
+        } else if (state == 1 || state == 3) {
+          push(2);
+          --ii;
+        } else {
+          push(1);
+          --jj;
+        }
+      }
     }
-    if (state == 0)
-      state = code & 7;
-    else if (!((code >> (state + 2)) & 1))
-      state = 0;
-    if (state == 0) state = code & 7;
-    if (state == 0) {
-      push(0);
-      --ii;
-      --jj;
-    } else if (state == 1 || state == 3) {
-      push(2);
-      --ii;
-    } else {
-      push(1);
-      --jj;
+    need = __shfl_sync(0xFFFFFFFFu, need, 0);
+    if (need < 0) break;
+    // the window that ends (16-byte aligned) just past the needed byte, clipped to the store
+    base = (((need + 16) & ~(int64_t)15) - kSgTbWin);
+    if (base < 0) base = 0;
+    __syncwarp();
+    for (int c = lane; c < kSgTbWin / 16; c += 32) {
+      const int64_t a = base + 16 * (int64_t)c;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (a + 16 <= tb_bytes) v = __ldg(reinterpret_cast<const uint4 *>(tb + a));
+      *reinterpret_cast<uint4 *>(&win[wb][16 * c]) = v;
     }
+    __syncwarp();
   }
-  while (ii > 0) push(2), --ii;
-  while (jj > 0) push(1), --jj;
-  for (int a = 0, b = nc - 1; a < b; ++a, --b) {  // the reference reverses the walk (:915)
-    const uint32_t tmp = out[a];
-    out[a] = out[b];
-    out[b] = tmp;
+  if (lane == 0) {
+    while (ii > 0) push(2), --ii;
+    while (jj > 0) push(1), --jj;
+    for (int a = 0, b = nc - 1; a < b; ++a, --b) {  // the reference reverses the walk (:915)
+      const uint32_t tmp = out[a];
+      out[a] = out[b];
+      out[b] = tmp;
+    }
+    T.ncig = nc;
+    if (full) T.status = 3;
   }
-  T.ncig = nc;
 }
 
-void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, uint32_t *cig,
-                         cudaStream_t st, bool weighted_layout) {
+void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, int64_t tb_bytes,
+                         uint32_t *cig, cudaStream_t st, bool weighted_layout) {
   if (n <= 0) return;
+  const int blocks = (n + 3) / 4;
   if (weighted_layout)
-    sg_traceback_kernel<1><<<(n + 127) / 128, 128, 0, st>>>(tasks, idx, n, bandwidth, tb, cig);
+    sg_traceback_warp_kernel<1><<<blocks, 128, 0, st>>>(tasks, idx, n, bandwidth, tb, tb_bytes, cig);
   else
-    sg_traceback_kernel<kSgR><<<(n + 127) / 128, 128, 0, st>>>(tasks, idx, n, bandwidth, tb, cig);
+    sg_traceback_warp_kernel<kSgR><<<blocks, 128, 0, st>>>(tasks, idx, n, bandwidth, tb, tb_bytes, cig);
 }
 
 // ------------------------------------------------------------------ weighted DPs (one warp per DP)

@@ -949,76 +949,119 @@ int launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, in
 // State machine of impl/sequenceAlignment3.cpp:1413-1438: start in the state that produced the cell; a gap state
 // persists while the cell's continuation bit is set; ops are appended as the walk goes (no final reverse, because
 // the walk over the reverse-complement pass already runs in forward order).  Unwritten cells read 255.
-__device__ void xdrop_traceback_kernel_body(XTask &T, const uint32_t *__restrict__ tb, uint32_t *__restrict__ cig) {
+//
+// One warp per pass.  The band store is row-major, so every move of the walk (diagonal, up, left) goes to the same
+// or a lower word: the warp stages the kXtWin words that end at the cell it needs with coalesced 16-byte loads, and
+// lane 0 walks them until the path leaves the window below (one memory round trip per window instead of one per
+// move).  tb_words: size of the band store (no load goes past it).
+constexpr int kXtWin = 1024;
+
+__device__ void xdrop_traceback_warp(XTask &T, const uint32_t *__restrict__ tb, int64_t tb_words,
+                                     uint32_t *__restrict__ cig, uint32_t *__restrict__ win, int lane) {
   const int w = T.w, wpr = xd_words_per_row(w);
   int ii = T.end1, jj = T.end2, state = 0, nc = 0;
   uint32_t *out = cig + T.cig_off;
   uint32_t last = 0xFFFFFFFFu;
-  while (ii > 0 && jj > 0) {
-    int code = 255;
-    const int k = jj - ii + w;
-    if (ii <= T.rows && k >= 0 && k <= 2 * w) {
-      const uint32_t nib = (tb[T.tb_off + (int64_t)(ii - 1) * wpr + (k >> 3)] >> (4 * (k & 7))) & 0xFu;
-      if ((nib & 3u) != 3u) code = (int)((nib & 3u) | (((nib >> 2) & 1u) << 3) | (((nib >> 3) & 1u) << 4));
-    }
-    if (state == 0)
-      state = code & 7;
-    else if (!((code >> (state + 2)) & 1))
-      state = 0;
-    if (state == 0) state = code & 7;
-    uint32_t op;
-    if (state == 0) {
-      op = 0;
-      --ii;
-      --jj;
-    } else if (state == 1 || state == 3) {
-      op = 2;
-      --ii;
-    } else {
-      op = 1;
-      --jj;
-    }
-    if (nc > 0 && (last & 0xFu) == op) {
-      last += 1u << 4;
-      out[nc - 1] = last;
-    } else {
-      if (nc >= T.cig_cap) {
-        T.status = 3;
-        break;
+  int64_t base = -1;  // window [base, base + kXtWin) of the store; -1: none yet
+  bool full = false;
+  for (;;) {
+    int64_t need = -1;
+    if (lane == 0) {
+      while (ii > 0 && jj > 0 && !full) {
+        int code = 255;
+        const int k = jj - ii + w;
+        if (ii <= T.rows && k >= 0 && k <= 2 * w) {
+          const int64_t a = T.tb_off + (int64_t)(ii - 1) * wpr + (k >> 3);
+          if (base < 0 || a < base || a >= base + kXtWin) {
+            need = a;
+            break;
+          }
+          const uint32_t nib = (win[a - base] >> (4 * (k & 7))) & 0xFu;
+          if ((nib & 3u) != 3u) code = (int)((nib & 3u) | (((nib >> 2) & 1u) << 3) | (((nib >> 3) & 1u) << 4));
+        }
+        if (state == 0)
+          state = code & 7;
+        else if (!((code >> (state + 2)) & 1))
+          state = 0;
+        if (state == 0) state = code & 7;
+        uint32_t op;
+        if (state == 0) {
+          op = 0;
+          --ii;
+          --jj;
+        } else if (state == 1 || state == 3) {
+          op = 2;
+          --ii;
+        } else {
+          op = 1;
+          --jj;
+        }
+        if (nc > 0 && (last & 0xFu) == op) {
+          last += 1u << 4;
+          out[nc - 1] = last;
+        } else if (nc >= T.cig_cap) {
+          full = true;
+        } else {
+          last = (1u << 4) | op;
+          out[nc++] = last;
+        }
       }
-      last = (1u << 4) | op;
-      out[nc++] = last;
     }
+    need = __shfl_sync(0xFFFFFFFFu, need, 0);
+    if (need < 0) break;
+    base = ((need + 4) & ~(int64_t)3) - kXtWin;  // ends (16-byte aligned) just past the needed word
+    if (base < 0) base = 0;
+    __syncwarp();
+    for (int c = lane; c < kXtWin / 4; c += 32) {
+      const int64_t a = base + 4 * (int64_t)c;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (a + 4 <= tb_words) v = __ldg(reinterpret_cast<const uint4 *>(tb + a));
+      *reinterpret_cast<uint4 *>(win + 4 * c) = v;
+    }
+    __syncwarp();
   }
-  T.iii = ii;
-  T.jjj = jj;
-  T.ncig = nc;
+  if (lane == 0) {
+    if (full) T.status = 3;
+    T.iii = ii;
+    T.jjj = jj;
+    T.ncig = nc;
+  }
 }
 
-__global__ void xdrop_traceback_kernel(XTask *__restrict__ tasks, const int *__restrict__ idx, int n,
-                                       const uint32_t *__restrict__ tb, uint32_t *__restrict__ cig) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  xdrop_traceback_kernel_body(tasks[idx[t]], tb, cig);
+__global__ void __launch_bounds__(128) xdrop_traceback_kernel(XTask *__restrict__ tasks, const int *__restrict__ idx,
+                                                              int n, const uint32_t *__restrict__ tb, int64_t tb_words,
+                                                              uint32_t *__restrict__ cig) {
+  __shared__ __align__(16) uint32_t win[4][kXtWin];
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (gw >= n) return;  // whole warp
+  xdrop_traceback_warp(tasks[idx[gw]], tb, tb_words, cig, win[threadIdx.x >> 5], lane);
 }
 
 // Chained form: every task of the batch that finished with codes takes a CIGAR slot of end1 + end2 + 2 words from an
-// arena sized for the bound n1 + n2 + 2 per task, then runs the state machine above.
-__global__ void xdrop_traceback_all_kernel(XTask *__restrict__ tasks, int n, const uint32_t *__restrict__ tb,
-                                           uint32_t *__restrict__ cig, unsigned long long *__restrict__ cig_cursor) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
+// arena sized for the bound n1 + n2 + 2 per task, then runs the walk above.
+__global__ void __launch_bounds__(128) xdrop_traceback_all_kernel(XTask *__restrict__ tasks, int n,
+                                                                  const uint32_t *__restrict__ tb, int64_t tb_words,
+                                                                  uint32_t *__restrict__ cig,
+                                                                  unsigned long long *__restrict__ cig_cursor) {
+  __shared__ __align__(16) uint32_t win[4][kXtWin];
+  const int lane = threadIdx.x & 31;
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (t >= n) return;  // whole warp
   XTask &T = tasks[t];
   if (T.status != 0 || !T.want_codes) return;
-  T.cig_cap = max(T.end1, 0) + max(T.end2, 0) + 2;
-  T.cig_off = (int64_t)atomicAdd(cig_cursor, (unsigned long long)T.cig_cap);
-  xdrop_traceback_kernel_body(T, tb, cig);
+  if (lane == 0) {
+    T.cig_cap = max(T.end1, 0) + max(T.end2, 0) + 2;
+    T.cig_off = (int64_t)atomicAdd(cig_cursor, (unsigned long long)T.cig_cap);
+  }
+  __syncwarp();
+  xdrop_traceback_warp(T, tb, tb_words, cig, win[threadIdx.x >> 5], lane);
 }
 
-void launch_xdrop_traceback_all(XTask *tasks, int n, const uint32_t *tb, uint32_t *cig,
+void launch_xdrop_traceback_all(XTask *tasks, int n, const uint32_t *tb, int64_t tb_words, uint32_t *cig,
                                 unsigned long long *cig_cursor, cudaStream_t st) {
   if (n <= 0) return;
-  xdrop_traceback_all_kernel<<<(n + 127) / 128, 128, 0, st>>>(tasks, n, tb, cig, cig_cursor);
+  xdrop_traceback_all_kernel<<<(n + 3) / 4, 128, 0, st>>>(tasks, n, tb, tb_words, cig, cig_cursor);
 }
 
 // Dense offsets of the finished tasks' CIGARs in task order: one block; each thread sums a contiguous run of tasks,
@@ -1066,9 +1109,10 @@ void launch_xdrop_cigar_pack(XTask *tasks, int n, const uint32_t *cig, uint32_t 
   xdrop_cigar_copy_kernel<<<(n + 7) / 8, 256, 0, st>>>(tasks, n, cig, dense);
 }
 
-void launch_xdrop_traceback(XTask *tasks, const int *idx, int n, const uint32_t *tb, uint32_t *cig, cudaStream_t st) {
+void launch_xdrop_traceback(XTask *tasks, const int *idx, int n, const uint32_t *tb, int64_t tb_words, uint32_t *cig,
+                            cudaStream_t st) {
   if (n <= 0) return;
-  xdrop_traceback_kernel<<<(n + 127) / 128, 128, 0, st>>>(tasks, idx, n, tb, cig);
+  xdrop_traceback_kernel<<<(n + 3) / 4, 128, 0, st>>>(tasks, idx, n, tb, tb_words, cig);
 }
 
 }  // namespace dcns

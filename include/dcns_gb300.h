@@ -190,7 +190,9 @@ typedef struct {
   int32_t lanes, bins;
   double bin_ratio;
   int32_t scan_tiles_per_thread;  /* seed-scan tiling target: rows split into chunks below this many tiles per thread */
-  int32_t sg_warps;               /* warps per 2-piece DP (0: two for launches of many DPs, else eight) */
+  int32_t sg_warps;               /* warps per 2-piece DP when one CTA runs a DP (0: two for launches of many DPs,
+                                     else eight) */
+  int32_t sg_flow;                /* 1: 2-piece DPs run as a flow of 128-row stripe units over one persistent grid */
   int32_t n_bins_tuned;           /* bins with their own x-drop forms below (0: every bin uses bin 0's values) */
   int32_t xdrop_warp_from[16], xdrop_wave_max_w[16], xdrop_flat[16], xdrop_handoff[16];
 } dcns_tuning;

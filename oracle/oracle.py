@@ -216,8 +216,9 @@ class Oracle(_Lib):
         assert n >= 0, "fragment buffer too small"
         return _unflatten(n, frag, pe, cg)
 
-    def find_seeded(self, s1, s2, seeds, max_align=20000, **kw):
-        """The seeded 2-piece overload (cut2Gaps2): seeds = [(start1, end1, start2, end2)] 0-based, in order."""
+    def find_seeded(self, s1, s2, seeds, max_align=20000, with_cells=False, **kw):
+        """The seeded 2-piece overload (cut2Gaps2): seeds = [(start1, end1, start2, end2)] 0-based, in order.  With
+        with_cells, also the algorithmic cells it evaluated ({"scan", "scan_rev", "xdrop", "semiglobal"})."""
         _, ip, dp = params(**kw)
         s1, s2 = _i8(s1), _i8(s2)
         sd = np.asarray(seeds, np.int32).reshape(-1, 4)
@@ -231,7 +232,10 @@ class Oracle(_Lib):
                                          _p(ip, I32P), _p(dp, F64P), _p(frag, I64P), _p(pe, F64P), _p(cg, U32P), fcap,
                                          ccap, _p(nc, I32P), _p(cells, I64P))
         assert n >= 0, "fragment buffer too small"
-        return _unflatten(n, frag, pe, cg)
+        out = _unflatten(n, frag, pe, cg)
+        if with_cells:
+            return out, dict(zip(("scan", "scan_rev", "xdrop", "semiglobal"), map(int, cells)))
+        return out
 
     def find_xseeds(self, s1, s2, seeds, **kw):
         """The x-seed overload without maximumAlignLength (findSimilar...4.cpp:532): seeds = [(start1, end1, start2,
