@@ -290,21 +290,25 @@ def line_seeded_chromosome(eng, timed, threads, gpu, steps=3, n_seeds=16, cpu_se
     pair's leading part (a whole-pair seed takes minutes on one core), one seed per thread."""
     from concurrent.futures import ThreadPoolExecutor
     from dcns_gb300 import workloads as W
+    import dcns_gb300 as D
     a, b = W.long_pairs_200kb(n_pairs=1)[0]
     frs = eng.align_pairs([(a, b)], 1)[0][:n_seeds]
     seeds = [(f.start1 - 1, f.end1 - 1, f.start2 - 1, f.end2 - 1) for f in frs]
-    eng.align_seeded([(a, b)], [seeds], max_align_len=0)
+    # a context of its own, so that its buffers are this call's alone (device_bytes)
+    own = D.Engine(gpu)
+    own.align_seeded([(a, b)], [seeds], max_align_len=0)
     tot_ms, cells, sg_ms, tb_ms, nfrag, dev = 0.0, 0, 0.0, 0.0, 0, 0
     with ClockSampler(gpu) as clk:
         for _ in range(steps):
-            res, t = timed(lambda: eng.align_seeded([(a, b)], [seeds], max_align_len=0))
-            st = eng.last_stats()
+            res, t = timed(lambda: own.align_seeded([(a, b)], [seeds], max_align_len=0))
+            st = own.last_stats()
             tot_ms += t
             cells += st["cells_semiglobal"]
             sg_ms += st["ms_sg_kernel"]
             tb_ms += st["ms_sg_tb_kernel"]
             nfrag = len(res[0])
             dev = max(dev, st["bytes_device"])
+    own.close()
     # CPU: the same kind of call on the pair's first cpu_len bases of each sequence (a whole-pair seed takes about two
     # minutes of one core), one x-seed per thread, cells counted by the oracle
     from oracle import oracle as O

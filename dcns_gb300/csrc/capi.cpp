@@ -527,10 +527,17 @@ static int copy_cigars(const std::vector<std::vector<uint32_t>> &cg, uint32_t *c
 int dcns_xextend_batch(dcns_ctx *ctx, const dcns_pair *tasks, int64_t n, const dcns_params *params, int want_cigar,
                        int32_t *out, uint32_t *cigar, int64_t cigar_cap, int64_t *cigar_offset) {
   if (!ctx || !params || (n > 0 && !out)) return DCNS_ERR_INVALID;
-  std::vector<std::vector<uint32_t>> cg;
-  int rc = guarded(ctx, [&] { xextend_batch(ctx->C, to_pairs(tasks, n), to_params(params), want_cigar != 0, out, cg); });
+  std::vector<uint32_t> cg;
+  std::vector<int64_t> off;
+  int rc = guarded(ctx, [&] {
+    xextend_batch(ctx->C, to_pairs(tasks, n), to_params(params), want_cigar != 0, out, cg, off);
+  });
   if (rc != DCNS_OK) return rc;
-  return copy_cigars(cg, cigar, cigar_cap, cigar_offset);
+  if (cigar_offset) std::memcpy(cigar_offset, off.data(), sizeof(int64_t) * off.size());
+  if (!cigar) return DCNS_OK;
+  if ((int64_t)cg.size() > cigar_cap) return DCNS_ERR_NOMEM;
+  if (!cg.empty()) std::memcpy(cigar, cg.data(), sizeof(uint32_t) * cg.size());
+  return DCNS_OK;
 }
 
 int dcns_semiglobal_batch(dcns_ctx *ctx, const dcns_pair *tasks, int64_t n, const dcns_params *params,

@@ -155,6 +155,7 @@ struct SgFlow {
   SgTask *tasks;
   const int *idx;                   // queue order: DP q is tasks[idx[q]]
   const int64_t *unit_begin;        // [n]: first unit (stripe) of DP q; DP q has max(1, stripes) units
+  const int2 *order;                // [total_units]: (q, stripe) in hand-out order (each DP's stripes ascending)
   SgFlowDP *dps;                    // [n], queue order
   SgRec *bnd;
   int *prog;                        // [total_units]: columns of the unit's last row published (zero before launch)
@@ -217,6 +218,7 @@ int sg_ctas_per_sm(int nw);
 // codes: the DPs keep direction codes (every DP of a launch alike)
 void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, bool codes, int nsm, cudaStream_t st);
 int64_t sg_flow_units(int n1, int n2, int w);  // stripe units of one DP in the flow form (at least 1)
+int64_t sg_flow_grid_warps(int nsm);           // warps of the flow kernel's persistent grid
 int64_t sg_bnd_bytes(int grid, int max_n2, int nw);
 // tb_bytes: size of the code store tb (the traceback reads nothing past it)
 void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, int64_t tb_bytes,

@@ -33,7 +33,6 @@
 #include <condition_variable>
 #include <functional>
 #include <thread>
-#include <unordered_map>
 
 namespace dcns {
 
@@ -350,10 +349,11 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
   std::vector<int64_t> src_off(ns);
   std::vector<int32_t> len(ns);
   int64_t total_src = 0, total_dst = 0;
-  // A sequence passed for several pairs (the same pointer and length: one reference against many queries, as in the
-  // multi-species caller) is staged and packed once; the later pairs point at the first copy.
-  std::unordered_map<const int8_t *, std::pair<int32_t, int64_t>> seen;
-  seen.reserve((size_t)ns);
+  // A sequence passed again for the next pair on the same side (the same pointer and length: one reference against
+  // many queries, as in the multi-species caller) is staged and packed once; the later pairs point at the first copy.
+  const int8_t *last_src[2] = {nullptr, nullptr};
+  int32_t last_n[2] = {-1, -1};
+  int64_t last_base[2] = {0, 0};
   for (int64_t k = 0; k < np; ++k) {
     for (int h = 0; h < 2; ++h) {
       const int32_t n = h ? pairs[k].n2 : pairs[k].n1;
@@ -361,14 +361,13 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
       if (n < 0) throw Error(DCNS_ERR_INVALID, "negative sequence length");
       if (n >= kMaxSeqLen) throw Error(DCNS_ERR_INVALID, "sequences must be shorter than 2^28 bases");
       if (n > 0) {
-        auto it = seen.find(src);
-        if (it != seen.end() && it->second.first == n) {
+        if (src == last_src[h] && n == last_n[h]) {
           len[2 * k + h] = 0;  // nothing to stage or pack
           src_off[2 * k + h] = total_src;
-          seq_base[2 * k + h] = it->second.second;
+          seq_base[2 * k + h] = last_base[h];
           continue;
         }
-        seen[src] = {n, total_dst};
+        last_src[h] = src, last_n[h] = n, last_base[h] = total_dst;
       }
       len[2 * k + h] = n;
       src_off[2 * k + h] = total_src;
@@ -1433,7 +1432,7 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
   const bool flow = W == nullptr && C.sg_flow;
   auto flow_bytes = [&](const SgTask &g) -> int64_t {
     return flow ? (int64_t)sizeof(SgRec) * (std::max(g.n2, 0) + 2) + (int64_t)sizeof(SgFlowDP) + 8 +
-                      4 * sg_flow_units(g.n1, g.n2, P.bandwidth)
+                      12 * sg_flow_units(g.n1, g.n2, P.bandwidth)
                 : 0;
   };
   while (k0 < n) {
@@ -1474,30 +1473,56 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
     h2d(C, C.d_sg, G.data(), (size_t)n);
     SgFlow F{};
     if (flow) {
-      // units (stripes) and boundary rows in queue order; flow state in one buffer: unit_begin | dps | prog | counters
+      // units (stripes) and boundary rows in queue order; flow state in one buffer:
+      // unit_begin | dps | order | prog | counters
       std::vector<int64_t> ub((size_t)m);
+      std::vector<int32_t> nst((size_t)m);
       std::vector<SgFlowDP> dps((size_t)m);
       int64_t units = 0, brows = 0;
       for (int64_t q = 0; q < m; ++q) {
         const SgTask &g = G[idx[q]];
         ub[q] = units;
-        units += sg_flow_units(g.n1, g.n2, P.bandwidth);
+        nst[q] = (int32_t)sg_flow_units(g.n1, g.n2, P.bandwidth);
+        units += nst[q];
         dps[q] = SgFlowDP{brows, 0, 0, 0, -1, -1, 0, kOut, kOut};
         brows += std::max(g.n2, 0) + 2;
       }
+      // hand-out order: stripe-major within groups of consecutive DPs holding at least eight grid-fulls of units;
+      // inside a group the DPs go by stripe count, most first, so the DPs that have a stripe s form a prefix
+      const int64_t group_units = 8 * sg_flow_grid_warps(C.nsm);
+      std::vector<int2> order((size_t)units);
+      {
+        int64_t u = 0;
+        std::vector<int32_t> perm;
+        for (int64_t g0 = 0; g0 < m;) {
+          int64_t g1 = g0, gu = 0;
+          while (g1 < m && (g1 == g0 || gu < group_units)) gu += nst[g1++];
+          perm.resize((size_t)(g1 - g0));
+          for (int64_t k = g0; k < g1; ++k) perm[k - g0] = (int32_t)k;
+          std::stable_sort(perm.begin(), perm.end(), [&](int32_t a, int32_t b) { return nst[a] > nst[b]; });
+          for (int32_t s = 0, cnt = (int32_t)perm.size(); cnt > 0; ++s) {
+            while (cnt > 0 && nst[perm[cnt - 1]] <= s) --cnt;
+            for (int32_t k = 0; k < cnt; ++k) order[u++] = int2{perm[k], s};
+          }
+          g0 = g1;
+        }
+        if (u != units) throw Error(DCNS_ERR_DEVICE, "semi-global stripe order: unit count mismatch");
+      }
       auto al = [](int64_t b) { return (b + 255) / 256 * 256; };
-      const int64_t o_dps = al(8 * m), o_prog = o_dps + al((int64_t)sizeof(SgFlowDP) * m);
-      const int64_t o_cnt = o_prog + al(4 * units), total = o_cnt + 256;
+      const int64_t o_dps = al(8 * m), o_ord = o_dps + al((int64_t)sizeof(SgFlowDP) * m);
+      const int64_t o_prog = o_ord + al(8 * units), o_cnt = o_prog + al(4 * units), total = o_cnt + 256;
       C.d_flow.ensure(C, (size_t)total);
       C.d_bnd.ensure(C, (size_t)(sizeof(SgRec) * brows));
       char *base = static_cast<char *>(C.d_flow.p);
       DCNS_CK(cudaMemcpyAsync(base, ub.data(), 8 * m, cudaMemcpyHostToDevice, C.st));
       DCNS_CK(cudaMemcpyAsync(base + o_dps, dps.data(), sizeof(SgFlowDP) * m, cudaMemcpyHostToDevice, C.st));
+      DCNS_CK(cudaMemcpyAsync(base + o_ord, order.data(), 8 * units, cudaMemcpyHostToDevice, C.st));
       DCNS_CK(cudaMemsetAsync(base + o_prog, 0, (size_t)(total - o_prog), C.st));
       F.tasks = C.d_sg.as<SgTask>();
       F.idx = C.d_idx.as<int>();
       F.unit_begin = reinterpret_cast<const int64_t *>(base);
       F.dps = reinterpret_cast<SgFlowDP *>(base + o_dps);
+      F.order = reinterpret_cast<const int2 *>(base + o_ord);
       F.bnd = C.d_bnd.as<SgRec>();
       F.prog = reinterpret_cast<int *>(base + o_prog);
       F.unit_counter = reinterpret_cast<unsigned long long *>(base + o_cnt);
@@ -2325,37 +2350,65 @@ void smith_waterman_batch(Context &C, const std::vector<PairIn> &tasks, const Pa
 }
 
 void xextend_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, bool want_cigar, int32_t *out,
-                   std::vector<std::vector<uint32_t>> &cigars) {
+                   std::vector<uint32_t> &cigar, std::vector<int64_t> &cigar_off) {
   validate(P);
   const int64_t n = (int64_t)tasks.size();
+  auto t0 = Clock::now();
+  C.call_t0 = t0;
   C.stats = dcns_stats{};
-  cigars.assign(n, {});
+  cigar.clear();
+  cigar_off.assign(n + 1, 0);
   if (n == 0) return;
   upload(C, tasks);
+  auto tp = phase(C, "upload", t0);
   std::vector<XTask> X(n);
-  for (int64_t k = 0; k < n; ++k) {
-    XTask x{};
-    x.base1 = C.seq_base[2 * k];
-    x.base2 = C.seq_base[2 * k + 1];
-    x.n1 = tasks[k].n1;
-    x.n2 = tasks[k].n2;
-    x.dir = 0;
-    x.w = P.w;
-    X[k] = x;
-  }
-  std::vector<uint32_t> flat;
+  parallel_for((n + 4095) / 4096, [&](int64_t b) {
+    for (int64_t k = b * 4096, e = std::min(n, k + 4096); k < e; ++k) {
+      XTask x{};
+      x.base1 = C.seq_base[2 * k];
+      x.base2 = C.seq_base[2 * k + 1];
+      x.n1 = tasks[k].n1;
+      x.n2 = tasks[k].n2;
+      x.dir = 0;
+      x.w = P.w;
+      X[k] = x;
+    }
+  });
+  tp = phase(C, "tasks", tp);
   std::vector<int64_t> hoff;
-  run_xdrop(C, X, P, want_cigar, want_cigar ? &flat : nullptr, want_cigar ? &hoff : nullptr);
-  if (want_cigar)
-    for (int64_t k = 0; k < n; ++k) cigars[k].assign(flat.begin() + hoff[k], flat.begin() + hoff[k] + X[k].ncig);
-  for (int64_t k = 0; k < n; ++k) {
-    out[6 * k + 0] = X[k].score;
-    out[6 * k + 1] = X[k].end1 - 1;
-    out[6 * k + 2] = X[k].end2 - 1;
-    out[6 * k + 3] = want_cigar ? X[k].iii : 0;
-    out[6 * k + 4] = want_cigar ? X[k].jjj : 0;
-    out[6 * k + 5] = (int32_t)cigars[k].size();
+  run_xdrop(C, X, P, want_cigar, want_cigar ? &cigar : nullptr, want_cigar ? &hoff : nullptr);
+  tp = phase(C, "xdrop", tp);
+  if (want_cigar) {
+    // the CIGARs in task order, densely (the chained levels already pack them so; retried passes come after)
+    bool dense = true;
+    for (int64_t k = 0; k < n; ++k) {
+      cigar_off[k + 1] = cigar_off[k] + X[k].ncig;
+      dense &= hoff[k] == cigar_off[k] || X[k].ncig == 0;
+    }
+    if (!dense || (int64_t)cigar.size() != cigar_off[n]) {
+      std::vector<uint32_t> packed((size_t)cigar_off[n]);
+      parallel_for((n + 4095) / 4096, [&](int64_t b) {
+        for (int64_t k = b * 4096, e = std::min(n, k + 4096); k < e; ++k)
+          if (X[k].ncig > 0)
+            std::memcpy(packed.data() + cigar_off[k], cigar.data() + hoff[k], sizeof(uint32_t) * X[k].ncig);
+      });
+      cigar.swap(packed);
+    }
   }
+  parallel_for((n + 4095) / 4096, [&](int64_t b) {
+    for (int64_t k = b * 4096, e = std::min(n, k + 4096); k < e; ++k) {
+      out[6 * k + 0] = X[k].score;
+      out[6 * k + 1] = X[k].end1 - 1;
+      out[6 * k + 2] = X[k].end2 - 1;
+      out[6 * k + 3] = want_cigar ? X[k].iii : 0;
+      out[6 * k + 4] = want_cigar ? X[k].jjj : 0;
+      out[6 * k + 5] = want_cigar ? X[k].ncig : 0;
+    }
+  });
+  phase(C, "results", tp);
+  C.stats.ms_total = ms_since(t0);
+  C.stats.bytes_device = device_bytes(C);
+  print_phases(C, "xextend_batch");
 }
 
 void semiglobal_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, bool want_cigar, int32_t *out,

@@ -200,8 +200,9 @@ void align_xseeds(Context &C, const std::vector<PairIn> &pairs, const std::vecto
 void autotune(Context &C, Batch &B, const Params &P, int mode);
 double measure_issue_rate(int nsm, cudaStream_t st);
 void smith_waterman_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, int32_t *out);
+// cigar: every task's CIGAR in task order; cigar_off[k] .. cigar_off[k + 1] is task k's (n + 1 offsets)
 void xextend_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, bool want_cigar, int32_t *out,
-                   std::vector<std::vector<uint32_t>> &cigars);
+                   std::vector<uint32_t> &cigar, std::vector<int64_t> &cigar_off);
 void semiglobal_batch(Context &C, const std::vector<PairIn> &tasks, const Params &P, bool want_cigar, int32_t *out,
                       std::vector<std::vector<uint32_t>> &cigars);
 void sliding_window(Context &C, const int8_t *const *seqs, const int32_t *lens, int32_t n, const Params &P,

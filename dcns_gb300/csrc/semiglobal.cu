@@ -323,16 +323,20 @@ void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p,
 }
 
 // ------------------------------------------------------------------ stripes as a flow of independent warp units
-// The DPs of a launch are cut into their 128-row stripes, numbered DP after DP (queue order: largest DPs first) and
-// handed out by one atomic counter; every warp of a persistent grid takes the next stripe, computes it with the
-// per-cell code of sg_kernel (same wavefront, same code layout), and takes the next.  Stripe s of a DP depends only
+// The DPs of a launch are cut into their 128-row stripes (units), handed out by one atomic counter in the order of
+// SgFlow::order; every warp of a persistent grid takes the next unit, computes it with the per-cell code of sg_kernel
+// (same wavefront, same code layout), and takes the next.  The host orders the units stripe-major within groups of
+// consecutive DPs (queue order: largest DPs first): stripe 0 of every DP of the group, then stripe 1, ... so that
+// when a warp takes stripe s its stripe s - 1 has been running for a while, even when a few DPs of 200,000 rows make
+// up the whole launch (in DP order the late stripes of one long DP would wait for its wavefront to reach them).
+// Stripe s of a DP depends only
 // on stripe s - 1: the last row of s - 1 reaches s through the DP's boundary row in global memory (one row per DP:
 // stripe s reads a column before it overwrites it with its own last row, and s + 1 reads it only after s published
 // it), and s - 1 publishes how many columns of that row it has written (release / acquire per 32-column chunk).  So
 // a long DP runs on as many warps as it has stripes, each one chunk pair behind the stripe above it, instead of on
-// one CTA.  Stripes are handed out in increasing order and a stripe waits only on lower stripes of its own DP, which
-// are held by running warps, so the waits always end; each still has an iteration limit, after which the warp flags
-// a device error (SgFlow::err) and abandons the DP.
+// one CTA.  Each DP's stripes are handed out in increasing order and a stripe waits only on lower stripes of its own
+// DP, which are held by running warps, so the waits always end; each still has an iteration limit, after which the
+// warp flags a device error (SgFlow::err) and abandons the DP.
 //
 // Row-level decisions (running maximum, z-drop, non-positive row maximum) are taken in row order: after computing
 // stripe s, its warp waits until s - 1 is evaluated, evaluates its 128 rows from the DP's running state and
@@ -429,16 +433,12 @@ __global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Ar
     u = __shfl_sync(0xFFFFFFFFu, u, 0);
     if (u >= F.total_units) break;
     if (__any_sync(0xFFFFFFFFu, sg_ld_relaxed(F.err) != 0)) break;  // a wait ran out: the launch fails as a whole
-    // the DP of unit u: the last q with unit_begin[q] <= u
-    int lo = 0, hi = F.n - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (F.unit_begin[mid] <= u) lo = mid; else hi = mid - 1;
-    }
-    const int q = lo, s = (int)(u - F.unit_begin[q]);
+    const int2 qs = F.order[u];  // the u-th unit handed out: stripe qs.y of DP qs.x
+    const int q = qs.x, s = qs.y;
+    const int64_t ui = F.unit_begin[q] + s;  // its progress counter
     SgTask &T = F.tasks[F.idx[q]];
     SgFlowDP &D = F.dps[q];
-    int *const prog_self = F.prog + u;
+    int *const prog_self = F.prog + ui;
     const int n1 = T.n1, n2 = T.n2;
     const int n1_eff = (n1 <= 0 || n2 <= 0) ? 0 : min(n1, n2 + w);
     const int nstripes = (n1_eff + kSgRows - 1) / kSgRows;
@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Ar
     const int r_last = n2 - 1 + w;
     const int64_t stride = sg_stride_steps(n2, w);
     SgRec *const brow = F.bnd + D.bnd_off;  // the DP's boundary row, by column
-    const int *const prog_up = s > 0 ? F.prog + (u - 1) : nullptr;
+    const int *const prog_up = s > 0 ? F.prog + (ui - 1) : nullptr;
     const int i0 = kSgRows * s + 1 + kSgR * lane;
     const bool live = i0 <= n1_eff;
     // per row of the lane: band [c0, c0 + span] (rows past the DP: an empty band), its base, the stale-column role,
@@ -655,9 +655,11 @@ int sg_flow_blocks_per_sm() {
   return nb;
 }
 
+int64_t sg_flow_grid_warps(int nsm) { return (int64_t)nsm * sg_flow_blocks_per_sm() * kSgFlowWarps; }
+
 void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, bool codes, int nsm, cudaStream_t st) {
   if (f.total_units <= 0) return;
-  const int64_t warps = std::min<int64_t>(f.total_units, (int64_t)nsm * sg_flow_blocks_per_sm() * kSgFlowWarps);
+  const int64_t warps = std::min<int64_t>(f.total_units, sg_flow_grid_warps(nsm));
   const int blocks = (int)((warps + kSgFlowWarps - 1) / kSgFlowWarps);
   if (codes)
     sg_flow_kernel<true><<<blocks, 32 * kSgFlowWarps, 0, st>>>(f, ar, p, tb);
@@ -679,12 +681,21 @@ void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, bo
 // (no load goes past it).
 constexpr int kSgTbWin = 4096;
 
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 template <int R>
 __global__ void __launch_bounds__(128) sg_traceback_warp_kernel(SgTask *__restrict__ tasks, const int *__restrict__ idx,
                                                                 int n, int w, const uint8_t *__restrict__ tb,
                                                                 int64_t tb_bytes, uint32_t *__restrict__ cig) {
   constexpr int kRows = 32 * R;
-  __shared__ __align__(16) uint8_t win[4][kSgTbWin];
+  // two windows per warp: lane 0 walks one while the warp's asynchronous copies fill the other with the window just
+  // below it, where the walk goes next unless it crosses into the stripe above (a jump: then a synchronous fill)
+  __shared__ __align__(16) uint8_t win2[4][2][kSgTbWin];
   const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (gw >= n) return;  // whole warp
@@ -695,7 +706,11 @@ __global__ void __launch_bounds__(128) sg_traceback_warp_kernel(SgTask *__restri
   int ii = T.end1, jj = T.end2, state = 0, nc = 0;
   uint32_t *out = cig + T.cig_off;
   uint32_t last = 0xFFFFFFFFu;
-  int64_t base = -1;  // window [base, base + kSgTbWin) of the code store; -1: none yet
+  int64_t wbase[2] = {-1, -1};  // window [wbase, wbase + kSgTbWin) of the code store in each buffer; -1: none
+  int cur = 0;
+  bool pending = false;  // the other buffer is being filled with the window below the current one
+  int64_t base = -1;
+  const uint8_t *win = win2[wb][0];
   bool full = false;
   auto push = [&](uint32_t op) {
     if (nc > 0 && (last & 0xFu) == op) {
@@ -707,6 +722,16 @@ __global__ void __launch_bounds__(128) sg_traceback_warp_kernel(SgTask *__restri
     } else {
       full = true;
     }
+  };
+  auto fill = [&](int b, int64_t from) {  // every lane: its share of [from, from + kSgTbWin), asynchronously
+    for (int c = lane; c < kSgTbWin / 16; c += 32) {
+      const int64_t a = from + 16 * (int64_t)c;
+      if (a + 16 <= tb_bytes)
+        cp_async16(&win2[wb][b][16 * c], tb + a);
+      else
+        *reinterpret_cast<uint4 *>(&win2[wb][b][16 * c]) = make_uint4(0, 0, 0, 0);
+    }
+    cp_async_commit();
   };
   for (;;) {
     // lane 0 walks while the next cell is outside the band (no read) or inside the window; the warp refills the
@@ -725,7 +750,7 @@ __global__ void __launch_bounds__(128) sg_traceback_warp_kernel(SgTask *__restri
             need = a;
             break;
           }
-          code = win[wb][a - base];
+          code = win[a - base];
         }
         if (state == 0)
           state = code & 7;
@@ -747,18 +772,28 @@ __global__ void __launch_bounds__(128) sg_traceback_warp_kernel(SgTask *__restri
     }
     need = __shfl_sync(0xFFFFFFFFu, need, 0);
     if (need < 0) break;
-    // the window that ends (16-byte aligned) just past the needed byte, clipped to the store
-    base = (((need + 16) & ~(int64_t)15) - kSgTbWin);
-    if (base < 0) base = 0;
+    cp_async_wait_all();  // this lane's copies, for either buffer, have landed
     __syncwarp();
-    for (int c = lane; c < kSgTbWin / 16; c += 32) {
-      const int64_t a = base + 16 * (int64_t)c;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (a + 16 <= tb_bytes) v = __ldg(reinterpret_cast<const uint4 *>(tb + a));
-      *reinterpret_cast<uint4 *>(&win[wb][16 * c]) = v;
+    if (pending && need >= wbase[1 - cur] && need < wbase[1 - cur] + kSgTbWin) {
+      cur = 1 - cur;  // the prefetched window below
+    } else {
+      // the window that ends (16-byte aligned) just past the needed byte, clipped to the store
+      wbase[cur] = (((need + 16) & ~(int64_t)15) - kSgTbWin);
+      if (wbase[cur] < 0) wbase[cur] = 0;
+      fill(cur, wbase[cur]);
+      cp_async_wait_all();
+      __syncwarp();
     }
-    __syncwarp();
+    pending = false;
+    base = wbase[cur];
+    win = win2[wb][cur];
+    if (base > 0) {  // prefetch the window below while lane 0 walks this one
+      wbase[1 - cur] = base - kSgTbWin > 0 ? base - kSgTbWin : 0;
+      fill(1 - cur, wbase[1 - cur]);
+      pending = true;
+    }
   }
+  cp_async_wait_all();
   if (lane == 0) {
     while (ii > 0) push(2), --ii;
     while (jj > 0) push(1), --jj;
