@@ -141,7 +141,7 @@ class Tuning(C.Structure):
                 ("scan_tiles_per_thread", C.c_int32), ("sg_warps", C.c_int32), ("sg_flow", C.c_int32),
                 ("n_bins_tuned", C.c_int32),
                 ("xdrop_warp_from", C.c_int32 * 16), ("xdrop_wave_max_w", C.c_int32 * 16), ("xdrop_flat", C.c_int32 * 16),
-                ("xdrop_handoff", C.c_int32 * 16)]
+                ("xdrop_handoff", C.c_int32 * 16), ("xdrop_resume_lanes", C.c_int32 * 16)]
 
     def as_dict(self):
         n = max(self.n_bins_tuned, 1)
@@ -150,7 +150,8 @@ class Tuning(C.Structure):
                 "sg_flow": bool(self.sg_flow),
                 "xdrop_per_bin": [{"warp_from": self.xdrop_warp_from[b], "wave_max_w": self.xdrop_wave_max_w[b],
                                    "row_interleaved": bool(self.xdrop_flat[b]),
-                                   "handoff_rows": self.xdrop_handoff[b]} for b in range(n)]}
+                                   "handoff_rows": self.xdrop_handoff[b],
+                                   "handoff_lanes": self.xdrop_resume_lanes[b]} for b in range(n)]}
 
 
 class Results(C.Structure):

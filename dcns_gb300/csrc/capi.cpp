@@ -491,6 +491,7 @@ int dcns_get_tuning(const dcns_ctx *ctx, dcns_tuning *out) {
     out->xdrop_wave_max_w[b] = own ? C.bin_tune[b].xdrop_wave_max_w : C.xdrop_wave_max_w;
     out->xdrop_flat[b] = (own ? C.bin_tune[b].xdrop_flat : C.xdrop_flat) ? 1 : 0;
     out->xdrop_handoff[b] = own ? C.bin_tune[b].xdrop_handoff : C.xdrop_handoff;
+    out->xdrop_resume_lanes[b] = own ? C.bin_tune[b].xdrop_resume_lanes : C.xdrop_resume_lanes;
   }
   return DCNS_OK;
 }

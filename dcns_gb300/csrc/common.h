@@ -192,18 +192,20 @@ void launch_xdrop_traceback(XTask *tasks, const int *idx, int n, const uint32_t 
 void launch_xdrop_iota(int *list, int n, int *count, cudaStream_t st);
 // Hand-off of long register-band passes to the wavefront form: a pass of a row-interleaved level still running after
 // `rows` rows moves its band state to one of `cap` spill slots (2 x (2 x 20 + 2) ints each) and its id to list;
-// *count (zero before the level) counts the slots taken.  rows = 0 or cap = 0: off.
+// *count (zero before the level) counts the slots taken; `lanes` lanes then run each such pass.  rows = 0 or
+// cap = 0: off.
 struct XHandoff {
   int *list, *count;
   int32_t *spill;
   int cap, rows;
+  int lanes;  // lanes per handed-off pass: 8 or 16 (G-lane groups, 32 / G passes per warp) or 32 (one warp)
 };
 constexpr int kXdropSpillInts = 2 * (2 * 20 + 2);
 // fetch: the level's pass counter, zero before the launch (the row-interleaved register-band kernel, flat = true).
-// Returns the number of kernels launched.
+// Traceback slots hold min(n1, slot_rows) rows.  Returns the number of kernels launched.
 int launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
-                       int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int *fetch,
-                       const XHandoff &H, Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm,
+                       int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int slot_rows,
+                       int *fetch, const XHandoff &H, Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm,
                        int32_t *scratch, int64_t per_warp, int warps, int warp_from, int wave_max_w, bool flat,
                        cudaStream_t st);
 void launch_xdrop_traceback_all(XTask *tasks, int n, const uint32_t *tb, int64_t tb_words, uint32_t *cig,

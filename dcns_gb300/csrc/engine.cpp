@@ -148,6 +148,10 @@ void init_context(Context &C, int device, size_t budget) {
   if (const char *e = std::getenv("DCNS_XDROP_WAVE")) C.xdrop_wave_max_w = std::max(0, std::atoi(e));
   if (const char *e = std::getenv("DCNS_XDROP_FLAT")) C.xdrop_flat = std::atoi(e) != 0;
   if (const char *e = std::getenv("DCNS_XDROP_HANDOFF")) C.xdrop_handoff = std::max(0, std::atoi(e));
+  if (const char *e = std::getenv("DCNS_XDROP_RESUME_LANES")) {
+    const int v = std::atoi(e);
+    C.xdrop_resume_lanes = (v == 8 || v == 16 || v == 32) ? v : 8;
+  }
   if (const char *e = std::getenv("DCNS_SCAN_TILES")) C.scan_tiles_per_thread = std::max(1, std::min(64, std::atoi(e)));
   if (const char *e = std::getenv("DCNS_SG_WARPS")) {
     const int v = std::atoi(e);
@@ -382,14 +386,24 @@ void upload_into(Context &C, const std::vector<PairIn> &pairs, DevBuf &d_pk, Dev
   int8_t *stage = C.h_codes.as<int8_t>();
   // staged copy; the reference indexes its 5x5 score table with the codes, so anything outside 0..4 is rejected
   std::atomic<bool> badcode(false);
-  parallel_for(ns, [&](int64_t s) {
-    const PairIn &p = pairs[s / 2];
-    const int8_t *src = (s & 1) ? p.s2 : p.s1;
-    if (!len[s]) return;
-    int8_t *dst = stage + src_off[s];
-    std::memcpy(dst, src, (size_t)len[s]);
+  // blocks of consecutive sequences of about 1 MB each (one work item per sequence would serialise a million short
+  // sequences on the pool's work counter)
+  std::vector<int64_t> blk{0};
+  for (int64_t s = 0, acc = 0; s < ns; ++s) {
+    acc += len[s] + 64;
+    if (acc >= (1 << 20)) blk.push_back(s + 1), acc = 0;
+  }
+  if (blk.back() != ns) blk.push_back(ns);
+  parallel_for((int64_t)blk.size() - 1, [&](int64_t b) {
     uint8_t bad = 0;
-    for (int32_t i = 0; i < len[s]; ++i) bad |= (uint8_t)((uint8_t)dst[i] > 4);
+    for (int64_t s = blk[b]; s < blk[b + 1]; ++s) {
+      if (!len[s]) continue;
+      const PairIn &p = pairs[s / 2];
+      const int8_t *src = (s & 1) ? p.s2 : p.s1;
+      int8_t *dst = stage + src_off[s];
+      std::memcpy(dst, src, (size_t)len[s]);
+      for (int32_t i = 0; i < len[s]; ++i) bad |= (uint8_t)((uint8_t)dst[i] > 4);
+    }
     if (bad) badcode = true;
   });
   if (badcode) throw Error(DCNS_ERR_INVALID, "sequence codes must be dCNS codes 0..4 (A C N G T)");
@@ -1109,6 +1123,8 @@ void run_xdrop_rounds(Context &C, std::vector<XTask> &X, const Params &P, bool w
         X[k].w *= 2;  // the reference restarts the whole pass with twice the band (:1272-1276)
         next.push_back(k);
       } else if (Xc[q].status == 2) {
+        if (rows_cap[k] >= X[k].n1)  // a whole-pass slot did not fit its capacity field
+          throw Error(DCNS_ERR_NOMEM, "x-drop traceback slot larger than 2^31 words");
         rows_cap[k] = X[k].n1;
         next.push_back(k);
       } else {
@@ -1178,7 +1194,7 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
   if (flat) flat->clear();
   if (hoff) hoff->assign(n, -1);
   const int w0 = X[0].w;
-  int64_t maxdim = 1, tb_words = 1 << 20, cig_words = 1;
+  int64_t maxdim = 1, max_n1 = 1, tb_words = 1 << 20, cig_words = 1;
   bool uniform = w0 >= 1;
   for (int64_t k = 0; k < n; ++k) {
     XTask &T = X[k];
@@ -1188,10 +1204,26 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
     T.score = T.end1 = T.end2 = T.rows = 0;
     T.iii = T.jjj = T.ncig = 0;
     maxdim = std::max<int64_t>(maxdim, std::max(T.n1, T.n2));
-    if (want_codes) {
-      tb_words += 3 * std::min<int64_t>(T.n1, 1024) * wpr_of(w0);
-      cig_words += (int64_t)std::max(T.n1, 0) + std::max(T.n2, 0) + 2;
-    }
+    max_n1 = std::max<int64_t>(max_n1, T.n1);
+    if (want_codes) cig_words += (int64_t)std::max(T.n1, 0) + std::max(T.n2, 0) + 2;
+  }
+  // Traceback slots of min(n1, slot_rows) rows, the arena sized for three slots per pass (a band restart takes a new
+  // slot of twice the width): slot_rows is the longest pass when that arena fits a quarter of the free device budget
+  // (no pass then outgrows its slot), else halved down to 1,024 (longer passes are retried with whole-pass slots).
+  int slot_rows = 1024;
+  if (want_codes) {
+    auto words_for = [&](int64_t rows) {
+      int64_t wsum = 1 << 20;
+      for (int64_t k = 0; k < n; ++k) wsum += 3 * std::min<int64_t>(X[k].n1, rows) * wpr_of(w0);
+      return wsum;
+    };
+    const int64_t room = (int64_t)((C.budget > C.used ? C.budget - C.used : 0) / 4);
+    for (int64_t rows = max_n1; rows > 1024; rows /= 2)
+      if ((int64_t)sizeof(uint32_t) * words_for(rows) <= room) {
+        slot_rows = (int)std::min<int64_t>(rows, INT32_MAX / 64);
+        break;
+      }
+    tb_words = words_for(slot_rows);
   }
   auto tp = phase(C, "xc_setup", t0);
   if (!uniform || n >= INT32_MAX / 4) {
@@ -1240,12 +1272,13 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
     for (int L = 0; L < nlev; ++L) {
       const int out = 1 - in;
       DCNS_CK(cudaMemsetAsync(cnt + out, 0, sizeof(int), C.st));
-      const XHandoff H{long_list, cnt + 4 + nlev + L, C.d_spill.as<int32_t>(), spill_cap, C.xdrop_handoff};
+      const XHandoff H{long_list, cnt + 4 + nlev + L, C.d_spill.as<int32_t>(), spill_cap, C.xdrop_handoff,
+                       C.xdrop_resume_lanes};
       launched += launch_xdrop_level(C.d_x.as<XTask>(), lists + in * n, cnt + in, lists + out * n, cnt + out,
-                                     lists + 2 * n, cnt + 2, cur, want_codes ? tb_words : 0, cnt + 4 + L, H, C.arena, P,
-                                     C.d_tb.as<uint32_t>(), w0 << L, (int)n, C.nsm, C.d_scratch.as<int32_t>(),
-                                     per_warp[L], warps[L], C.xdrop_warp_from, C.xdrop_wave_max_w, C.xdrop_flat,
-                                     C.st);
+                                     lists + 2 * n, cnt + 2, cur, want_codes ? tb_words : 0, slot_rows, cnt + 4 + L, H,
+                                     C.arena, P, C.d_tb.as<uint32_t>(), w0 << L, (int)n, C.nsm,
+                                     C.d_scratch.as<int32_t>(), per_warp[L], warps[L], C.xdrop_warp_from,
+                                     C.xdrop_wave_max_w, C.xdrop_flat, C.st);
       in = out;
     }
     DCNS_CK(cudaEventRecord(C.ev1, C.st));
@@ -2076,10 +2109,10 @@ void autotune(Context &C, Batch &B, const Params &P, int mode) {
   // each candidate applied to every bin; the bins differ in how many long and wide-band passes they hold.
   C.bin_tune.clear();
   if (C.max_lanes > 1 && (int64_t)B.lens.size() >= 4096) {
-    const int h = C.xdrop_handoff;
-    const Context::BinTune cands[] = {{20, 256, true, h},  {20, 256, false, 0}, {10, 256, true, h},
-                                      {20, 256, true, 0},  {20, 256, true, 48}, {20, 256, true, 192},
-                                      {20, 128, true, h}};
+    const int h = C.xdrop_handoff, g = C.xdrop_resume_lanes;
+    const Context::BinTune cands[] = {{20, 256, true, h, g},   {20, 256, false, 0, g}, {10, 256, true, h, g},
+                                      {20, 256, true, 0, g},   {20, 256, true, 48, g}, {20, 256, true, 192, g},
+                                      {20, 256, true, 48, 32}, {20, 256, true, 96, 32}, {20, 128, true, h, g}};
     const int nb = std::max(C.bins, C.max_lanes);
     std::vector<double> best_ms(nb, 1e300);
     std::vector<Context::BinTune> choice(nb, cands[0]);
@@ -2225,9 +2258,9 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
         const Context::BinTune bt = b < (int)C.bin_tune.size()
                                         ? C.bin_tune[b]
                                         : Context::BinTune{C.xdrop_warp_from, C.xdrop_wave_max_w, C.xdrop_flat,
-                                                           C.xdrop_handoff};
+                                                           C.xdrop_handoff, C.xdrop_resume_lanes};
         L.xdrop_warp_from = bt.xdrop_warp_from, L.xdrop_wave_max_w = bt.xdrop_wave_max_w, L.xdrop_flat = bt.xdrop_flat;
-        L.xdrop_handoff = bt.xdrop_handoff;
+        L.xdrop_handoff = bt.xdrop_handoff, L.xdrop_resume_lanes = bt.xdrop_resume_lanes;
         L.sg_warps = C.sg_warps;
         L.sg_flow = C.sg_flow;
         L.scan_tiles_per_thread = C.scan_tiles_per_thread;

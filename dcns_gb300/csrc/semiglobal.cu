@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Ar
     const bool live = i0 <= n1_eff;
     // per row of the lane: band [c0, c0 + span] (rows past the DP: an empty band), its base, the stale-column role,
     // running states
-    int ci[kSgR], c0[kSgR], span[kSgR], e1[kSgR], e2[kSgR], best[kSgR], bestj[kSgR], prevM[kSgR];
+    int ci[kSgR], rmask[kSgR], c0[kSgR], span[kSgR], e1[kSgR], e2[kSgR], best[kSgR], bestj[kSgR], prevM[kSgR];
     int stale_rows = 0;  // bit k: row k is row r_last (bit 4 + k: row r_last - 1)
 #pragma unroll
     for (int k = 0; k < kSgR; ++k) {
@@ -468,6 +468,7 @@ __global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Ar
       c0[k] = lv ? max(i - w, 1) : INT_MAX / 2;
       span[k] = lv ? min(i + w, n2) - c0[k] : 0;
       ci[k] = lv ? s1.at(ar, i - 1) : 0;
+      rmask[k] = ci[k] == 2 ? 0 : -1;  // Scorei: an N row scores 0 against every base
       if (lv && i == r_last) stale_rows |= 1 << k;
       if (lv && i == r_last - 1) stale_rows |= 16 << k;
       e1[k] = kOut, e2[k] = kOut, best[k] = 0, bestj[k] = 0, prevM[k] = kOut;
@@ -505,58 +506,65 @@ __global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Ar
     stage_chunk(1);
     __syncwarp();
     int outM = kOut, outF1 = kOut, outF2 = kOut, outC = 0;
-    for (int t = 0; t < nsteps && abandon == 0; ++t) {
-      int upM = __shfl_up_sync(0xFFFFFFFFu, outM, 1);
-      int upF1 = __shfl_up_sync(0xFFFFFFFFu, outF1, 1);
-      int upF2 = __shfl_up_sync(0xFFFFFFFFu, outF2, 1);
-      int cj = __shfl_up_sync(0xFFFFFFFFu, outC, 1);
-      if ((t & 31) == 0 && t > 0) {
+    const bool lane0 = lane == 0, write_bnd = lane == 31 && produce;
+    for (int tc = 0; tc < nsteps && abandon == 0; tc += 32) {  // 32-step chunks
+      if (tc > 0) {
         // chunk boundary: publish the columns of this stripe's last row written so far, stop early if the DP
         // ended, stage the chunk two ahead of lane 0's reads
-        if (lane == 31 && produce) sg_st_release(prog_self, jstart + t - 32);
+        if (write_bnd) sg_st_release(prog_self, jstart + tc - 32);
         if (__any_sync(0xFFFFFFFFu, sg_ld_relaxed(&D.stop) != 0)) {
           abandon = 1;
           break;
         }
         __syncwarp();
-        stage_chunk((t >> 5) + 1);
+        stage_chunk((tc >> 5) + 1);
         if (abandon != 0) break;
       }
-      const int j = jstart + t - lane;
-      if (lane == 0) {
-        const SgRec r = stage[warp][(t >> 5) & 1][t & 31];
-        upM = r.m, upF1 = r.f1, upF2 = r.f2;
-        cj = stage_c[warp][(t >> 5) & 1][t & 31];
-      }
-      int aF1 = upF1, aF2 = upF2, dg = diag;
-      uint32_t word = 0;
-      const int mt = cj == 2 ? 0 : P.match, mm = cj == 2 ? 0 : P.mismatch;  // Scorei: N scores 0
-#pragma unroll
-      for (int k = 0; k < kSgR; ++k) {
-        const int dj = j - c0[k];
-        const bool valid = (unsigned)dj <= (unsigned)span[k];
-        const bool last = dj == span[k];
-        const int sc = ci[k] == 2 ? 0 : (ci[k] == cj ? mt : mm);
-        int cF1, cF2;
-        uint32_t d = 0;
-        const int cM = sg_cell<CODES>(sc, dg, aF1, aF2, e1[k], e2[k], valid, last, o1, x1, o2, x2, cF1, cF2, &d);
-        if (CODES) word |= d << (8 * k);
-        bool keep;
-        best[k] = __vibmax_s32(best[k], cM, &keep);  // keep: !(cM > best), the first maximum of the row stays
-        bestj[k] = keep ? bestj[k] : j;
-        if (stale_rows && j == n2 - 1 && valid) {
-          if ((stale_rows >> k) & 1) D.stale_last = cM;
-          if ((stale_rows >> (4 + k)) & 1) D.stale_prev = cM;
+      const SgRec *const srow = stage[warp][(tc >> 5) & 1];
+      const int *const scol = stage_c[warp][(tc >> 5) & 1];
+      const int tend = min(tc + 32, nsteps);
+      for (int t = tc; t < tend; ++t) {
+        int upM = __shfl_up_sync(0xFFFFFFFFu, outM, 1);
+        int upF1 = __shfl_up_sync(0xFFFFFFFFu, outF1, 1);
+        int upF2 = __shfl_up_sync(0xFFFFFFFFu, outF2, 1);
+        int cj = __shfl_up_sync(0xFFFFFFFFu, outC, 1);
+        const int j = jstart + t - lane;
+        if (lane0) {
+          const SgRec r = srow[t - tc];
+          upM = r.m, upF1 = r.f1, upF2 = r.f2;
+          cj = scol[t - tc];
         }
-        if (k == kSgR - 1 && lane == 31 && produce && valid) brow[j] = SgRec{cM, cF1, cF2};
-        dg = prevM[k];  // row k at column j - 1: the diagonal of row k + 1
-        prevM[k] = cM;
-        aF1 = cF1, aF2 = cF2;
-        if (k == kSgR - 1) outM = cM;
+        int aF1 = upF1, aF2 = upF2, dg = diag;
+        uint32_t word = 0;
+        const int mt = cj == 2 ? 0 : P.match, mm = cj == 2 ? 0 : P.mismatch;  // Scorei: N scores 0
+        const bool stale_col = stale_rows != 0 && j == n2 - 1;
+#pragma unroll
+        for (int k = 0; k < kSgR; ++k) {
+          const int dj = j - c0[k];
+          const bool valid = (unsigned)dj <= (unsigned)span[k];
+          const bool last = dj == span[k];
+          const int sc = (ci[k] == cj ? mt : mm) & rmask[k];
+          int cF1, cF2;
+          uint32_t d = 0;
+          const int cM = sg_cell<CODES>(sc, dg, aF1, aF2, e1[k], e2[k], valid, last, o1, x1, o2, x2, cF1, cF2, &d);
+          if (CODES) word |= d << (8 * k);
+          bool keep;
+          best[k] = __vibmax_s32(best[k], cM, &keep);  // keep: !(cM > best), the first maximum of the row stays
+          bestj[k] = keep ? bestj[k] : j;
+          if (stale_col && valid) {
+            if ((stale_rows >> k) & 1) D.stale_last = cM;
+            if ((stale_rows >> (4 + k)) & 1) D.stale_prev = cM;
+          }
+          if (k == kSgR - 1 && write_bnd && valid) brow[j] = SgRec{cM, cF1, cF2};
+          dg = prevM[k];  // row k at column j - 1: the diagonal of row k + 1
+          prevM[k] = cM;
+          aF1 = cF1, aF2 = cF2;
+          if (k == kSgR - 1) outM = cM;
+        }
+        if (CODES && live) trow[(int64_t)t * 32 + lane] = word;
+        diag = upM;
+        outF1 = aF1, outF2 = aF2, outC = cj;
       }
-      if (CODES && live) trow[(int64_t)t * 32 + lane] = word;
-      diag = upM;
-      outF1 = aF1, outF2 = aF2, outC = cj;
     }
     __syncwarp();
     if (lane == 31) sg_st_release(prog_self, INT_MAX);  // every column written (or abandoned): release the consumer

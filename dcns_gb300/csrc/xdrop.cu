@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(128) xdrop_warp_kernel(XTask *__restrict__ tas
 // kernel reads its work list and count from device memory, appends the passes that must restart (band edge touched;
 // band doubled here, as the reference does) to the next level's list, and the passes whose traceback slot did not fit
 // to the retry list; the host enqueues every level at once and synchronises once.  Traceback slots (reverse passes)
-// are taken from an arena by atomic add: min(n1, 1024) rows of the pass's band.
+// are taken from an arena by atomic add: min(n1, slot_rows) rows of the pass's band.
 struct XLevelArgs {
   XTask *tasks;
   const int *list_in;
@@ -520,11 +520,14 @@ struct XLevelArgs {
   int *long_list, *long_count;
   int32_t *spill;
   int spill_cap, spill_half, handoff_rows;
+  int level_w;    // the level's band half-width (every pass of a level has it)
+  int slot_rows;  // rows of a traceback slot: min(n1, slot_rows)
 };
 
 __device__ __forceinline__ bool xd_take_slot(XTask &T, const XLevelArgs &L) {
-  const int64_t rows = min(T.n1, 1024);
+  const int64_t rows = min(T.n1, L.slot_rows);
   const int64_t words = max((int64_t)1, rows * xd_words_per_row(T.w));
+  if (words > INT32_MAX) return false;  // the capacity is an int: such a pass is retried with a whole-pass slot
   const unsigned long long off = atomicAdd(L.tb_cursor, (unsigned long long)words);
   if ((int64_t)off + words > L.tb_words) return false;
   T.tb_off = (int64_t)off;
@@ -854,6 +857,162 @@ __global__ void __launch_bounds__(128) xdrop_level_resume_kernel(XLevelArgs L, A
   }
 }
 
+// The same passes on G-lane groups (32 / G passes per warp), each group a wavefront over G-row stripes: lane g of a
+// group owns row r0 + g and computes band cell k = t - 2g at step t, with the cell above and the diagonal from lane
+// g - 1 (__shfl_up_sync within the group); lane 0 of the group reads the row above the stripe from the group's
+// boundary row in shared memory, which lane G - 1 rewrites (index k at step k + 2(G - 1), after lane 0 read it).
+// A G-row stripe is 2w + 1 + 2(G - 1) steps, so fewer lanes idle in the skew than with a 32-row stripe at bands
+// 10-20 (G = 8: 75 % of lane-steps compute a cell at band 20, against 40 % for one warp per pass); every group runs
+// its stripes in step with the warp (all passes of a level have the same band), evaluates its rows in order after
+// each stripe, and takes its next pass (list index + the grid's group count) when its pass ends.
+template <int G>
+__global__ void __launch_bounds__(128) xdrop_level_resume_group_kernel(XLevelArgs L, Arena ar, Params P,
+                                                                       uint32_t *__restrict__ tb) {
+  constexpr int NG = 32 / G;
+  __shared__ int32_t sM[4][NG][2 * kXrMaxW + 2], sF[4][NG][2 * kXrMaxW + 2];
+  const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5, g = lane / G, gl = lane % G;
+  const int n = min(*L.long_count, L.spill_cap);
+  const int ngroups = (int)((gridDim.x * blockDim.x) / G);
+  const int w = L.level_w, nk = 2 * w + 1, wpr = xd_words_per_row(w), nsteps = nk + 2 * (G - 1);
+  const int open = P.open1, ext = P.ext1;
+  int32_t *const bM = sM[wb][g], *const bF = sF[wb][g];
+  int q = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G);  // the group's list index
+  // the group's pass (the same values in every lane of the group)
+  bool active = false, codes = false;
+  XTask *T = nullptr;
+  int id = 0, n1 = 0, n2 = 0, cap = 0, score = 0, e1 = 0, e2 = 0, rows = 0, r0 = 1;
+  int64_t off = 0;
+  SeqView s1{0, 0, 0}, s2{0, 0, 0};
+  auto begin = [&]() {  // list entry q into the group: its spilled band (the row before r0) and running state
+    active = q < n;
+    if (!active) return;
+    id = L.long_list[q];
+    T = &L.tasks[id];
+    const int32_t *sp = L.spill + (int64_t)q * 2 * L.spill_half;
+    n1 = T->n1, n2 = T->n2, codes = T->want_codes != 0, off = T->tb_off, cap = T->tb_cap;
+    s1 = SeqView{T->base1, T->a1, T->dir}, s2 = SeqView{T->base2, T->a2, T->dir};
+    score = T->score, e1 = T->end1, e2 = T->end2, rows = T->rows, r0 = rows + 1;
+    for (int k = gl; k <= nk; k += G) bM[k] = sp[k], bF[k] = sp[L.spill_half + k];
+  };
+  begin();
+  __syncwarp();
+  while (__any_sync(0xFFFFFFFFu, active)) {
+    const int i = r0 + gl;
+    const bool live = active && i <= n1;
+    const int c0 = max(i - w, 1), c1 = min(i + w, n2);
+    const int ci = live ? s1.at(ar, i - 1) : 0;
+    const bool wcode = codes && live && (int64_t)i * wpr <= cap;  // rows past the slot are never kept
+    uint32_t *row_codes = tb + off + (int64_t)(i - 1) * wpr;
+    int e = kOut, best = 0, bestj = -1, outM = kOut, outF = kOut, outC = 0, prevUp = kOut, kw = 0;
+    uint32_t cw = 0;
+    for (int t = 0; t < nsteps; ++t) {
+      const int upM = __shfl_up_sync(0xFFFFFFFFu, outM, 1, G);
+      int upF = __shfl_up_sync(0xFFFFFFFFu, outF, 1, G);
+      int cj = __shfl_up_sync(0xFFFFFFFFu, outC, 1, G);
+      const int k = t - 2 * gl, j = i - w + k;
+      int diagv = prevUp;
+      if (gl == 0) {
+        diagv = (active && k >= 0 && k < nk) ? bM[k] : kOut;
+        upF = (active && k >= 0 && k + 1 <= nk) ? bF[k + 1] : kOut;
+        cj = (active && j >= 1 && j <= n2) ? s2.at(ar, j - 1) : 0;
+      }
+      int nM = kOut, nF = kOut;
+      if (k >= 0 && k < nk) {
+        uint32_t nib = 0xFu;
+        if (live && j >= c0 && j <= c1) {
+          const int32_t diag = (j == 1) ? (i == 1 ? 0 : kOut) : diagv;
+          const int32_t fin = (j == c1) ? kOut : upF;
+          int32_t v = score_of(ci, cj, P.match, P.mismatch) + diag;
+          uint32_t d = v > fin ? 0u : 1u;
+          if (!(v > fin)) v = fin;
+          if (!(v > e)) {
+            d = 2u;
+            v = e;
+          }
+          if (v > best) {
+            best = v;
+            bestj = j;
+          }
+          const int32_t h = v + open;
+          const int32_t f = fin + ext;
+          if (f >= h) d |= 4u;
+          nM = v;
+          nF = f >= h ? f : h;
+          e += ext;
+          if (e >= h) d |= 8u;
+          e = e >= h ? e : h;
+          nib = d;
+          if (gl == G - 1) {
+            bM[k] = nM;
+            bF[k] = nF;
+          }
+        }
+        if (wcode) {
+          cw |= nib << (4 * (k & 7));
+          if ((k & 7) == 7 || k == nk - 1) {
+            row_codes[kw++] = cw;
+            cw = 0;
+          }
+        }
+      }
+      prevUp = upM;
+      outM = nM;
+      outF = nF;
+      outC = cj;
+    }
+    __syncwarp();
+    // the stripe's rows in order (every lane of a group keeps the same state)
+    bool stop = false;
+    int status = 0;
+    for (int rr = 0; rr < G; ++rr) {
+      const int src = (lane & ~(G - 1)) + rr;
+      const int tm = __shfl_sync(0xFFFFFFFFu, best, src), tj = __shfl_sync(0xFFFFFFFFu, bestj, src);
+      if (!active || stop) continue;
+      const int ii = r0 + rr;
+      if (ii > n1) {
+        stop = true;
+        continue;
+      }
+      if (codes && (int64_t)ii * wpr > cap) {
+        status = 2;
+        stop = true;
+        continue;
+      }
+      rows = ii;
+      const int cc0 = max(ii - w, 1), cc1 = min(ii + w, n2);
+      if (tj != n2 && tj != 1 && (tj == cc0 || tj == cc1)) {
+        status = 1;
+        stop = true;
+        continue;
+      }
+      if (tm > score) {
+        score = tm;
+        e1 = ii;
+        e2 = tj;
+      }
+      if (score - tm > P.xdrop || tm <= 0) stop = true;
+    }
+    if (active) {
+      r0 += G;
+      if (stop || r0 > n1) {  // the pass ended: its result, its route, then the group's next pass
+        if (gl == 0) {
+          T->status = status;
+          T->rows = rows;
+          if (status == 0) {
+            T->score = score;
+            T->end1 = e1;
+            T->end2 = e2;
+          }
+          xd_route(*T, id, L);
+        }
+        q += ngroups;
+        begin();
+      }
+    }
+    __syncwarp();
+  }
+}
+
 __global__ void xdrop_iota_kernel(int *list, int n, int *count) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) list[k] = k;
@@ -908,8 +1067,8 @@ int flat_blocks_per_sm() {
 }
 
 int launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
-                       int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int *fetch,
-                       const XHandoff &H, Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm,
+                       int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int slot_rows,
+                       int *fetch, const XHandoff &H, Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm,
                        int32_t *scratch, int64_t per_warp, int warps, int warp_from, int wave_max_w, bool flat,
                        cudaStream_t st) {
   if (n_bound <= 0) return 0;
@@ -917,7 +1076,7 @@ int launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, in
   const bool handoff = flat_level && H.rows > 0 && H.cap > 0;
   XLevelArgs L{tasks, list_in, count_in, list_out, count_out, retry, retry_count, tb_cursor, tb_words, fetch,
                H.list, H.count, H.spill, handoff ? H.cap : 0, w <= 10 ? XBand<10>::NA : XBand<20>::NA,
-               handoff ? H.rows : 0};
+               handoff ? H.rows : 0, w, slot_rows};
   const int g = (int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * 16);
   if (flat_level) {  // register band, row-interleaved: one resident wave of blocks, then the handed-off passes
     if (w <= 10)
@@ -927,8 +1086,15 @@ int launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, in
       xdrop_level_flat_kernel<20><<<(int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * flat_blocks_per_sm<20>()),
                                     128, 0, st>>>(L, ar, p, tb);
     if (!handoff) return 1;
-    xdrop_level_resume_kernel<<<(int)std::min<int64_t>((H.cap + 3) / 4, (int64_t)nsm * 16), 128, 0, st>>>(L, ar, p,
-                                                                                                         tb);
+    if (H.lanes == 8)
+      xdrop_level_resume_group_kernel<8>
+          <<<(int)std::min<int64_t>((H.cap + 15) / 16, (int64_t)nsm * 16), 128, 0, st>>>(L, ar, p, tb);
+    else if (H.lanes == 16)
+      xdrop_level_resume_group_kernel<16>
+          <<<(int)std::min<int64_t>((H.cap + 7) / 8, (int64_t)nsm * 16), 128, 0, st>>>(L, ar, p, tb);
+    else
+      xdrop_level_resume_kernel<<<(int)std::min<int64_t>((H.cap + 3) / 4, (int64_t)nsm * 16), 128, 0, st>>>(L, ar, p,
+                                                                                                           tb);
     return 2;
   }
   if (w > warp_from && w <= wave_max_w && w <= kXwMaxW)  // wide bands up to 256: the wavefront

@@ -184,8 +184,8 @@ int dcns_autotune(dcns_ctx *ctx, dcns_batch *batch, const dcns_params *params, i
 
 /* The context's kernel shapes (no counterpart in the reference): what dcns_autotune chose, or the defaults and the
  * DCNS_* environment settings.  Per bin (at most 16 reported): the x-drop band from which passes run one warp each,
- * the widest band of the one-warp wavefront form, whether the register-band levels run row-interleaved, and the rows
- * after which a register-band pass moves to the wavefront form (0: never). */
+ * the widest band of the one-warp wavefront form, whether the register-band levels run row-interleaved, the rows
+ * after which a register-band pass moves to the wavefront form (0: never), and the lanes per such pass (8, 16, 32). */
 typedef struct {
   int32_t lanes, bins;
   double bin_ratio;
@@ -194,7 +194,7 @@ typedef struct {
                                      else eight) */
   int32_t sg_flow;                /* 1: 2-piece DPs run as a flow of 128-row stripe units over one persistent grid */
   int32_t n_bins_tuned;           /* bins with their own x-drop forms below (0: every bin uses bin 0's values) */
-  int32_t xdrop_warp_from[16], xdrop_wave_max_w[16], xdrop_flat[16], xdrop_handoff[16];
+  int32_t xdrop_warp_from[16], xdrop_wave_max_w[16], xdrop_flat[16], xdrop_handoff[16], xdrop_resume_lanes[16];
 } dcns_tuning;
 int dcns_get_tuning(const dcns_ctx *ctx, dcns_tuning *out);
 
