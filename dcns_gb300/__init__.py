@@ -138,7 +138,8 @@ class ServingStats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("lanes", C.c_int32), ("bins", C.c_int32), ("bin_ratio", C.c_double),
-                ("scan_tiles_per_thread", C.c_int32), ("sg_warps", C.c_int32), ("sg_flow", C.c_int32),
+                ("scan_tiles_per_thread", C.c_int32), ("sg_warps", C.c_int32), ("sg_flow", C.c_int32), ("sg_flow_blocks", C.c_int32),
+                ("bins_by_size", C.c_int32),
                 ("n_bins_tuned", C.c_int32),
                 ("xdrop_warp_from", C.c_int32 * 16), ("xdrop_wave_max_w", C.c_int32 * 16), ("xdrop_flat", C.c_int32 * 16),
                 ("xdrop_handoff", C.c_int32 * 16), ("xdrop_resume_lanes", C.c_int32 * 16)]
@@ -147,7 +148,8 @@ class Tuning(C.Structure):
         n = max(self.n_bins_tuned, 1)
         return {"lanes": self.lanes, "bins": self.bins, "bin_ratio": self.bin_ratio,
                 "scan_tiles_per_thread": self.scan_tiles_per_thread, "sg_warps": self.sg_warps,
-                "sg_flow": bool(self.sg_flow),
+                "sg_flow": bool(self.sg_flow), "sg_flow_blocks": self.sg_flow_blocks,
+                "bins_by_size": bool(self.bins_by_size),
                 "xdrop_per_bin": [{"warp_from": self.xdrop_warp_from[b], "wave_max_w": self.xdrop_wave_max_w[b],
                                    "row_interleaved": bool(self.xdrop_flat[b]),
                                    "handoff_rows": self.xdrop_handoff[b],

@@ -484,6 +484,8 @@ int dcns_get_tuning(const dcns_ctx *ctx, dcns_tuning *out) {
   out->scan_tiles_per_thread = C.scan_tiles_per_thread;
   out->sg_warps = C.sg_warps;
   out->sg_flow = C.sg_flow ? 1 : 0;
+  out->sg_flow_blocks = C.sg_flow_blocks;
+  out->bins_by_size = C.bins_by_size ? 1 : 0;
   out->n_bins_tuned = (int32_t)std::min<size_t>(C.bin_tune.size(), 16);
   for (int b = 0; b < 16; ++b) {
     const bool own = b < (int)C.bin_tune.size();

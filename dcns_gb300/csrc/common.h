@@ -218,9 +218,11 @@ void launch_semiglobal(SgTask *tasks, const int *idx, int n, Arena ar, Params p,
                        int max_n2, int *work_counter, int grid, int nw, cudaStream_t st);
 int sg_ctas_per_sm(int nw);
 // codes: the DPs keep direction codes (every DP of a launch alike)
-void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, bool codes, int nsm, cudaStream_t st);
+// minb: 5 or 6 resident blocks per SM (the register budget of the kernel instantiation)
+void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, bool codes, int nsm, int minb,
+                            cudaStream_t st);
 int64_t sg_flow_units(int n1, int n2, int w);  // stripe units of one DP in the flow form (at least 1)
-int64_t sg_flow_grid_warps(int nsm);           // warps of the flow kernel's persistent grid
+int64_t sg_flow_grid_warps(int nsm, int minb);  // warps of the flow kernel's persistent grid
 int64_t sg_bnd_bytes(int grid, int max_n2, int nw);
 // tb_bytes: size of the code store tb (the traceback reads nothing past it)
 void launch_sg_traceback(SgTask *tasks, const int *idx, int n, int bandwidth, const uint8_t *tb, int64_t tb_bytes,

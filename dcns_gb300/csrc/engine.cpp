@@ -160,7 +160,9 @@ void init_context(Context &C, int device, size_t budget) {
   if (const char *e = std::getenv("DCNS_SG_FLOW")) {
     C.sg_flow = std::atoi(e) != 0;
   }
-  if (const char *e = std::getenv("DCNS_BIN_RATIO")) C.bin_ratio = std::max(0.1, std::min(1.0, std::atof(e)));
+  if (const char *e = std::getenv("DCNS_SG_FLOW_BLOCKS")) C.sg_flow_blocks = std::atoi(e) == 6 ? 6 : 5;
+  if (const char *e = std::getenv("DCNS_BIN_RATIO")) C.bin_ratio = std::max(0.1, std::min(4.0, std::atof(e)));
+  if (const char *e = std::getenv("DCNS_BINS_BY_SIZE")) C.bins_by_size = std::atoi(e) != 0;
 }
 
 Params to_params(const dcns_params *p) {
@@ -313,8 +315,8 @@ class HostPool {
 };
 thread_local bool HostPool::in_worker = false;
 
-void parallel_for(int64_t n, const std::function<void(int64_t)> &f) {
-  if (n < 64 || HostPool::in_worker || std::thread::hardware_concurrency() <= 1) {
+void parallel_for(int64_t n, const std::function<void(int64_t)> &f, int64_t min_items = 64) {
+  if (n < min_items || n < 2 || HostPool::in_worker || std::thread::hardware_concurrency() <= 1) {
     for (int64_t i = 0; i < n; ++i) f(i);
     return;
   }
@@ -882,23 +884,23 @@ void link_seeds(SeedSet &seeds) {  // :288-344
   while (changed) {
     changed = false;
     std::vector<Seed4> next;
-    std::set<int> used;
     const int n = (int)cur.size();
+    std::vector<uint8_t> used((size_t)n, 0);  // the reference's usedList
     for (int i = 0; i < n; ++i) {
-      if (used.count(i)) continue;
+      if (used[i]) continue;
       const Seed4 a = cur[i];
       bool merged = false;
       for (int j = i + 1; j < n; ++j) {
-        if (used.count(j)) continue;
+        if (used[j]) continue;
         const Seed4 b = cur[j];
         if (a.s2 <= b.s2 && a.e1 >= b.e1 && a.e2 >= b.e2) {
-          used.insert(j);
+          used[j] = 1;
         } else if (a.s2 <= b.s2 && a.e1 <= b.e1 && a.e2 <= b.e2) {
           const int32_t d = b.s1 - a.s1;
           if (d == b.s2 - a.s2 && d == b.e1 - a.e1 && d == b.e2 - a.e2) {
             next.push_back(Seed4{a.s1, b.e1, a.s2, b.e2});
-            used.insert(i);
-            used.insert(j);
+            used[i] = 1;
+            used[j] = 1;
             merged = true;
             break;
           }
@@ -990,10 +992,13 @@ void scan_and_link(Context &C, const std::vector<PairIn> &pairs, const Params &P
   C.stats.tasks_scan_speculative += (S.size() - S.ns) - visited_final;
   auto t0 = Clock::now();
   linked.assign(np, {});
-  parallel_for(np, [&](int64_t p) {
-    link_seeds(sets[p]);
-    linked[p].assign(sets[p].begin(), sets[p].end());
-  });
+  parallel_for(
+      np,
+      [&](int64_t p) {
+        link_seeds(sets[p]);
+        linked[p].assign(sets[p].begin(), sets[p].end());
+      },
+      2);  // a pair of long sequences holds thousands of seeds: spread even a few pairs over the pool
   C.stats.ms_link += ms_since(t0);
 }
 
@@ -1208,8 +1213,9 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
     if (want_codes) cig_words += (int64_t)std::max(T.n1, 0) + std::max(T.n2, 0) + 2;
   }
   // Traceback slots of min(n1, slot_rows) rows, the arena sized for three slots per pass (a band restart takes a new
-  // slot of twice the width): slot_rows is the longest pass when that arena fits a quarter of the free device budget
-  // (no pass then outgrows its slot), else halved down to 1,024 (longer passes are retried with whole-pass slots).
+  // slot of twice the width).  A slot is reserved for the pass's bound n1, not for the rows it will use, so slot_rows
+  // stays at 1,024-2,048: the longest pass up to 2,048 rows when that arena fits a quarter of the free device budget
+  // (passes longer than their slot are retried with whole-pass slots).
   int slot_rows = 1024;
   if (want_codes) {
     auto words_for = [&](int64_t rows) {
@@ -1218,11 +1224,8 @@ void run_xdrop(Context &C, std::vector<XTask> &X, const Params &P, bool want_cod
       return wsum;
     };
     const int64_t room = (int64_t)((C.budget > C.used ? C.budget - C.used : 0) / 4);
-    for (int64_t rows = max_n1; rows > 1024; rows /= 2)
-      if ((int64_t)sizeof(uint32_t) * words_for(rows) <= room) {
-        slot_rows = (int)std::min<int64_t>(rows, INT32_MAX / 64);
-        break;
-      }
+    const int64_t want = std::min<int64_t>(max_n1, 2048);
+    if (want > 1024 && (int64_t)sizeof(uint32_t) * words_for(want) <= room) slot_rows = (int)want;
     tb_words = words_for(slot_rows);
   }
   auto tp = phase(C, "xc_setup", t0);
@@ -1522,7 +1525,7 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
       }
       // hand-out order: stripe-major within groups of consecutive DPs holding at least eight grid-fulls of units;
       // inside a group the DPs go by stripe count, most first, so the DPs that have a stripe s form a prefix
-      const int64_t group_units = 8 * sg_flow_grid_warps(C.nsm);
+      const int64_t group_units = 8 * sg_flow_grid_warps(C.nsm, C.sg_flow_blocks);
       std::vector<int2> order((size_t)units);
       {
         int64_t u = 0;
@@ -1570,7 +1573,7 @@ void run_semiglobal(Context &C, std::vector<SgTask> &G, const Params &P, bool wa
       launch_semiglobal_weighted(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, *W,
                                  C.d_sgtb.as<uint8_t>(), C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, C.st);
     else if (flow)
-      launch_semiglobal_flow(F, C.arena, P, C.d_sgtb.as<uint8_t>(), want_codes, C.nsm, C.st);
+      launch_semiglobal_flow(F, C.arena, P, C.d_sgtb.as<uint8_t>(), want_codes, C.nsm, C.sg_flow_blocks, C.st);
     else
       launch_semiglobal(C.d_sg.as<SgTask>(), C.d_idx.as<int>(), (int)m, C.arena, P, C.d_sgtb.as<uint8_t>(),
                         C.d_bnd.p, maxn2, C.d_counter.as<int>(), grid, nw, C.st);
@@ -2079,16 +2082,18 @@ void autotune(Context &C, Batch &B, const Params &P, int mode) {
   struct Shape {
     int lanes, bins;
     double ratio;
+    bool by_size;
   };
   auto run = [&](const Shape &sh) {
-    C.max_lanes = sh.lanes, C.bins = sh.bins, C.bin_ratio = sh.ratio;
+    C.max_lanes = sh.lanes, C.bins = sh.bins, C.bin_ratio = sh.ratio, C.bins_by_size = sh.by_size;
     std::vector<std::vector<FragOut>> out;
     const auto t0 = Clock::now();
     align_batch(C, B, P, mode, out);
     return ms_since(t0);
   };
-  const Shape first[] = {{1, 1, 0.6}, {2, 2, 0.6}, {3, 3, 0.6}, {4, 4, 0.6}, {4, 6, 0.6}, {6, 6, 0.6}};
-  run(Shape{C.max_lanes, C.bins, C.bin_ratio});  // warm: buffers of the current shape
+  const Shape first[] = {{1, 1, 0.6, false}, {2, 2, 0.6, false}, {3, 3, 0.6, false},
+                         {4, 4, 0.6, false}, {4, 6, 0.6, false}, {6, 6, 0.6, false}};
+  run(Shape{C.max_lanes, C.bins, C.bin_ratio, C.bins_by_size});  // warm: buffers of the current shape
   Shape best = first[0];
   double best_ms = 1e300;
   for (const Shape &sh : first) {
@@ -2096,12 +2101,14 @@ void autotune(Context &C, Batch &B, const Params &P, int mode) {
     const double ms = std::min(run(sh), run(sh));
     if (ms < best_ms) best_ms = ms, best = sh;
   }
-  for (double r : {0.45, 0.75}) {
-    const Shape sh{best.lanes, best.bins, r};
+  // the bin shares, and bins by size (the largest pairs last) against mixed bins
+  for (const Shape sh : {Shape{best.lanes, best.bins, 0.45, false}, Shape{best.lanes, best.bins, 0.75, false},
+                         Shape{best.lanes, best.bins, 0.6, true}, Shape{best.lanes, best.bins, 1.0, true},
+                         Shape{best.lanes, best.bins, 1.6, true}}) {
     const double ms = std::min(run(sh), run(sh));
     if (ms < best_ms) best_ms = ms, best = sh;
   }
-  C.max_lanes = best.lanes, C.bins = best.bins, C.bin_ratio = best.ratio;
+  C.max_lanes = best.lanes, C.bins = best.bins, C.bin_ratio = best.ratio, C.bins_by_size = best.by_size;
 
   // Per bin: the x-drop pass forms (register-band levels row-interleaved or one pass per thread, the band where one
   // warp per pass takes over, the widest band of the wavefront form, the rows after which a register-band pass moves
@@ -2141,16 +2148,19 @@ void autotune(Context &C, Batch &B, const Params &P, int mode) {
     C.scan_tiles_per_thread = best_t;
   }
   if (mode == DCNS_MODE_TWO_GAP) {
-    // the stripe flow (-1 below), or one CTA per DP with 2, 4 or 8 warps (0: by the number of DPs)
-    int best_w = -1;
+    // the stripe flow with 5 or 6 blocks per SM (-5, -6 below), or one CTA per DP with 2, 4 or 8 warps (0: by the
+    // number of DPs)
+    int best_w = -5;
     double best_w_ms = 1e300;
-    for (int nw : {-1, 0, 2, 4, kSgNW}) {
+    for (int nw : {-5, -6, 0, 2, 4, kSgNW}) {
       C.sg_flow = nw < 0;
+      C.sg_flow_blocks = nw == -6 ? 6 : 5;
       C.sg_warps = std::max(nw, 0);
       const double ms = std::min(run(best), run(best));
       if (ms < best_w_ms) best_w_ms = ms, best_w = nw;
     }
     C.sg_flow = best_w < 0;
+    C.sg_flow_blocks = best_w == -6 ? 6 : 5;
     C.sg_warps = std::max(best_w, 0);
   }
 }
@@ -2194,12 +2204,17 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
   }
   std::vector<int64_t> order(np);
   for (int64_t p = 0; p < np; ++p) order[p] = p;
+  const bool ascending = C.bins_by_size;
   std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
     const int64_t wa = (int64_t)pairs[a].n1 * pairs[a].n2, wb = (int64_t)pairs[b].n1 * pairs[b].n2;
-    return wa != wb ? wa > wb : a < b;
+    return wa != wb ? (ascending ? wa < wb : wa > wb) : a < b;
   });
-  // bin b's share of the work is proportional to bin_ratio^b: the last bins to finish their level-0 scan have the
-  // least host work left; pairs are dealt in decreasing work to the bin furthest below its share
+  // bin b's share of the seed-scan work is proportional to bin_ratio^b.  Two ways to fill the bins:
+  //  * mixed (default): pairs dealt in decreasing work to the bin furthest below its share, so every bin holds a mix
+  //    of sizes and the last bins to finish their level-0 scan have the least scan work;
+  //  * by size: consecutive runs of pairs in increasing work, so the last bin holds the largest pairs.  The host and
+  //    x-drop work after a bin's scan grows with its number of pairs (seeds per pair do not grow with pair length),
+  //    so the bin whose tail is on the critical path then has the fewest pairs.
   std::vector<double> target(kBins);
   {
     double tot = 0, wsum = 0, f = 1;
@@ -2208,13 +2223,19 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
     for (int b = 0; b < kBins; ++b) target[b] *= tot / wsum;
   }
   std::vector<std::vector<int64_t>> bins(kBins);
-  for (int64_t q = 0; q < np; ++q) {
+  for (int64_t q = 0, cur = 0; q < np; ++q) {
     const int64_t p = order[q];
+    const double wk = (double)pairs[p].n1 * pairs[p].n2 + 1;
     int bb = 0;
-    for (int b = 1; b < kBins; ++b)
-      if (target[b] > target[bb]) bb = b;
+    if (ascending) {
+      while (cur + 1 < kBins && target[cur] <= 0) ++cur;
+      bb = (int)cur;
+    } else {
+      for (int b = 1; b < kBins; ++b)
+        if (target[b] > target[bb]) bb = b;
+    }
     bins[bb].push_back(p);
-    target[bb] -= (double)pairs[p].n1 * pairs[p].n2 + 1;
+    target[bb] -= wk;
   }
   for (auto &b : bins) std::sort(b.begin(), b.end());  // each bin keeps the caller's pair order
   std::atomic<int> next(0);
@@ -2263,6 +2284,7 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
         L.xdrop_handoff = bt.xdrop_handoff, L.xdrop_resume_lanes = bt.xdrop_resume_lanes;
         L.sg_warps = C.sg_warps;
         L.sg_flow = C.sg_flow;
+        L.sg_flow_blocks = C.sg_flow_blocks;
         L.scan_tiles_per_thread = C.scan_tiles_per_thread;
         L.call_t0 = C.call_t0;
         L.lane_id = l;

@@ -122,6 +122,7 @@ struct Context {
   // DCNS_LANES / DCNS_BINS in the environment override the defaults at context creation.
   bool is_lane = false;
   double bin_ratio = 0.6;    // bin b holds a share of the work proportional to bin_ratio^b (later bins smaller)
+  bool bins_by_size = false;  // bins are consecutive runs of pairs in increasing size (else a mix of sizes each)
   int xdrop_warp_from = 20;  // x-drop bands wider than this run one warp per pass (DCNS_XDROP_WARP_FROM)
   // x-drop bands wider than xdrop_warp_from and up to this run as one-warp wavefronts (DCNS_XDROP_WAVE; 0 = off)
   int xdrop_wave_max_w = 256;
@@ -136,6 +137,8 @@ struct Context {
   int sg_warps = 0;
   // unweighted semi-global DPs as a flow of stripe units over one persistent grid (DCNS_SG_FLOW=0: one CTA per DP)
   bool sg_flow = true;
+  // resident blocks per SM of the stripe-flow kernel: 5 (96 registers) or 6 (80 registers) (DCNS_SG_FLOW_BLOCKS)
+  int sg_flow_blocks = 5;
   // seed-scan tiling target: reference rows are split into chunks while a launch has fewer tiles than this many per
   // resident thread (DCNS_SCAN_TILES)
   int scan_tiles_per_thread = 8;

@@ -420,9 +420,10 @@ __device__ __forceinline__ int sg_cell(int sc, int dg, int aF1, int aF2, int &e1
   return valid ? v : kOut;
 }
 
-template <bool CODES>
-__global__ void __launch_bounds__(32 * kSgFlowWarps) sg_flow_kernel(SgFlow F, Arena ar, Params P,
-                                                                   uint8_t *__restrict__ tb) {
+// MINB: resident blocks per SM the register allocation must allow (5: 96 registers; 6: 80, a few spilled words)
+template <bool CODES, int MINB>
+__global__ void __launch_bounds__(32 * kSgFlowWarps, MINB) sg_flow_kernel(SgFlow F, Arena ar, Params P,
+                                                                         uint8_t *__restrict__ tb) {
   __shared__ SgRec stage[kSgFlowWarps][2][32];
   __shared__ int stage_c[kSgFlowWarps][2][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -650,29 +651,42 @@ int64_t sg_flow_units(int n1, int n2, int w) {
   return std::max<int64_t>(1, (n1_eff + kSgRows - 1) / kSgRows);
 }
 
-int sg_flow_blocks_per_sm() {
-  static int nb = 0;
-  if (nb == 0) {
+int sg_flow_blocks_per_sm(int minb) {
+  static int nb[2] = {0, 0};
+  int &r = nb[minb == 6 ? 1 : 0];
+  if (r == 0) {
     int v = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, sg_flow_kernel<true>, 32 * kSgFlowWarps, 0) != cudaSuccess) {
+    const cudaError_t e = minb == 6 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, sg_flow_kernel<true, 6>,
+                                                                                     32 * kSgFlowWarps, 0)
+                                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, sg_flow_kernel<true, 5>,
+                                                                                     32 * kSgFlowWarps, 0);
+    if (e != cudaSuccess) {
       (void)cudaGetLastError();
       v = 1;
     }
-    nb = v > 0 ? v : 1;
+    r = v > 0 ? v : 1;
   }
-  return nb;
+  return r;
 }
 
-int64_t sg_flow_grid_warps(int nsm) { return (int64_t)nsm * sg_flow_blocks_per_sm() * kSgFlowWarps; }
+int64_t sg_flow_grid_warps(int nsm, int minb) { return (int64_t)nsm * sg_flow_blocks_per_sm(minb) * kSgFlowWarps; }
 
-void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, bool codes, int nsm, cudaStream_t st) {
+void launch_semiglobal_flow(const SgFlow &f, Arena ar, Params p, uint8_t *tb, bool codes, int nsm, int minb,
+                            cudaStream_t st) {
   if (f.total_units <= 0) return;
-  const int64_t warps = std::min<int64_t>(f.total_units, sg_flow_grid_warps(nsm));
+  const int64_t warps = std::min<int64_t>(f.total_units, sg_flow_grid_warps(nsm, minb));
   const int blocks = (int)((warps + kSgFlowWarps - 1) / kSgFlowWarps);
-  if (codes)
-    sg_flow_kernel<true><<<blocks, 32 * kSgFlowWarps, 0, st>>>(f, ar, p, tb);
-  else
-    sg_flow_kernel<false><<<blocks, 32 * kSgFlowWarps, 0, st>>>(f, ar, p, tb);
+  if (minb == 6) {
+    if (codes)
+      sg_flow_kernel<true, 6><<<blocks, 32 * kSgFlowWarps, 0, st>>>(f, ar, p, tb);
+    else
+      sg_flow_kernel<false, 6><<<blocks, 32 * kSgFlowWarps, 0, st>>>(f, ar, p, tb);
+  } else {
+    if (codes)
+      sg_flow_kernel<true, 5><<<blocks, 32 * kSgFlowWarps, 0, st>>>(f, ar, p, tb);
+    else
+      sg_flow_kernel<false, 5><<<blocks, 32 * kSgFlowWarps, 0, st>>>(f, ar, p, tb);
+  }
 }
 
 // ------------------------------------------------------------------ traceback (:869-914)

@@ -193,6 +193,8 @@ typedef struct {
   int32_t sg_warps;               /* warps per 2-piece DP when one CTA runs a DP (0: two for launches of many DPs,
                                      else eight) */
   int32_t sg_flow;                /* 1: 2-piece DPs run as a flow of 128-row stripe units over one persistent grid */
+  int32_t sg_flow_blocks;         /* resident blocks per SM of that grid: 5 or 6 */
+  int32_t bins_by_size;           /* 1: bins are runs of pairs in increasing size (the largest last); 0: mixed */
   int32_t n_bins_tuned;           /* bins with their own x-drop forms below (0: every bin uses bin 0's values) */
   int32_t xdrop_warp_from[16], xdrop_wave_max_w[16], xdrop_flat[16], xdrop_handoff[16], xdrop_resume_lanes[16];
 } dcns_tuning;

@@ -50,3 +50,32 @@ def test_no_gpu_fails_loudly(so_path):
     with pytest.raises(dcns_gb300.DcnsError):
         dcns_gb300.Engine(0)
 
+
+
+def test_python_structs_match_the_c_layout(tmp_path):
+    """The ctypes mirrors of the header's structs have the C compiler's size and field offsets (a mismatch would make
+    the library write past the Python buffers)."""
+    import shutil
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    pairs = [("dcns_params", dcns_gb300.Params), ("dcns_pair", dcns_gb300.Pair), ("dcns_stats", dcns_gb300.Stats),
+             ("dcns_serving_stats", dcns_gb300.ServingStats), ("dcns_tuning", dcns_gb300.Tuning),
+             ("dcns_results", dcns_gb300.Results)]
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "dcns_gb300.h"', "int main(void) {"]
+    for cname, py in pairs:
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:  # Python spells the C field `lambda` as lambda_
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname.rstrip("_")}));')
+    lines.append("  return 0;\n}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        name, key, val = line.split()
+        got[(name, key)] = int(val)
+    for cname, py in pairs:
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
