@@ -179,6 +179,10 @@ void launch_l0_select(const unsigned long long *keys, int64_t n0, const int64_t 
                       cudaStream_t st);
 void launch_scan_generic(const ScanTask *tasks, const int *idx, int n, const int64_t *seq_base, Arena ar, Params p,
                          unsigned long long *keys, int32_t *scratch, int64_t scratch_per_thread, cudaStream_t st);
+// Long tasks (either semantics), one warp each as a wavefront; scratch: per_task >= 2 (tw + 2) ints per task.
+void launch_scan_generic_wave(const ScanTask *tasks, const int *idx, int n, const int64_t *seq_base, Arena ar,
+                              Params p, unsigned long long *keys, int32_t *scratch, int64_t per_task,
+                              cudaStream_t st);
 void launch_reverse(ScanTask *tasks, int first, int n, const unsigned long long *keys, const int64_t *pair_base,
                     const int32_t *pair_len, Arena ar, Params p, cudaStream_t st);
 // wcap: 10 or 20 (one thread per pass, band in registers), 0 (one warp per pass, band in scratch), -1 (one warp per

@@ -490,15 +490,33 @@ void run_scan_round(Context &C, ScanState &S, const Params &P, int64_t first, in
     C.stats.kernel_launches += 1;
   }
   if (!generic.empty()) {
+    // large tasks (long reads: only the kernel-level call has them) run one warp each as wavefronts, the rest one
+    // thread each
+    auto wave = [&](int32_t k) {
+      const ScanTask &T = S.task(k + S.ns);
+      return T.tw >= 64 && (int64_t)(T.hi - T.lo) * T.tw >= (1 << 20);
+    };
+    std::vector<int32_t> gl;
+    gl.reserve(generic.size());
     int maxtw = 0;
-    for (int32_t k : generic) maxtw = std::max(maxtw, S.task(k + S.ns).tw);
+    for (int32_t k : generic) {
+      maxtw = std::max(maxtw, S.task(k + S.ns).tw);
+      if (!wave(k)) gl.push_back(k);
+    }
+    const int64_t nthread = (int64_t)gl.size();
+    for (int32_t k : generic)
+      if (wave(k)) gl.push_back(k);
+    const int64_t nwave = (int64_t)gl.size() - nthread;
     const int64_t per = 3 * ((int64_t)maxtw + 2);
-    C.d_idx.ensure(C, sizeof(int32_t) * generic.size());
-    C.d_scratch.ensure(C, sizeof(int32_t) * per * generic.size());
-    h2d(C, C.d_idx, generic.data(), generic.size());
-    launch_scan_generic(C.d_tasks.as<ScanTask>(), C.d_idx.as<int>(), (int)generic.size(), C.seqbase_dev, C.arena,
-                        P, C.d_keys.as<unsigned long long>(), C.d_scratch.as<int32_t>(), per, C.st);
-    C.stats.kernel_launches += 1;
+    C.d_idx.ensure(C, sizeof(int32_t) * gl.size());
+    C.d_scratch.ensure(C, sizeof(int32_t) * per * gl.size());
+    h2d(C, C.d_idx, gl.data(), gl.size());
+    launch_scan_generic(C.d_tasks.as<ScanTask>(), C.d_idx.as<int>(), (int)nthread, C.seqbase_dev, C.arena, P,
+                        C.d_keys.as<unsigned long long>(), C.d_scratch.as<int32_t>(), per, C.st);
+    launch_scan_generic_wave(C.d_tasks.as<ScanTask>(), C.d_idx.as<int>() + nthread, (int)nwave, C.seqbase_dev,
+                             C.arena, P, C.d_keys.as<unsigned long long>(), C.d_scratch.as<int32_t>() + per * nthread,
+                             per, C.st);
+    C.stats.kernel_launches += (nthread > 0) + (nwave > 0);
   }
   launch_reverse(C.d_tasks.as<ScanTask>(), (int)d0, (int)n, C.d_keys.as<unsigned long long>(), C.seqbase_dev,
                  nullptr, C.arena, P, C.st);

@@ -12,6 +12,7 @@
 //                       the duo table
 //   scan_generic_kernel int32 lanes, any window width, both reference semantics (striped / scalar); used where the
 //                       fast kernel's static int16 bound or width does not hold
+//   scan_generic_wave_kernel  the same semantics for one large task per warp (long reads: kernel-level calls)
 //   reverse_kernel      the reverse-complement re-scan that fixes each seed's start (getSeeds :156-166)
 //   l0_*_kernel         device selection of the level-0 windows that reached min_score (count, scan, emit in window
 //                       order) and their reverse re-scans, one thread per selected window
@@ -454,6 +455,115 @@ __global__ void scan_generic_kernel(const ScanTask *__restrict__ tasks, const in
          [&](int p) { return base_code(ar, b2 + T.s2 + p); }, T.tw, P.open1, P.ext1, P.match, P.mismatch,
          T.striped != 0, H, Hp, E, best, bi, bj);
   keys[ti] = best > 0 ? scan_key(best, T.lo + bi, bj) : 0ull;
+}
+
+// Either semantics of sw_one for one long task per warp, as an anti-diagonal wavefront over 32-row stripes: lane l
+// owns reference row r0 + l and computes read column j (1-based) at step t = j - 1 + l, with the cell above (H and
+// the column's vertical gap E after the row above) and the diagonal H from lane l - 1 by __shfl_up_sync, and its own
+// left H and horizontal gap state in registers.  Both semantics are local recurrences on those five values: the
+// scalar kernel's (SmithWaterman_non_avx) and the striped kernels' (the vertical gap advanced from the cell's value
+// before the horizontal gap is merged, and the horizontal gap merged last, as the AVX2 code's second pass does).  Lane 0 takes the row above the stripe from the task's boundary row in
+// global scratch (H and E by column), staged into shared memory two 32-column chunks ahead; lane 31 rewrites it
+// with the stripe's last row (column j at step j + 30, after lane 0 staged it).  Each lane keeps its row's first
+// maximum; after each stripe the rows are taken in order, so the task's maximum is the first one in row-major,
+// column-minor order, as the scalar kernel finds it.  scratch: 2 (read length + 2) ints per task.
+__global__ void __launch_bounds__(128) scan_generic_wave_kernel(const ScanTask *__restrict__ tasks,
+                                                                const int *__restrict__ idx, int n,
+                                                                const int64_t *__restrict__ seq_base, Arena ar,
+                                                                Params P, unsigned long long *__restrict__ keys,
+                                                                int32_t *__restrict__ scratch, int64_t per_task) {
+  __shared__ int stH[4][2][32], stE[4][2][32], stC[4][2][32];
+  const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (gw >= n) return;  // whole warp
+  const int ti = idx[gw];
+  const ScanTask T = tasks[ti];
+  const int64_t b1 = seq_base[2 * T.pair] + T.lo, b2 = seq_base[2 * T.pair + 1] + T.s2;
+  const int na = T.hi - T.lo, nb = T.tw;
+  const int open = P.open1, ext = P.ext1;
+  const bool striped = T.striped != 0;
+  int32_t *const bH = scratch + per_task * gw, *const bE = bH + (nb + 2);
+  for (int j = lane; j <= nb + 1; j += 32) bH[j] = 0, bE[j] = 0;  // row -1: H = 0, E = 0
+  __syncwarp();
+  int gbest = 0, gi = -1, gj = -1;
+  const int nsteps = nb + 31;
+  for (int r0 = 0; r0 < na; r0 += 32) {
+    const int i = r0 + lane;
+    const bool live = i < na;
+    const int ci = live ? base_code(ar, b1 + i) : 0;
+    // columns 32 * chunk + 1 .. + 32 of the row above (and the read's codes there) into stage[chunk & 1]
+    auto stage = [&](int chunk) {
+      const int j = 32 * chunk + 1 + lane;
+      const bool in = j <= nb;
+      stH[wb][chunk & 1][lane] = in ? __ldcg(bH + j) : 0;
+      stE[wb][chunk & 1][lane] = in ? __ldcg(bE + j) : 0;
+      stC[wb][chunk & 1][lane] = in ? base_code(ar, b2 + j - 1) : 0;
+    };
+    stage(0);
+    stage(1);
+    __syncwarp();
+    int leftH = 0, e = 0, best = 0, bestj = -1, outH = 0, outE = 0, outC = 0, prevUp = 0;
+    for (int t = 0; t < nsteps; ++t) {
+      int upH = __shfl_up_sync(0xFFFFFFFFu, outH, 1);
+      int upE = __shfl_up_sync(0xFFFFFFFFu, outE, 1);
+      int cj = __shfl_up_sync(0xFFFFFFFFu, outC, 1);
+      if ((t & 31) == 0 && t > 0) {
+        __syncwarp();
+        stage((t >> 5) + 1);  // two chunks ahead of lane 0's reads
+        __syncwarp();
+      }
+      const int j = t + 1 - lane;  // 1-based read column of this lane's cell
+      int diagH = prevUp;
+      if (lane == 0) {
+        upH = stH[wb][(t >> 5) & 1][t & 31];
+        upE = stE[wb][(t >> 5) & 1][t & 31];
+        cj = stC[wb][(t >> 5) & 1][t & 31];
+        diagH = t == 0 ? 0 : diagH;  // column 0 of the row above is 0
+      }
+      if (j == 1) diagH = 0;  // column 0 of the row above
+      int nH = 0, nE = 0;
+      if (live && j >= 1 && j <= nb) {
+        const int s = score_of(ci, cj, P.match, P.mismatch);
+        if (striped) {
+          // first pass (H before the horizontal gap, E from it), then the horizontal gap `e` (del) merged
+          const int hp = max(max(diagH + s, 0), upE);
+          nE = max(max(upE + ext, hp + open), 0);
+          e = max(leftH + open, e + ext);
+          nH = hp < e ? e : hp;
+          e = max(e, 0);
+          if (nH > best) best = nH, bestj = j - 1;
+        } else {
+          e = max(open + leftH, ext + e);
+          const int Ej = max(open + upH, ext + upE);
+          int v = max(s + diagH, e);
+          v = max(v, Ej);
+          nH = max(v, 0);
+          nE = max(Ej, 0);
+          e = max(e, 0);
+          if (v > best) best = v, bestj = j - 1;
+        }
+        leftH = nH;
+        if (lane == 31) bH[j] = nH, bE[j] = nE;
+      }
+      prevUp = upH;
+      outH = nH;
+      outE = nE;
+      outC = cj;
+    }
+    __syncwarp();
+    for (int rr = 0; rr < 32; ++rr) {  // the stripe's rows in order: the first maximum in row-major order
+      const int tm = __shfl_sync(0xFFFFFFFFu, best, rr), tj = __shfl_sync(0xFFFFFFFFu, bestj, rr);
+      if (r0 + rr < na && tm > gbest) gbest = tm, gi = r0 + rr, gj = tj;
+    }
+  }
+  if (lane == 0) keys[ti] = gbest > 0 ? scan_key(gbest, T.lo + gi, gj) : 0ull;
+}
+
+void launch_scan_generic_wave(const ScanTask *tasks, const int *idx, int n, const int64_t *seq_base, Arena ar,
+                              Params p, unsigned long long *keys, int32_t *scratch, int64_t per_task,
+                              cudaStream_t st) {
+  if (n <= 0) return;
+  scan_generic_wave_kernel<<<(n + 3) / 4, 128, 0, st>>>(tasks, idx, n, seq_base, ar, p, keys, scratch, per_task);
 }
 
 void launch_scan_generic(const ScanTask *tasks, const int *idx, int n, const int64_t *seq_base, Arena ar, Params p,

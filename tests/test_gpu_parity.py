@@ -61,6 +61,26 @@ def test_known_answer_inline_sequences(eng, golden):
         assert sc[i] == [int(c) for c in ragged(z, "ka_cigar", 2 * i + 1)]
 
 
+def test_smith_waterman_long_tasks_vs_oracle(eng, oracle):
+    """Large kernel-level SmithWaterman calls, which the engine runs as one-warp wavefronts: both sequences too long
+    for the reference's striped kernels (its scalar semantics, impl/sequenceAlignment3.cpp:223-225) and long pairs
+    the striped int16 kernel still takes, against the oracle's own dispatch, with N runs, planted similarity, a task
+    whose maximum sits in the last rows and a non-default scoring."""
+    rng = np.random.default_rng(17000)
+    tasks = []
+    for n1, n2 in [(21000, 20000), (17000, 16500), (12000, 30000)]:
+        a, b = W.planted_pair(rng, n1, n2, 6, 100, 900, 0.8, 0.95, 0.01, 0.1)
+        tasks.append((W.prepare(a), W.prepare(b)))
+    a, b = tasks[0]
+    tasks[0] = (np.concatenate([a, b[-3000:]]), b)  # a copy of the read's tail at the reference's end
+    for kw in ({}, {"open1": -5, "ext1": -1, "match": 3, "mismatch": -4}):
+        out = eng.SmithWaterman(tasks, **kw)
+        okw = {"open": kw.get("open1", -4), "ext": kw.get("ext1", -2), "match": kw.get("match", 2),
+               "mismatch": kw.get("mismatch", -3)}
+        for k, (a, b) in enumerate(tasks):
+            assert tuple(int(v) for v in out[k]) == oracle.sw(a, b, mode=0, **okw), (k, kw)
+
+
 def test_xextend_golden(eng, golden):
     z = golden
     n = len(z["xe_exp"])
