@@ -142,7 +142,8 @@ class Tuning(C.Structure):
                 ("bins_by_size", C.c_int32),
                 ("n_bins_tuned", C.c_int32),
                 ("xdrop_warp_from", C.c_int32 * 16), ("xdrop_wave_max_w", C.c_int32 * 16), ("xdrop_flat", C.c_int32 * 16),
-                ("xdrop_handoff", C.c_int32 * 16), ("xdrop_resume_lanes", C.c_int32 * 16)]
+                ("xdrop_handoff", C.c_int32 * 16), ("xdrop_resume_lanes", C.c_int32 * 16),
+                ("xdrop_group_from", C.c_int32 * 16)]
 
     def as_dict(self):
         n = max(self.n_bins_tuned, 1)
@@ -153,7 +154,8 @@ class Tuning(C.Structure):
                 "xdrop_per_bin": [{"warp_from": self.xdrop_warp_from[b], "wave_max_w": self.xdrop_wave_max_w[b],
                                    "row_interleaved": bool(self.xdrop_flat[b]),
                                    "handoff_rows": self.xdrop_handoff[b],
-                                   "handoff_lanes": self.xdrop_resume_lanes[b]} for b in range(n)]}
+                                   "handoff_lanes": self.xdrop_resume_lanes[b],
+                                   "groups_from_band": self.xdrop_group_from[b]} for b in range(n)]}
 
 
 class Results(C.Structure):

@@ -494,6 +494,7 @@ int dcns_get_tuning(const dcns_ctx *ctx, dcns_tuning *out) {
     out->xdrop_flat[b] = (own ? C.bin_tune[b].xdrop_flat : C.xdrop_flat) ? 1 : 0;
     out->xdrop_handoff[b] = own ? C.bin_tune[b].xdrop_handoff : C.xdrop_handoff;
     out->xdrop_resume_lanes[b] = own ? C.bin_tune[b].xdrop_resume_lanes : C.xdrop_resume_lanes;
+    out->xdrop_group_from[b] = own ? C.bin_tune[b].xdrop_group_from : C.xdrop_group_from;
   }
   return DCNS_OK;
 }

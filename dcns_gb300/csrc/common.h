@@ -202,16 +202,17 @@ struct XHandoff {
   int *list, *count;
   int32_t *spill;
   int cap, rows;
-  int lanes;  // lanes per handed-off pass: 8 or 16 (G-lane groups, 32 / G passes per warp) or 32 (one warp)
+  int lanes;  // lanes per handed-off pass: 4, 8 or 16 (G-lane groups, 32 / G passes per warp) or 32 (one warp)
 };
 constexpr int kXdropSpillInts = 2 * (2 * 20 + 2);
 // fetch: the level's pass counter, zero before the launch (the row-interleaved register-band kernel, flat = true).
-// Traceback slots hold min(n1, slot_rows) rows.  Returns the number of kernels launched.
+// Traceback slots hold min(n1, slot_rows) rows.  group_from > 0: register-band levels of band group_from and wider
+// run every pass on H.lanes-lane groups from row 1 (no one-thread form).  Returns the number of kernels launched.
 int launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, int *list_out, int *count_out,
                        int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int slot_rows,
                        int *fetch, const XHandoff &H, Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm,
                        int32_t *scratch, int64_t per_warp, int warps, int warp_from, int wave_max_w, bool flat,
-                       cudaStream_t st);
+                       int group_from, bool codes, cudaStream_t st);
 void launch_xdrop_traceback_all(XTask *tasks, int n, const uint32_t *tb, int64_t tb_words, uint32_t *cig,
                                 unsigned long long *cig_cursor, cudaStream_t st);
 // Packs the CIGARs of every finished task in task order into dense (cig_dense offsets); *total = their words.

@@ -131,8 +131,11 @@ struct Context {
   // a pass of a row-interleaved level still running after this many rows moves to the wavefront form
   // (DCNS_XDROP_HANDOFF; 0 = off)
   int xdrop_handoff = 96;
-  // lanes that run each handed-off pass as a wavefront: 8, 16 or 32 (DCNS_XDROP_RESUME_LANES)
+  // lanes that run each handed-off pass as a wavefront: 4, 8, 16 or 32 (DCNS_XDROP_RESUME_LANES)
   int xdrop_resume_lanes = 8;
+  // register-band levels of this band and wider run every pass on lane groups from row 1 (DCNS_XDROP_GROUP_FROM;
+  // 0 = off)
+  int xdrop_group_from = 0;
   // warps per DP of the unweighted semi-global kernel: 2, 4 or 8 (DCNS_SG_WARPS; 0 = by the number of DPs)
   int sg_warps = 0;
   // unweighted semi-global DPs as a flow of stripe units over one persistent grid (DCNS_SG_FLOW=0: one CTA per DP)
@@ -146,7 +149,7 @@ struct Context {
   struct BinTune {
     int xdrop_warp_from, xdrop_wave_max_w;
     bool xdrop_flat;
-    int xdrop_handoff, xdrop_resume_lanes;
+    int xdrop_handoff, xdrop_resume_lanes, xdrop_group_from;
   };
   std::vector<BinTune> bin_tune;
   std::vector<double> last_bin_xdrop_ms;  // x-drop kernel time of each bin of the last binned call

@@ -156,7 +156,8 @@ __device__ __forceinline__ int xd_row(XPassScalars &x, int32_t (&M)[XBand<WC>::N
 // Row x.i as one left-to-right loop: the same cells, comparisons and tie rules as xd_row, with A (the diagonal /
 // vertical choice) and the incoming horizontal gap e of each cell kept in registers for that cell only, so the band
 // arrays are the only per-cell state (a third of xd_row's registers: more warps per SM).  Returns as xd_row.
-template <int WC>
+// CODES = false (the forward passes, which keep no direction codes) leaves out the codes and their comparisons.
+template <int WC, bool CODES>
 __device__ __forceinline__ int xd_row_fused(XPassScalars &x, int32_t (&M)[XBand<WC>::NA], int32_t (&F)[XBand<WC>::NA],
                                             uint64_t (&qw)[XBand<WC>::NQ], const Arena &ar, const Params &P,
                                             uint32_t *__restrict__ tb) {
@@ -164,7 +165,8 @@ __device__ __forceinline__ int xd_row_fused(XPassScalars &x, int32_t (&M)[XBand<
   const int i = x.i, w = x.w, nk = x.nk, n2 = x.n2;
   if (i > x.n1) return 0;
   const int c0 = max(i - w, 1), c1 = min(i + w, n2);
-  if (x.codes && (int64_t)i * x.wpr > x.tb_cap) return 2;
+  const bool codes = CODES && x.codes;
+  if (codes && (int64_t)i * x.wpr > x.tb_cap) return 2;
   const int open = P.open1, ext = P.ext1, g = ext > open ? ext : open;
   const int ci = x.s1.at(ar, i - 1);
   int best = 0, bestj = -1;
@@ -176,7 +178,8 @@ __device__ __forceinline__ int xd_row_fused(XPassScalars &x, int32_t (&M)[XBand<
   for (int k = 0; k < NK; ++k) {
     const int j = i - w + k;
     uint32_t nib = 0xFu;
-    if (k < nk && j >= c0 && j <= c1) {
+    // k in [0, 2w] puts j in [i - w, i + w], so the band test is 1 <= j <= n2
+    if (k < nk && (unsigned)(j - 1) < (unsigned)n2) {
       // M[k] and F[k + 1] still hold the row above: F[k + 1] is rewritten at the next cell
       const int cj = (int)((qw[k >> 4] >> (4 * (k & 15))) & 15u);
       const int32_t diag = (j == 1) ? (i == 1 ? 0 : kOut) : M[k];
@@ -185,7 +188,6 @@ __device__ __forceinline__ int xd_row_fused(XPassScalars &x, int32_t (&M)[XBand<
       const int32_t A = sd > fin ? sd : fin;
       const bool ge = !(A > ec);  // the horizontal gap wins ties
       const int32_t v = ge ? ec : A;
-      uint32_t d = ge ? 2u : (sd > fin ? 0u : 1u);
       M[k] = v;
       if (v > best) {
         best = v;
@@ -193,13 +195,16 @@ __device__ __forceinline__ int xd_row_fused(XPassScalars &x, int32_t (&M)[XBand<
       }
       const int32_t h = v + open;
       const int32_t f = fin + ext;
-      if (f >= h) d |= 4u;
       F[k] = f >= h ? f : h;
-      if (ec + ext >= h) d |= 8u;
+      if constexpr (CODES) {
+        uint32_t d = ge ? 2u : (sd > fin ? 0u : 1u);
+        if (f >= h) d |= 4u;
+        if (ec + ext >= h) d |= 8u;
+        nib = d;
+      }
       ec = max(ec + g, A + open);  // = max(e + ext, max(A, e) + open), the reference's e update
-      nib = d;
     }
-    if (x.codes && k < nk) {
+    if (CODES && codes && k < nk) {
       cw |= nib << (4 * (k & 7));
       if ((k & 7) == 7 || k == nk - 1) {
         row_codes[kw++] = cw;
@@ -568,7 +573,7 @@ __global__ void __launch_bounds__(128) xdrop_level_kernel(XLevelArgs L, Arena ar
 // the end of seq1) leaves its band state in a spill slot for the wavefront form (xdrop_level_resume_kernel), which
 // runs the rest of the pass 32 rows at a time: the level then no longer lasts as long as its longest pass on one
 // thread.  A pass that finds the spill slots full stays on its thread.
-template <int WC>
+template <int WC, bool CODES>
 __global__ void __launch_bounds__(128) xdrop_level_flat_kernel(XLevelArgs L, Arena ar, Params P,
                                                                uint32_t *__restrict__ tb) {
   constexpr int NA = XBand<WC>::NA;
@@ -608,7 +613,7 @@ __global__ void __launch_bounds__(128) xdrop_level_flat_kernel(XLevelArgs L, Are
     }
     if (!__any_sync(0xFFFFFFFFu, id >= 0 || more)) break;
     if (id >= 0) {
-      const int st = xd_row_fused<WC>(x, Mr, Fr, qw, ar, P, tb);
+      const int st = xd_row_fused<WC, CODES>(x, Mr, Fr, qw, ar, P, tb);
       if (st >= 0) {
         XTask &T = L.tasks[id];
         xd_finish(x, T, st);
@@ -864,14 +869,20 @@ __global__ void __launch_bounds__(128) xdrop_level_resume_kernel(XLevelArgs L, A
 // A G-row stripe is 2w + 1 + 2(G - 1) steps, so fewer lanes idle in the skew than with a 32-row stripe at bands
 // 10-20 (G = 8: 75 % of lane-steps compute a cell at band 20, against 40 % for one warp per pass); every group runs
 // its stripes in step with the warp (all passes of a level have the same band), evaluates its rows in order after
-// each stripe, and takes its next pass (list index + the grid's group count) when its pass ends.
-template <int G>
+// each stripe, and takes its next pass (list index + the grid's group count) when its pass ends.  G = 4 idles the
+// fewest lanes in the skew (78 % of lane-steps compute at band 10, 87 % at band 20) but needs eight passes per warp;
+// CODES = false (forward passes) leaves out the direction codes and their comparisons.  FRESH = true runs the level's
+// whole list (L.list_in) from row 1 instead of the handed-off passes: each group takes its pass's traceback slot and
+// starts from the zero row, so a level of long passes (band 20: the passes that restarted) skips the one-thread form.
+template <int G, bool CODES, bool FRESH>
 __global__ void __launch_bounds__(128) xdrop_level_resume_group_kernel(XLevelArgs L, Arena ar, Params P,
                                                                        uint32_t *__restrict__ tb) {
   constexpr int NG = 32 / G;
   __shared__ int32_t sM[4][NG][2 * kXrMaxW + 2], sF[4][NG][2 * kXrMaxW + 2];
   const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5, g = lane / G, gl = lane % G;
-  const int n = min(*L.long_count, L.spill_cap);
+  const unsigned gmask = G == 32 ? 0xFFFFFFFFu : ((1u << G) - 1u) << (lane & ~(G - 1));  // the group's lanes
+  const int n = FRESH ? *L.count_in : min(*L.long_count, L.spill_cap);
+  const int *const list = FRESH ? L.list_in : L.long_list;
   const int ngroups = (int)((gridDim.x * blockDim.x) / G);
   const int w = L.level_w, nk = 2 * w + 1, wpr = xd_words_per_row(w), nsteps = nk + 2 * (G - 1);
   const int open = P.open1, ext = P.ext1;
@@ -883,25 +894,58 @@ __global__ void __launch_bounds__(128) xdrop_level_resume_group_kernel(XLevelArg
   int id = 0, n1 = 0, n2 = 0, cap = 0, score = 0, e1 = 0, e2 = 0, rows = 0, r0 = 1;
   int64_t off = 0;
   SeqView s1{0, 0, 0}, s2{0, 0, 0};
-  auto begin = [&]() {  // list entry q into the group: its spilled band (the row before r0) and running state
-    active = q < n;
-    if (!active) return;
-    id = L.long_list[q];
-    T = &L.tasks[id];
-    const int32_t *sp = L.spill + (int64_t)q * 2 * L.spill_half;
-    n1 = T->n1, n2 = T->n2, codes = T->want_codes != 0, off = T->tb_off, cap = T->tb_cap;
-    s1 = SeqView{T->base1, T->a1, T->dir}, s2 = SeqView{T->base2, T->a2, T->dir};
-    score = T->score, e1 = T->end1, e2 = T->end2, rows = T->rows, r0 = rows + 1;
-    for (int k = gl; k <= nk; k += G) bM[k] = sp[k], bF[k] = sp[L.spill_half + k];
+  // List entry q into the group: its band of the row before r0 and its running state (a handed-off pass: from its
+  // spill slot; a fresh pass: the zero row, after its traceback slot is taken).  Called by whole groups only.
+  auto begin = [&]() {
+    for (;;) {
+      active = q < n;
+      if (!active) return;
+      id = list[q];
+      T = &L.tasks[id];
+      n1 = T->n1, n2 = T->n2, codes = T->want_codes != 0;
+      s1 = SeqView{T->base1, T->a1, T->dir}, s2 = SeqView{T->base2, T->a2, T->dir};
+      if constexpr (FRESH) {
+        int ok = 1;
+        long long o = 0;
+        int c = 0;
+        if (gl == 0) {
+          if (codes) ok = xd_take_slot(*T, L) ? 1 : 0;
+          if (!ok) {
+            T->status = 2;
+            L.retry[atomicAdd(L.retry_count, 1)] = id;
+          }
+          o = T->tb_off;
+          c = T->tb_cap;
+        }
+        ok = __shfl_sync(gmask, ok, 0, G);
+        if (!ok) {
+          q += ngroups;
+          continue;
+        }
+        off = __shfl_sync(gmask, o, 0, G);
+        cap = __shfl_sync(gmask, c, 0, G);
+        score = e1 = e2 = rows = 0, r0 = 1;
+        for (int k = gl; k <= nk; k += G) bM[k] = kOut, bF[k] = kOut;
+      } else {
+        const int32_t *sp = L.spill + (int64_t)q * 2 * L.spill_half;
+        off = T->tb_off, cap = T->tb_cap;
+        score = T->score, e1 = T->end1, e2 = T->end2, rows = T->rows, r0 = rows + 1;
+        for (int k = gl; k <= nk; k += G) bM[k] = sp[k], bF[k] = sp[L.spill_half + k];
+      }
+      return;
+    }
   };
   begin();
   __syncwarp();
   while (__any_sync(0xFFFFFFFFu, active)) {
     const int i = r0 + gl;
     const bool live = active && i <= n1;
-    const int c0 = max(i - w, 1), c1 = min(i + w, n2);
+    const int c1 = min(i + w, n2);
     const int ci = live ? s1.at(ar, i - 1) : 0;
-    const bool wcode = codes && live && (int64_t)i * wpr <= cap;  // rows past the slot are never kept
+    // the row's band cells: k in [0, 2w] puts j = i - w + k in [i - w, i + w], so the band test is 1 <= j <= n2,
+    // i.e. j - 1 unsigned below un2 (0 for a row past the pass: no cell)
+    const unsigned un2 = live ? (unsigned)n2 : 0u;
+    const bool wcode = CODES && codes && live && (int64_t)i * wpr <= cap;  // rows past the slot are never kept
     uint32_t *row_codes = tb + off + (int64_t)(i - 1) * wpr;
     int e = kOut, best = 0, bestj = -1, outM = kOut, outF = kOut, outC = 0, prevUp = kOut, kw = 0;
     uint32_t cw = 0;
@@ -917,31 +961,26 @@ __global__ void __launch_bounds__(128) xdrop_level_resume_group_kernel(XLevelArg
         cj = (active && j >= 1 && j <= n2) ? s2.at(ar, j - 1) : 0;
       }
       int nM = kOut, nF = kOut;
-      if (k >= 0 && k < nk) {
+      if ((unsigned)k < (unsigned)nk) {
         uint32_t nib = 0xFu;
-        if (live && j >= c0 && j <= c1) {
+        if ((unsigned)(j - 1) < un2) {
           const int32_t diag = (j == 1) ? (i == 1 ? 0 : kOut) : diagv;
           const int32_t fin = (j == c1) ? kOut : upF;
-          int32_t v = score_of(ci, cj, P.match, P.mismatch) + diag;
-          uint32_t d = v > fin ? 0u : 1u;
-          if (!(v > fin)) v = fin;
-          if (!(v > e)) {
-            d = 2u;
-            v = e;
-          }
+          const int32_t sd = score_of(ci, cj, P.match, P.mismatch) + diag;
+          const int32_t A = sd > fin ? sd : fin;
+          const bool ge = !(A > e);  // the horizontal gap wins ties
+          const int32_t v = ge ? e : A;
           if (v > best) {
             best = v;
             bestj = j;
           }
           const int32_t h = v + open;
           const int32_t f = fin + ext;
-          if (f >= h) d |= 4u;
           nM = v;
           nF = f >= h ? f : h;
-          e += ext;
-          if (e >= h) d |= 8u;
-          e = e >= h ? e : h;
-          nib = d;
+          const int32_t ee = e + ext;
+          if constexpr (CODES) nib = (ge ? 2u : (sd > fin ? 0u : 1u)) | (f >= h ? 4u : 0u) | (ee >= h ? 8u : 0u);
+          e = ee >= h ? ee : h;
           if (gl == G - 1) {
             bM[k] = nM;
             bF[k] = nF;
@@ -1052,12 +1091,12 @@ void launch_xdrop_iota(int *list, int n, int *count, cudaStream_t st) {
   xdrop_iota_kernel<<<(n + 255) / 256, 256, 0, st>>>(list, n, count);
 }
 
-template <int WC>
+template <int WC, bool CODES>
 int flat_blocks_per_sm() {
   static int nb = 0;
   if (nb == 0) {
     int v = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, xdrop_level_flat_kernel<WC>, 128, 0) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, xdrop_level_flat_kernel<WC, CODES>, 128, 0) != cudaSuccess) {
       (void)cudaGetLastError();
       v = 1;
     }
@@ -1070,28 +1109,62 @@ int launch_xdrop_level(XTask *tasks, const int *list_in, const int *count_in, in
                        int *retry, int *retry_count, unsigned long long *tb_cursor, int64_t tb_words, int slot_rows,
                        int *fetch, const XHandoff &H, Arena ar, Params p, uint32_t *tb, int w, int n_bound, int nsm,
                        int32_t *scratch, int64_t per_warp, int warps, int warp_from, int wave_max_w, bool flat,
-                       cudaStream_t st) {
+                       int group_from, bool codes, cudaStream_t st) {
   if (n_bound <= 0) return 0;
   const bool flat_level = flat && w <= warp_from && w <= kXrMaxW;
+  // groups of G lanes: 128 / G passes per block
+  auto group_grid = [&](int g, int64_t passes) {
+    return (int)std::min<int64_t>((passes + 128 / g - 1) / (128 / g), (int64_t)nsm * 16);
+  };
   const bool handoff = flat_level && H.rows > 0 && H.cap > 0;
   XLevelArgs L{tasks, list_in, count_in, list_out, count_out, retry, retry_count, tb_cursor, tb_words, fetch,
                H.list, H.count, H.spill, handoff ? H.cap : 0, w <= 10 ? XBand<10>::NA : XBand<20>::NA,
                handoff ? H.rows : 0, w, slot_rows};
   const int g = (int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * 16);
-  if (flat_level) {  // register band, row-interleaved: one resident wave of blocks, then the handed-off passes
-    if (w <= 10)
-      xdrop_level_flat_kernel<10><<<(int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * flat_blocks_per_sm<10>()),
-                                    128, 0, st>>>(L, ar, p, tb);
+  if (flat_level && group_from > 0 && w >= group_from) {  // every pass of the level on G-lane groups from row 1
+    XLevelArgs F = L;
+    F.spill_cap = 0;
+    const int G = (H.lanes == 4 || H.lanes == 16) ? H.lanes : 8;
+    const int gg = group_grid(G, n_bound);
+    if (G == 4 && codes)
+      xdrop_level_resume_group_kernel<4, true, true><<<gg, 128, 0, st>>>(F, ar, p, tb);
+    else if (G == 4)
+      xdrop_level_resume_group_kernel<4, false, true><<<gg, 128, 0, st>>>(F, ar, p, tb);
+    else if (G == 8 && codes)
+      xdrop_level_resume_group_kernel<8, true, true><<<gg, 128, 0, st>>>(F, ar, p, tb);
+    else if (G == 8)
+      xdrop_level_resume_group_kernel<8, false, true><<<gg, 128, 0, st>>>(F, ar, p, tb);
+    else if (codes)
+      xdrop_level_resume_group_kernel<16, true, true><<<gg, 128, 0, st>>>(F, ar, p, tb);
     else
-      xdrop_level_flat_kernel<20><<<(int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * flat_blocks_per_sm<20>()),
-                                    128, 0, st>>>(L, ar, p, tb);
+      xdrop_level_resume_group_kernel<16, false, true><<<gg, 128, 0, st>>>(F, ar, p, tb);
+    return 1;
+  }
+  if (flat_level) {  // register band, row-interleaved: one resident wave of blocks, then the handed-off passes
+    auto flat_grid = [&](int per_sm) {
+      return (int)std::min<int64_t>((n_bound + 127) / 128, (int64_t)nsm * per_sm);
+    };
+    if (w <= 10 && codes)
+      xdrop_level_flat_kernel<10, true><<<flat_grid(flat_blocks_per_sm<10, true>()), 128, 0, st>>>(L, ar, p, tb);
+    else if (w <= 10)
+      xdrop_level_flat_kernel<10, false><<<flat_grid(flat_blocks_per_sm<10, false>()), 128, 0, st>>>(L, ar, p, tb);
+    else if (codes)
+      xdrop_level_flat_kernel<20, true><<<flat_grid(flat_blocks_per_sm<20, true>()), 128, 0, st>>>(L, ar, p, tb);
+    else
+      xdrop_level_flat_kernel<20, false><<<flat_grid(flat_blocks_per_sm<20, false>()), 128, 0, st>>>(L, ar, p, tb);
     if (!handoff) return 1;
-    if (H.lanes == 8)
-      xdrop_level_resume_group_kernel<8>
-          <<<(int)std::min<int64_t>((H.cap + 15) / 16, (int64_t)nsm * 16), 128, 0, st>>>(L, ar, p, tb);
+    if (H.lanes == 4 && codes)
+      xdrop_level_resume_group_kernel<4, true, false><<<group_grid(4, H.cap), 128, 0, st>>>(L, ar, p, tb);
+    else if (H.lanes == 4)
+      xdrop_level_resume_group_kernel<4, false, false><<<group_grid(4, H.cap), 128, 0, st>>>(L, ar, p, tb);
+    else if (H.lanes == 8 && codes)
+      xdrop_level_resume_group_kernel<8, true, false><<<group_grid(8, H.cap), 128, 0, st>>>(L, ar, p, tb);
+    else if (H.lanes == 8)
+      xdrop_level_resume_group_kernel<8, false, false><<<group_grid(8, H.cap), 128, 0, st>>>(L, ar, p, tb);
+    else if (H.lanes == 16 && codes)
+      xdrop_level_resume_group_kernel<16, true, false><<<group_grid(16, H.cap), 128, 0, st>>>(L, ar, p, tb);
     else if (H.lanes == 16)
-      xdrop_level_resume_group_kernel<16>
-          <<<(int)std::min<int64_t>((H.cap + 7) / 8, (int64_t)nsm * 16), 128, 0, st>>>(L, ar, p, tb);
+      xdrop_level_resume_group_kernel<16, false, false><<<group_grid(16, H.cap), 128, 0, st>>>(L, ar, p, tb);
     else
       xdrop_level_resume_kernel<<<(int)std::min<int64_t>((H.cap + 3) / 4, (int64_t)nsm * 16), 128, 0, st>>>(L, ar, p,
                                                                                                            tb);

@@ -13,6 +13,7 @@ from dcns_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 KERNEL_KNOBS = [
+    {"DCNS_XDROP_RESUME_LANES": "4"},
     {"DCNS_XDROP_RESUME_LANES": "16"},
     {"DCNS_XDROP_RESUME_LANES": "32"},
     {"DCNS_XDROP_HANDOFF": "0"},
@@ -23,6 +24,10 @@ KERNEL_KNOBS = [
     {"DCNS_SG_FLOW": "0"},
     {"DCNS_SG_FLOW_BLOCKS": "6"},
     {"DCNS_SCAN_TILES": "16"},
+    {"DCNS_XDROP_GROUP_FROM": "20"},
+    {"DCNS_XDROP_GROUP_FROM": "10"},
+    {"DCNS_XDROP_GROUP_FROM": "10", "DCNS_XDROP_RESUME_LANES": "4"},
+    {"DCNS_XDROP_GROUP_FROM": "20", "DCNS_XDROP_RESUME_LANES": "16"},
 ]
 BIN_KNOBS = [
     {"DCNS_BINS_BY_SIZE": "1", "DCNS_BIN_RATIO": "1.6"},
