@@ -687,12 +687,14 @@ __global__ void __launch_bounds__(128) xdrop_level_warp_kernel(XLevelArgs L, Are
 constexpr int kXwMaxW = 256;
 
 // The pass resumes at row r_begin: bM / bF hold row r_begin - 1 by band index (row 0: every cell kOut), and the
-// running maximum, its cell and the rows evaluated so far are (score, e1, e2, rows).
-__device__ void xdrop_wave_pass(XTask &T, const Arena &ar, const Params &P, uint32_t *__restrict__ tb,
-                                int32_t *__restrict__ bM, int32_t *__restrict__ bF, int64_t tb_off, int32_t tb_cap,
-                                int lane, int r_begin, int score, int e1, int e2, int rows) {
+// running maximum, its cell and the rows evaluated so far are (score, e1, e2, rows).  CODES = false (forward passes)
+// leaves out the direction codes and their comparisons.
+template <bool CODES>
+__device__ void xdrop_wave_pass_t(XTask &T, const Arena &ar, const Params &P, uint32_t *__restrict__ tb,
+                                  int32_t *__restrict__ bM, int32_t *__restrict__ bF, int64_t tb_off, int32_t tb_cap,
+                                  int lane, int r_begin, int score, int e1, int e2, int rows) {
   const int w = T.w, n1 = T.n1, n2 = T.n2, nk = 2 * w + 1, wpr = xd_words_per_row(w);
-  const bool codes = T.want_codes != 0;
+  const bool codes = CODES && T.want_codes != 0;
   const SeqView s1{T.base1, T.a1, T.dir}, s2{T.base2, T.a2, T.dir};
   const int open = P.open1, ext = P.ext1;
   __syncwarp();
@@ -701,8 +703,11 @@ __device__ void xdrop_wave_pass(XTask &T, const Arena &ar, const Params &P, uint
   for (int r0 = r_begin; r0 <= n1 && !stop; r0 += 32) {
     const int i = r0 + lane;
     const bool live = i <= n1;
-    const int c0 = max(i - w, 1), c1 = min(i + w, n2);
+    const int c1 = min(i + w, n2);
     const int ci = live ? s1.at(ar, i - 1) : 0;
+    // k in [0, 2w] puts j = i - w + k in [i - w, i + w], so the band test is 1 <= j <= n2: j - 1 unsigned below un2
+    // (0 for a row past the pass: no cell)
+    const unsigned un2 = live ? (unsigned)n2 : 0u;
     const bool wcode = codes && live && (int64_t)i * wpr <= tb_cap;  // rows past the slot are never kept
     uint32_t *row_codes = tb + tb_off + (int64_t)(i - 1) * wpr;
     int e = kOut, best = 0, bestj = -1, outM = kOut, outF = kOut, outC = 0, prevUp = kOut, kw = 0;
@@ -720,31 +725,26 @@ __device__ void xdrop_wave_pass(XTask &T, const Arena &ar, const Params &P, uint
         cj = (j >= 1 && j <= n2) ? s2.at(ar, j - 1) : 0;
       }
       int nM = kOut, nF = kOut;
-      if (k >= 0 && k < nk) {
+      if ((unsigned)k < (unsigned)nk) {
         uint32_t nib = 0xFu;
-        if (live && j >= c0 && j <= c1) {
+        if ((unsigned)(j - 1) < un2) {
           const int32_t diag = (j == 1) ? (i == 1 ? 0 : kOut) : diagv;
           const int32_t fin = (j == c1) ? kOut : upF;
-          int32_t v = score_of(ci, cj, P.match, P.mismatch) + diag;
-          uint32_t d = v > fin ? 0u : 1u;
-          if (!(v > fin)) v = fin;
-          if (!(v > e)) {
-            d = 2u;
-            v = e;
-          }
+          const int32_t sd = score_of(ci, cj, P.match, P.mismatch) + diag;
+          const int32_t A = sd > fin ? sd : fin;
+          const bool ge = !(A > e);  // the horizontal gap wins ties
+          const int32_t v = ge ? e : A;
           if (v > best) {
             best = v;
             bestj = j;
           }
           const int32_t h = v + open;
           const int32_t f = fin + ext;
-          if (f >= h) d |= 4u;
           nM = v;
           nF = f >= h ? f : h;
-          e += ext;
-          if (e >= h) d |= 8u;
-          e = e >= h ? e : h;
-          nib = d;
+          const int32_t ee = e + ext;
+          if constexpr (CODES) nib = (ge ? 2u : (sd > fin ? 0u : 1u)) | (f >= h ? 4u : 0u) | (ee >= h ? 8u : 0u);
+          e = ee >= h ? ee : h;
           if (lane == 31) {
             bM[k] = nM;
             bF[k] = nF;
@@ -801,6 +801,16 @@ __device__ void xdrop_wave_pass(XTask &T, const Arena &ar, const Params &P, uint
       T.end2 = e2;
     }
   }
+}
+
+__device__ __forceinline__ void xdrop_wave_pass(XTask &T, const Arena &ar, const Params &P, uint32_t *__restrict__ tb,
+                                                int32_t *__restrict__ bM, int32_t *__restrict__ bF, int64_t tb_off,
+                                                int32_t tb_cap, int lane, int r_begin, int score, int e1, int e2,
+                                                int rows) {
+  if (T.want_codes)
+    xdrop_wave_pass_t<true>(T, ar, P, tb, bM, bF, tb_off, tb_cap, lane, r_begin, score, e1, e2, rows);
+  else
+    xdrop_wave_pass_t<false>(T, ar, P, tb, bM, bF, tb_off, tb_cap, lane, r_begin, score, e1, e2, rows);
 }
 
 __global__ void __launch_bounds__(128) xdrop_level_wave_kernel(XLevelArgs L, Arena ar, Params P,
