@@ -143,7 +143,7 @@ class Tuning(C.Structure):
                 ("n_bins_tuned", C.c_int32),
                 ("xdrop_warp_from", C.c_int32 * 16), ("xdrop_wave_max_w", C.c_int32 * 16), ("xdrop_flat", C.c_int32 * 16),
                 ("xdrop_handoff", C.c_int32 * 16), ("xdrop_resume_lanes", C.c_int32 * 16),
-                ("xdrop_group_from", C.c_int32 * 16)]
+                ("xdrop_group_from", C.c_int32 * 16), ("scan_tiles", C.c_int32 * 16)]
 
     def as_dict(self):
         n = max(self.n_bins_tuned, 1)
@@ -155,7 +155,8 @@ class Tuning(C.Structure):
                                    "row_interleaved": bool(self.xdrop_flat[b]),
                                    "handoff_rows": self.xdrop_handoff[b],
                                    "handoff_lanes": self.xdrop_resume_lanes[b],
-                                   "groups_from_band": self.xdrop_group_from[b]} for b in range(n)]}
+                                   "groups_from_band": self.xdrop_group_from[b],
+                                   "scan_tiles": self.scan_tiles[b]} for b in range(n)]}
 
 
 class Results(C.Structure):

@@ -495,6 +495,7 @@ int dcns_get_tuning(const dcns_ctx *ctx, dcns_tuning *out) {
     out->xdrop_handoff[b] = own ? C.bin_tune[b].xdrop_handoff : C.xdrop_handoff;
     out->xdrop_resume_lanes[b] = own ? C.bin_tune[b].xdrop_resume_lanes : C.xdrop_resume_lanes;
     out->xdrop_group_from[b] = own ? C.bin_tune[b].xdrop_group_from : C.xdrop_group_from;
+    out->scan_tiles[b] = own ? C.bin_tune[b].scan_tiles : C.scan_tiles_per_thread;
   }
   return DCNS_OK;
 }

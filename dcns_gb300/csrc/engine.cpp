@@ -2142,14 +2142,15 @@ void autotune(Context &C, Batch &B, const Params &P, int mode) {
   // each candidate applied to every bin; the bins differ in how many long and wide-band passes they hold.
   C.bin_tune.clear();
   if (C.max_lanes > 1 && (int64_t)B.lens.size() >= 4096) {
-    const int h = C.xdrop_handoff, g = C.xdrop_resume_lanes, gf = C.xdrop_group_from;
+    const int h = C.xdrop_handoff, g = C.xdrop_resume_lanes, gf = C.xdrop_group_from, ts = C.scan_tiles_per_thread;
     // the first candidate is the context's setting (the incumbent)
     const Context::BinTune cands[] = {
-        {C.xdrop_warp_from, C.xdrop_wave_max_w, C.xdrop_flat, h, g, gf},
-        {20, 256, false, 0, g, 0}, {10, 256, true, h, g, gf},   {20, 256, true, 0, g, 0},   {20, 256, true, 48, g, gf},
-        {20, 256, true, 192, g, gf}, {20, 256, true, 48, 32, 0}, {20, 256, true, 96, 32, 0}, {20, 128, true, h, g, gf},
-        {20, 256, true, h, 4, gf},  {20, 256, true, 48, 4, gf}, {20, 256, true, h, g, 20},   {20, 256, true, 48, g, 20},
-        {20, 256, true, h, 4, 20},  {20, 256, true, h, g, 10}};
+        {C.xdrop_warp_from, C.xdrop_wave_max_w, C.xdrop_flat, h, g, gf, ts},
+        {20, 256, false, 0, g, 0, ts},    {10, 256, true, h, g, gf, ts},   {20, 256, true, 0, g, 0, ts},
+        {20, 256, true, 48, g, gf, ts},   {20, 256, true, 192, g, gf, ts}, {20, 256, true, 48, 32, 0, ts},
+        {20, 256, true, 96, 32, 0, ts},   {20, 128, true, h, g, gf, ts},   {20, 256, true, h, 4, gf, ts},
+        {20, 256, true, 48, 4, gf, ts},   {20, 256, true, h, g, 20, ts},   {20, 256, true, 48, g, 20, ts},
+        {20, 256, true, h, 4, 20, ts},    {20, 256, true, h, g, 10, ts}};
     const int nb = std::max(C.bins, C.max_lanes);
     std::vector<double> best_ms(nb, 1e300);
     std::vector<Context::BinTune> choice(nb, cands[0]);
@@ -2167,17 +2168,36 @@ void autotune(Context &C, Batch &B, const Params &P, int mode) {
   }
   // the scan's tiling target (tiles per resident thread before reference rows are split into chunks; it matters
   // for batches of few long pairs) and, on the 2-gap path, the 2-piece kernel's warps per DP: by whole-call time
+  // (for the whole call, and per bin by that bin's seed-scan kernel time over the same runs)
   {
     const int t0 = C.scan_tiles_per_thread;
+    const int nb = (int)C.bin_tune.size();
+    std::vector<double> bin_best(nb, 1e300);
+    auto timed = [&](int t) {  // best of three calls with every bin at target t; each bin's fastest scan time
+      C.scan_tiles_per_thread = t;
+      for (auto &bt : C.bin_tune) bt.scan_tiles = t;
+      std::vector<double> bms(nb, 1e300);
+      double ms = 1e300;
+      for (int r = 0; r < 3; ++r) {
+        ms = std::min(ms, run(best));
+        for (int b = 0; b < nb && b < (int)C.last_bin_scan_ms.size(); ++b)
+          bms[b] = std::min(bms[b], C.last_bin_scan_ms[b]);
+      }
+      return std::make_pair(ms, bms);
+    };
+    std::vector<int> bin_t(nb, t0);
+    auto [best_t_ms, bms0] = timed(t0);
     int best_t = t0;
-    double best_t_ms = best_of3(best);
+    bin_best = bms0;
     for (int t : {4, 8, 16}) {
       if (t == t0) continue;
-      C.scan_tiles_per_thread = t;
-      const double ms = best_of3(best);
+      const auto [ms, bms] = timed(t);
       if (better(ms, best_t_ms)) best_t_ms = ms, best_t = t;
+      for (int b = 0; b < nb; ++b)
+        if (better(bms[b], bin_best[b])) bin_best[b] = bms[b], bin_t[b] = t;
     }
     C.scan_tiles_per_thread = best_t;
+    for (int b = 0; b < nb; ++b) C.bin_tune[b].scan_tiles = bin_t[b];
   }
   if (mode == DCNS_MODE_TWO_GAP) {
     // the stripe flow with 5 or 6 blocks per SM (-5, -6 below), or one CTA per DP with 2, 4 or 8 warps (0: by the
@@ -2282,7 +2302,7 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
   std::vector<std::string> errs(nl);
   std::vector<int> codes(nl, 0);
   std::vector<dcns_stats> st(nl, dcns_stats{});
-  std::vector<double> bin_xdrop_ms(kBins, 0.0);
+  std::vector<double> bin_xdrop_ms(kBins, 0.0), bin_scan_ms(kBins, 0.0);
   auto worker = [&](int l) {
     Context &L = *C.lanes[l];
     try {
@@ -2312,14 +2332,15 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
         const Context::BinTune bt = b < (int)C.bin_tune.size()
                                         ? C.bin_tune[b]
                                         : Context::BinTune{C.xdrop_warp_from, C.xdrop_wave_max_w, C.xdrop_flat,
-                                                           C.xdrop_handoff, C.xdrop_resume_lanes, C.xdrop_group_from};
+                                                           C.xdrop_handoff, C.xdrop_resume_lanes, C.xdrop_group_from,
+                                                           C.scan_tiles_per_thread};
         L.xdrop_warp_from = bt.xdrop_warp_from, L.xdrop_wave_max_w = bt.xdrop_wave_max_w, L.xdrop_flat = bt.xdrop_flat;
         L.xdrop_handoff = bt.xdrop_handoff, L.xdrop_resume_lanes = bt.xdrop_resume_lanes;
         L.xdrop_group_from = bt.xdrop_group_from;
         L.sg_warps = C.sg_warps;
         L.sg_flow = C.sg_flow;
         L.sg_flow_blocks = C.sg_flow_blocks;
-        L.scan_tiles_per_thread = C.scan_tiles_per_thread;
+        L.scan_tiles_per_thread = bt.scan_tiles;
         L.call_t0 = C.call_t0;
         L.lane_id = l;
         L.trace = C.trace;
@@ -2332,6 +2353,7 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
         pass.failed = false;
         for (size_t k = 0; k < ids.size(); ++k) out[ids[k]] = std::move(so[k]);
         bin_xdrop_ms[b] = L.stats.ms_xdrop_kernel;
+        bin_scan_ms[b] = L.stats.ms_scan_kernel;
         add_stats(st[l], L.stats);
       }
     } catch (const Error &e) {
@@ -2351,6 +2373,7 @@ void align_core(Context &C, const std::vector<PairIn> &pairs, const Params &P, i
     if (codes[l]) throw Error(codes[l], errs[l]);
   for (int l = 0; l < nl; ++l) add_stats(C.stats, st[l]);
   C.last_bin_xdrop_ms = std::move(bin_xdrop_ms);
+  C.last_bin_scan_ms = std::move(bin_scan_ms);
 }
 
 void align_single(Context &C, const std::vector<PairIn> &pairs, const Params &P, int mode,

@@ -145,14 +145,17 @@ struct Context {
   // seed-scan tiling target: reference rows are split into chunks while a launch has fewer tiles than this many per
   // resident thread (DCNS_SCAN_TILES)
   int scan_tiles_per_thread = 8;
-  // per-bin x-drop pass forms chosen by the autotuner (empty: the values above for every bin)
+  // per-bin x-drop pass forms and seed-scan tiling target chosen by the autotuner (empty: the values above for every
+  // bin)
   struct BinTune {
     int xdrop_warp_from, xdrop_wave_max_w;
     bool xdrop_flat;
     int xdrop_handoff, xdrop_resume_lanes, xdrop_group_from;
+    int scan_tiles;
   };
   std::vector<BinTune> bin_tune;
   std::vector<double> last_bin_xdrop_ms;  // x-drop kernel time of each bin of the last binned call
+  std::vector<double> last_bin_scan_ms;   // seed-scan kernel time of each bin of the last binned call
   // Level-0 turnstile of one binned call: the bins enqueue their level-0 scans on the parent's bulk stream in bin
   // order, so the scans run one after another and the first bins' host work overlaps the later bins' scans.
   struct Turnstile {

@@ -198,6 +198,7 @@ typedef struct {
   int32_t n_bins_tuned;           /* bins with their own x-drop forms below (0: every bin uses bin 0's values) */
   int32_t xdrop_warp_from[16], xdrop_wave_max_w[16], xdrop_flat[16], xdrop_handoff[16], xdrop_resume_lanes[16];
   int32_t xdrop_group_from[16]; /* register-band levels of this band and wider: every pass on lane groups (0: off) */
+  int32_t scan_tiles[16];       /* each bin's seed-scan tiling target */
 } dcns_tuning;
 int dcns_get_tuning(const dcns_ctx *ctx, dcns_tuning *out);
 
